@@ -1,0 +1,436 @@
+"""Benchmark of the batched split-step BPM march on GB300.
+
+Workload (one step = one pass of the hot path over one batch): 64 illumination plane
+waves, tilts drawn area-uniformly inside NA 0.8, marched through one shared 512x512x256
+dn volume (seeded Gaussian random field, correlation length 5 px, sigma 0.02, clipped to
++-0.06), dx = dz = 0.1 um, lambda 0.5 um, n0 1.33, mean_mode "weighted" (bpm_3d's
+default), complex64 field, |u|^2 volume output (64 x 256 x 512 x 512 float32). Inputs are
+synthetic and seeded. Metric: voxel-updates/s, one voxel-update = one (x, y) point of one
+field advanced one z-step (Nx*Ny*(Nz-1) per field).
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+
+Prints one JSON line. `value` is device throughput with inputs resident in HBM (captured
+CUDA graph, timed with CUDA events); `e2e` is the same through the public API
+bpm_gb300.bpm_3d_batched with host buffers (pinned), H2D of u0 and dn and D2H of the
+volume inside the timed region; `plain` is the single-request path (one field per call).
+--impl reference times the CPU restatement of the reference's algorithm (numpy/scipy,
+FP32, all host cores) on a bounded sample of the same workload.
+"""
+import argparse
+import ctypes
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+NX = NY = 512
+NZ = 256
+BATCH = 64
+UNITS = (.1, .1, .1)
+LAM = .5
+N0 = 1.33
+MODE = "weighted"
+SEED = 0
+
+
+def env_int(k, d):
+    try:
+        return int(os.environ.get(k, d))
+    except ValueError:
+        return d
+
+
+def host_cores():
+    try:
+        return len(os.sched_getaffinity(0))
+    except AttributeError:
+        return os.cpu_count() or 1
+
+
+def make_u0(batch, nx, ny, seed):
+    rng = np.random.default_rng(seed)
+    r = .8 * np.sqrt(rng.uniform(0, 1, batch))
+    th = 2 * np.pi * rng.uniform(0, 1, batch)
+    k0 = 2 * np.pi / LAM
+    kx, ky = k0 * r * np.cos(th), k0 * r * np.sin(th)
+    x = UNITS[0] * np.arange(nx)
+    y = UNITS[1] * np.arange(ny)
+    return np.exp(-1j * (kx[:, None, None] * x[None, None, :] + ky[:, None, None] * y[None, :, None])
+                  ).astype(np.complex64)
+
+
+def make_dn_device(nx, ny, nz, seed, corr=5., sigma=.02, clip=.06):
+    """Gaussian-filtered white noise, generated on the device (input synthesis only)."""
+    import torch
+    g = torch.Generator(device="cuda").manual_seed(seed)
+    w = torch.randn((nz, ny, nx), device="cuda", generator=g)
+    fz = torch.fft.fftfreq(nz, device="cuda")[:, None, None]
+    fy = torch.fft.fftfreq(ny, device="cuda")[None, :, None]
+    fx = torch.fft.fftfreq(nx, device="cuda")[None, None, :]
+    k = torch.exp(-2 * np.pi ** 2 * corr ** 2 * (fx ** 2 + fy ** 2 + fz ** 2))
+    f = torch.fft.ifftn(torch.fft.fftn(w) * k).real
+    f = f * (sigma / f.std())
+    return f.clamp_(-clip, clip).float().contiguous()
+
+
+class ClockSampler:
+    """nvidia-smi clocks and throttle reasons sampled during the timed region."""
+    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+         "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+         "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index):
+        self.index = index
+        self.proc = None
+        self.lines = []
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.index), "--query-gpu=" + self.Q,
+                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.t = threading.Thread(target=self._read, daemon=True)
+            self.t.start()
+        except OSError:
+            self.proc = None
+        return self
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def __exit__(self, *a):
+        if self.proc is not None:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+            self.t.join(timeout=2)
+
+    def summary(self):
+        sm, smax, reasons = [], None, set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in self.lines:
+            f = [v.strip() for v in ln.split(",")]
+            if len(f) < 9:
+                continue
+            try:
+                sm.append(float(f[1]))
+                smax = float(f[2])
+            except ValueError:
+                continue
+            for n, v in zip(names, f[5:9]):
+                if v.lower().startswith("active"):
+                    reasons.add(n)
+        if not sm:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": [], "samples": 0}
+        return {"sm_mhz": statistics.median(sm), "sm_max_mhz": smax, "reasons": sorted(reasons),
+                "samples": len(sm)}
+
+
+def peaks():
+    p = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(p):
+        d = json.load(open(p))
+        return float(d["hbm_gbs"]), "measured"
+    return 6800., "fallback"
+
+
+def fp32_peak_tflops(sm_mhz):
+    """FP32 CUDA-core peak: 152 SMs x 128 FMA lanes x 2 flop x clock (no measured figure
+    exists for the FP32 pipe; this is the nominal formula at the sampled median clock)."""
+    mhz = sm_mhz or 2070.
+    return 152 * 128 * 2 * mhz * 1e6 / 1e12
+
+
+def bench_ours(args, rank, world, local_rank):
+    import torch
+    import bpm_gb300
+    from bpm_gb300 import _native as N
+    from bpm_gb300.bpm3d import _ptr
+
+    torch.cuda.set_device(local_rank)
+    dev = torch.device("cuda", local_rank)
+    units_per_step = BATCH * NX * NY * (NZ - 1)
+
+    dn = make_dn_device(NX, NY, NZ, SEED)
+    u0 = torch.from_numpy(make_u0(BATCH, NX, NY, SEED + 1)).to(dev)
+    march = bpm_gb300.BatchedMarch((NX, NY, NZ), UNITS, LAM, N0, BATCH, dn=dn, mean_mode=MODE,
+                                   out_kind="intensity", group=args.group)
+    march.u0.copy_(u0)
+    stream = torch.cuda.current_stream()
+
+    def barrier():
+        if world > 1:
+            torch.distributed.barrier()
+        torch.cuda.synchronize()
+
+    for _ in range(args.warmup):
+        march.run()
+    barrier()
+    l0 = bpm_gb300.launch_count()
+    ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    with ClockSampler(local_rank) as clk:
+        ev0.record(stream)
+        for _ in range(args.steps):
+            march.run()
+        ev1.record(stream)
+        barrier()
+    launches = bpm_gb300.launch_count() - l0
+    t_ms = ev0.elapsed_time(ev1) / args.steps
+    if world > 1:
+        t = torch.tensor([t_ms], device=dev)
+        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+        t_ms = float(t.item())
+    value = world * units_per_step / (t_ms * 1e-3)
+    clocks = clk.summary()
+
+    # per-kernel times of one group (CUDA events around single passes)
+    req, ws, wsb = march.req, march.ws, march.ws_bytes
+    L = N.lib()
+    grp = args.group if args.group > 0 else default_group(NX, BATCH)
+
+    def time_pass(kind, z, reps=20):
+        for _ in range(3):
+            N.check(L.bpm_launch_pass(march.plan.handle, ctypes.byref(req), _ptr(ws), wsb, kind, z,
+                                      ctypes.c_void_p(stream.cuda_stream)))
+        a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        a.record(stream)
+        for r in range(reps):
+            N.check(L.bpm_launch_pass(march.plan.handle, ctypes.byref(req), _ptr(ws), wsb, kind,
+                                      z + (r % 8 if z + 9 < NZ else 0), ctypes.c_void_p(stream.cuda_stream)))
+        b.record(stream)
+        torch.cuda.synchronize()
+        return a.elapsed_time(b) / reps
+
+    zmid = max(1, min(100, NZ - 2))
+    t_row = time_pass(N.PASS_ROW, zmid)
+    t_cr = time_pass(N.PASS_COLUMN_REDUCE, zmid)
+    t_cp = time_pass(N.PASS_COLUMN_PROPAGATE, zmid)
+    groups = -(-BATCH // grp)
+    t_step_sum = groups * (NZ - 1) * (t_row + t_cr + t_cp)
+    hbm_peak, peak_kind = peaks()
+    vox = grp * NX * NY
+    # algorithmic bytes of one row pass over a group: the dn slice once, the |u|^2 plane per
+    # field, and the field in/out once per request spread over the nz-1 steps
+    row_bytes = NX * NY * 4 + vox * 4 + vox * 16. / (NZ - 1)
+    row_gbs = row_bytes / (t_row * 1e-3) / 1e9
+    log2n = int(np.log2(NX))
+    row_flops = vox * (2 * 5 * log2n + 12)           # inverse + forward row FFT, mask, |u|^2
+    col_flops = vox * (2 * 5 * int(np.log2(NY)) + 8)  # forward + inverse column FFT, propagator
+    fp32_peak = fp32_peak_tflops(clocks.get("sm_mhz"))
+    traffic = profile_traffic()
+
+    # plain: one field per request through the same library, no graph
+    plain = bpm_gb300.BatchedMarch((NX, NY, NZ), UNITS, LAM, N0, 1, dn=dn, mean_mode=MODE,
+                                   out_kind="intensity", use_graph=False)
+    plain.u0.copy_(u0[:1])
+    for _ in range(2):
+        plain.run()
+    torch.cuda.synchronize()
+    n_plain = max(2, min(8, args.steps))
+    a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    a.record(stream)
+    for _ in range(n_plain):
+        plain.run()
+    b.record(stream)
+    torch.cuda.synchronize()
+    t_plain = a.elapsed_time(b) / n_plain
+    plain_value = NX * NY * (NZ - 1) / (t_plain * 1e-3)
+    same = bool(torch.equal(plain.out[0], march.out[0]))
+    del plain
+
+    # e2e through the public API with pinned host buffers
+    u0_h = torch.from_numpy(make_u0(BATCH, NX, NY, SEED + 1)).pin_memory()
+    dn_h = torch.empty(dn.shape, dtype=torch.float32, pin_memory=True)
+    dn_h.copy_(dn)
+    out_h = torch.empty((BATCH, NZ, NY, NX), dtype=torch.float32, pin_memory=True)
+    del march
+    torch.cuda.empty_cache()
+    e2e_steps = max(1, min(args.steps, 3))
+    for _ in range(1):
+        bpm_gb300.bpm_3d_batched((NX, NY, NZ), UNITS, lam=LAM, u0=u0_h, dn=dn_h, n0=N0, return_field=False,
+                                 mean_mode=MODE, group=args.group, out=out_h)
+    barrier()
+    t0 = time.perf_counter()
+    for _ in range(e2e_steps):
+        bpm_gb300.bpm_3d_batched((NX, NY, NZ), UNITS, lam=LAM, u0=u0_h, dn=dn_h, n0=N0, return_field=False,
+                                 mean_mode=MODE, group=args.group, out=out_h)
+    barrier()
+    t_e2e = (time.perf_counter() - t0) / e2e_steps
+    if world > 1:
+        t = torch.tensor([t_e2e], device=dev)
+        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+        t_e2e = float(t.item())
+    e2e = {"value": world * units_per_step / t_e2e, "unit": "voxel-updates/s",
+           "h2d_bytes_per_step": int(u0_h.numel() * 8 + dn_h.numel() * 4),
+           "d2h_bytes_per_step": int(out_h.numel() * 4), "ms_per_step": t_e2e * 1e3,
+           "api": "bpm_gb300.bpm_3d_batched (pinned host u0/dn/out)"}
+
+    res = {
+        "metric": "BPM voxel-updates/s, batched (64 fields, 512x512x256, |u|^2 volume)",
+        "value": value, "unit": "voxel-updates/s", "n_gpus": world, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": t_ms, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "c64", "data": "synthetic (seeded)",
+        "config": {"workload": "batched_64x512x512x256_weighted", "nx": NX, "ny": NY, "nz": NZ,
+                   "batch_per_gpu": BATCH, "units_um": UNITS, "lam_um": LAM, "n0": N0,
+                   "mean_mode": MODE, "output": "intensity volume", "group": grp,
+                   "dn": "gaussian random field corr 5 px sigma 0.02 clip 0.06 (shared)",
+                   "u0": "64 plane waves, tilts area-uniform in NA 0.8",
+                   "l2": "inputs larger than L2 (dn 256 MiB, output 16 GiB per step)",
+                   "parallelism": "replicas" if world > 1 else "single GPU",
+                   "graph": "one CUDA graph per step"},
+        "e2e": e2e,
+        "gpu_launches": int(launches),
+        "plain": {"value": plain_value, "unit": "voxel-updates/s", "ms_per_request": t_plain,
+                  "config": "one field per request, 512x512x256, no graph", "same_result_as_batched": same},
+        "batched_over_plain": value / world / plain_value,
+        "kernels_ms": {"row_pass": t_row, "col_fwd_reduce": t_cr, "col_inv": t_cp,
+                       "per_launch_group_fields": grp, "sum_over_step_ms": t_step_sum},
+        "roofline": {"bound": "hbm", "kernel": "row_pass_kernel<512>", "achieved": row_gbs,
+                     "peak": hbm_peak, "unit": "GB/s", "frac": row_gbs / hbm_peak,
+                     "traffic": traffic, "peak_kind": peak_kind + " (MEASURED_PEAKS.json hbm_gbs)",
+                     "algorithmic_bytes_per_launch": row_bytes,
+                     "fp32": {"row_pass_tflops": row_flops / (t_row * 1e-3) / 1e12,
+                              "col_pass_tflops": col_flops / ((t_cr + t_cp) * 1e-3) / 1e12,
+                              "peak_tflops_nominal": fp32_peak,
+                              "row_frac": row_flops / (t_row * 1e-3) / 1e12 / fp32_peak,
+                              "note": "FFT flops counted as 5 N log2 N per 1-D transform"}},
+        "clocks": clocks,
+    }
+    return res
+
+
+def profile_run(args):
+    """The device march alone (same buffers as the timed region), for ncu captures."""
+    import torch
+    import bpm_gb300
+    torch.cuda.set_device(0)
+    dn = make_dn_device(NX, NY, NZ, SEED)
+    march = bpm_gb300.BatchedMarch((NX, NY, NZ), UNITS, LAM, N0, BATCH, dn=dn, mean_mode=MODE,
+                                   out_kind="intensity", group=args.group)
+    march.u0.copy_(torch.from_numpy(make_u0(BATCH, NX, NY, SEED + 1)).cuda())
+    for _ in range(args.warmup + args.steps):
+        march.run()
+    torch.cuda.synchronize()
+    print(json.dumps({"profile_run": True, "batch": BATCH, "nz": NZ, "launches": bpm_gb300.launch_count()}))
+
+
+def default_group(nx, batch):
+    plane = nx * nx * 8
+    g_l2 = max(1, (48 << 20) // plane)
+    g_fill = max(1, (152 * 4) // max(1, nx // 16))
+    return max(1, min(min(g_l2, g_fill), batch))
+
+
+def profile_traffic():
+    """DRAM bytes per row-pass launch from the committed ncu summary, if one exists."""
+    p = os.path.join(ROOT, "profiles", "row_pass_512_traffic.json")
+    if os.path.exists(p):
+        try:
+            return float(json.load(open(p))["dram_bytes_per_launch"])
+        except (KeyError, ValueError):
+            return None
+    return None
+
+
+def cpu_sample(fields=1, steps=48):
+    """The CPU restatement of the reference's march (oracle, FP32, scipy.fft with all host
+    cores) on a bounded sample of the workload: `fields` fields x `steps` z-steps."""
+    from oracle import bpm_ref
+    rng = np.random.default_rng(SEED)
+    dn = (np.clip(rng.normal(0, .02, (steps + 1, NY, NX)), -.06, .06)).astype(np.float32)
+    u0 = make_u0(fields, NX, NY, SEED + 1)
+    t0 = time.perf_counter()
+    for f in range(fields):
+        bpm_ref.bpm_3d((NX, NY, steps + 1), UNITS, lam=LAM, n0=N0, u0=u0[f], dn=dn, mean_mode=MODE,
+                       return_field=False, precision="fp32", workers=host_cores())
+    t = time.perf_counter() - t0
+    units = fields * NX * NY * steps
+    return units / t, t, "%d field(s) x %dx%d x %d z-steps, mean_mode=%s, |u|^2 volume" % (
+        fields, NX, NY, steps, MODE)
+
+
+def bench_reference(args, rank):
+    if rank != 0:
+        return None
+    vals = []
+    for _ in range(args.warmup):
+        cpu_sample(1, 8)
+    for _ in range(args.steps):
+        v, t, sample = cpu_sample(1, 64)
+        vals.append((v, t))
+    v = statistics.median(x[0] for x in vals)
+    t_ms = statistics.median(x[1] for x in vals) * 1e3
+    cores = host_cores()
+    return {"impl": "reference",
+            "metric": "BPM voxel-updates/s, batched (64 fields, 512x512x256, |u|^2 volume)",
+            "value": v, "unit": "voxel-updates/s", "n_gpus": 0, "steps": args.steps, "warmup": args.warmup,
+            "ms_per_step": t_ms, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+            "dtype": "c64", "data": "synthetic (seeded)",
+            "config": {"workload": "batched_64x512x512x256_weighted", "sample": sample},
+            "cpu_baseline": {"value": v, "unit": "voxel-updates/s", "cores": cores, "kind": "port",
+                             "sample": sample + " per step (reference algorithm restated in numpy/scipy "
+                                                "FP32; the reference's OpenCL path cannot run here)"},
+            "e2e": {"value": v, "unit": "voxel-updates/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=5)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--group", type=int, default=0, help="fields per pass (0 = library default)")
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--batch", type=int, default=BATCH, help="fields per GPU (smaller for profiling)")
+    ap.add_argument("--nz", type=int, default=NZ, help="z planes (smaller for profiling)")
+    ap.add_argument("--profile", action="store_true",
+                    help="only the device march (warm-up + steps), for ncu launch lists")
+    args = ap.parse_args()
+    if args.warmup < 3:
+        args.warmup = 3
+    globals()["BATCH"] = args.batch
+    globals()["NZ"] = args.nz
+    if args.profile:
+        profile_run(args)
+        return
+
+    world = env_int("WORLD_SIZE", 1)
+    rank = env_int("RANK", 0)
+    local_rank = env_int("LOCAL_RANK", 0)
+
+    if args.impl == "reference":
+        res = bench_reference(args, rank)
+        if res is not None:
+            print(json.dumps(res))
+        return
+
+    if world > 1:
+        import torch
+        torch.cuda.set_device(local_rank)
+        torch.distributed.init_process_group("nccl")
+    res = bench_ours(args, rank, world, local_rank)
+    if rank == 0:
+        if not args.no_cpu_baseline:
+            v, t, sample = cpu_sample(4, NZ - 1)
+            res["cpu_baseline"] = {"value": v, "unit": "voxel-updates/s", "cores": host_cores(), "kind": "port",
+                                   "sample": sample + ", %.1f s" % t}
+        print(json.dumps(res))
+    if world > 1:
+        import torch
+        torch.distributed.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

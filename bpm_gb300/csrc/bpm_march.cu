@@ -1,0 +1,1015 @@
+// Split-step beam propagation z-march on GB300 (sm_103a).
+//
+// Reference algorithm (per z-step i, bpm/bpm/bpm_3d.py:283-381):
+//   u_hat = FFT2(u)                      (forward, unnormalised)
+//   [weighted] dn0 = sum|u_hat|*dn_slice0 / sum|u_hat|          (bpm_3d.py:302-303)
+//   u_hat *= h(n)                        (mult_propagator*, bpm_3d_kernels.cl:408-493)
+//   u = IFFT2(u_hat)                     (normalised by 1/(nx*ny))
+//   u *= exp(-i k0 dz (dn[i+1]-dn0)) * taper    (mult_dn*, bpm_3d_kernels.cl:20-283)
+//   store u or |u|^2 as plane i+1        (copy_intens, bpm_3d_kernels.cl:396-404)
+//
+// GB300 design. FFT2 = row FFTs (along x) then column FFTs (along y). A z-step is two
+// passes over the field held in a workspace W (one plane per field of the group):
+//   column pass : load 16 full columns, forward column FFT, multiply by the propagator
+//                 (with the 1/(nx*ny) normalisation folded in), inverse column FFT, store.
+//   row pass    : load 16 full rows, inverse row FFT, phase mask of dn slice z with taper,
+//                 write plane z of the output (field or |u|^2), forward row FFT of the next
+//                 step, store.
+// so the forward row FFT of step i+1 is fused with the inverse row FFT and mask of step i
+// and nothing but the field itself makes a round trip between passes. The weighted mean
+// mode needs the plane-wide sums between the forward column FFT and the propagator, so
+// its column pass is split in two (forward FFT + partial sums | propagator + inverse FFT).
+// Many fields (illumination angles, wavelengths) march together: grid.y indexes the
+// field within a group, and a group's planes stay L2-resident between passes while the
+// dn slice is read from HBM once for the whole group.
+#include <algorithm>
+#include <cmath>
+#include <cstring>
+#include <string>
+#include <vector>
+
+#include "common.cuh"
+#include "fft_tile.cuh"
+
+using namespace bpmgb;
+
+static const float PI_F = 3.14159265358979f;  // bpm_3d_kernels.cl:3
+
+struct bpm_plan {
+  bpm_grid_desc d;
+  int device;
+  float2* tw_x;     // W_nx^k
+  float2* tw_y;     // W_ny^k
+  float* kx2;       // (2.f*M_PI*FFTFREQ(i,nx,dx))^2, FP32 recipe
+  float* ky2;
+  float2* H;        // unnormalised propagator table (IGNORE mean mode), (ny, nx)
+  float* taper;     // taper value per distance < absorbing_width
+  float* sw;        // scattering weights cos(theta), (ny, nx)
+  float* gw;        // g-factor weights cos(theta)^2
+  float k0f, dzf, n0f, unit_k;
+  double k0;
+};
+
+struct bpm_exec {
+  cudaGraphExec_t exec;
+  cudaGraph_t graph;
+  unsigned long long launches;
+};
+
+namespace {
+
+// ---------------------------------------------------------------------------------------
+// host-side FP32 recipes (compiled with -ffp-contract=off: every operation rounds as written)
+// ---------------------------------------------------------------------------------------
+float fftfreq_f32(int i, int N, float d) {  // FFTFREQ, bpm_3d_kernels.cl:6
+  int half = (N - 1) / 2 + 1;
+  int num = (i < half) ? i : (i - half) - N / 2;
+  float f = 1.f * (float)num;
+  f = f / (float)N;
+  f = f / d;
+  return f;
+}
+
+float taper_value(int dist, int absorb) {  // bpm_3d_kernels.cl:36
+  float arg = PI_F * (float)dist;
+  arg = arg / (float)absorb;
+  float c = cosf(arg);
+  return 0.5f * (1.f - c);
+}
+
+// ---------------------------------------------------------------------------------------
+// plan tables on the device (FP64 arithmetic)
+// ---------------------------------------------------------------------------------------
+__global__ void build_tables_kernel(int nx, int ny, double dx, double dy, double dz, double n0,
+                                    double k0, float n0f, float k0f, int prop_kind, int fresnel,
+                                    const float* __restrict__ kx2, const float* __restrict__ ky2,
+                                    float2* __restrict__ H, float* __restrict__ sw,
+                                    float* __restrict__ gw) {
+  int x = blockIdx.x * blockDim.x + threadIdx.x;
+  int y = blockIdx.y;
+  if (x >= nx) return;
+  // FP64 k-grid, 2*pi*fftfreq (numpy)
+  const double twopi = 6.283185307179586476925286766559;
+  double fx = (x < (nx + 1) / 2) ? (double)x : (double)(x - nx);
+  double fy = (y < (ny + 1) / 2) ? (double)y : (double)(y - ny);
+  double kx = twopi * fx / (nx * dx);
+  double ky = twopi * fy / (ny * dy);
+  double tmp64 = n0 * n0 * k0 * k0 - kx * kx - ky * ky;
+  bool prop;
+  if (prop_kind == BPM_PROP_FUNCTIONAL) {
+    // evanescent mask of compute_propagator: FP32 recipe, no contraction
+    float nk = __fmul_rn(__fmul_rn(__fmul_rn(n0f, n0f), k0f), k0f);
+    float tmp = __fsub_rn(__fsub_rn(nk, kx2[x]), ky2[y]);
+    prop = tmp >= 0.f;
+  } else {
+    prop = tmp64 >= 0.0;  // host FP64 propagator: NaN where negative
+  }
+  double kz = tmp64 > 0.0 ? sqrt(tmp64) : 0.0;
+  double ph = -dz * kz;
+  double s, c;
+  sincos(ph, &s, &c);
+  H[(size_t)y * nx + x] = prop ? make_float2((float)c, (float)s) : make_float2(0.f, 0.f);
+  // scattering weights (bpm_3d.py:227-244): cos(theta) = real(H0)/n0/k0 with the FP64 host H0
+  double h0 = tmp64 >= 0.0 ? sqrt(tmp64) : 0.0;
+  if (fresnel) h0 = n0 * k0 - .5 * (kx * kx + ky * ky) / n0 / k0;
+  double ct = h0 / n0 / k0;
+  sw[(size_t)y * nx + x] = (float)ct;
+  gw[(size_t)y * nx + x] = (float)(ct * ct);
+}
+
+// ---------------------------------------------------------------------------------------
+// kernels
+// ---------------------------------------------------------------------------------------
+struct RowParams {
+  const float2* src;        // group's input planes (u0 + b0*plane, or W)
+  long long src_bstride;    // float2 elements between fields
+  float2* W;                // group workspace planes
+  int nx, ny, nz, z;        // z = plane produced by this pass
+  int do_inv, do_fwd, do_mask;
+  const void* dn;           // dn of field 0 of the group
+  int dn_dtype;
+  long long dn_bstride;     // elements
+  float unit_k;
+  int absorb;
+  const float* taper;
+  int mean_mode;
+  const float* dn0_field;   // weighted: per group field
+  const float* slice_dn0;   // simple: per slice
+  void* out;                // output of field 0 of the group
+  int out_kind;
+  long long out_bstride;    // elements
+  float2* last_plane;       // group's exit planes or NULL
+  const float* scat_part;   // [G][ntiles][2]
+  int n_ctiles;
+  float* scat_p;            // group's (nz) rows
+  float* scat_g;
+  float prefac_f;
+  const float2* tw;
+};
+
+__device__ __forceinline__ float load_dn_real(const void* dn, int dtype, size_t idx) {
+  if (dtype == BPM_DN_F16) return __half2float(reinterpret_cast<const __half*>(dn)[idx]);
+  return __ldg(reinterpret_cast<const float*>(dn) + idx);
+}
+
+template <int N>
+__global__ void __launch_bounds__(TileCfg<N>::THREADS)
+row_pass_kernel(RowParams p) {
+  constexpr int T = TileCfg<N>::THREADS;
+  constexpr int R = TileCfg<N>::R;
+  extern __shared__ float2 smem[];
+  float2* tile = smem;
+  float2* tw = smem + N * 16;
+  const int tid = threadIdx.x;
+  const int gl = blockIdx.y;
+  const int y0 = blockIdx.x * 16;
+  const size_t plane = (size_t)N * p.ny;
+
+  if (p.do_inv || p.do_fwd)
+    for (int k = tid; k < N; k += T) tw[k] = p.tw[k];
+
+  const float4* s4 = reinterpret_cast<const float4*>(p.src + gl * p.src_bstride + (size_t)y0 * N);
+  for (int e = tid; e < 8 * N; e += T) {
+    const int r = e / (N / 2);
+    const int x = 2 * (e - r * (N / 2));
+    float4 f = s4[e];
+    tile[tile_idx(x, r)] = make_float2(f.x, f.y);
+    tile[tile_idx(x + 1, r)] = make_float2(f.z, f.w);
+  }
+  __syncthreads();
+
+  if (p.do_inv) tile_fft<N, R, true>(tile, tw);
+
+  // mask, outputs
+  float dn0 = 0.f;
+  if (p.mean_mode == BPM_MEAN_WEIGHTED && p.dn0_field) dn0 = p.dn0_field[gl];
+  else if (p.mean_mode == BPM_MEAN_SIMPLE && p.slice_dn0) dn0 = p.slice_dn0[p.z];
+  const bool last = (p.z == p.nz - 1);
+  const size_t zoff = (size_t)p.z * plane;
+  for (int e = tid; e < 8 * N; e += T) {
+    const int r = e / (N / 2);
+    const int x = 2 * (e - r * (N / 2));
+    const int y = y0 + r;
+    const size_t pix = (size_t)y * N + x;
+    float2 v[2] = {tile[tile_idx(x, r)], tile[tile_idx(x + 1, r)]};
+    if (p.do_mask) {
+      if (p.dn_dtype == BPM_DN_C64) {
+        const float4 d = __ldg(reinterpret_cast<const float4*>(
+            reinterpret_cast<const float2*>(p.dn) + gl * p.dn_bstride + zoff + pix));
+        const float dre[2] = {d.x, d.z}, dim[2] = {d.y, d.w};
+#pragma unroll
+        for (int q = 0; q < 2; q++) {
+          float m = expf(p.unit_k * dim[q]);
+          float s, c;
+          sincosf((-p.unit_k) * dre[q], &s, &c);
+          v[q] = cmul(v[q], make_float2(m * c, m * s));
+        }
+      } else {
+        const size_t di = gl * p.dn_bstride + zoff + pix;
+        float dv[2];
+        if (p.dn_dtype == BPM_DN_F16) {
+          __half2 h = *reinterpret_cast<const __half2*>(reinterpret_cast<const __half*>(p.dn) + di);
+          float2 f = __half22float2(h);
+          dv[0] = f.x;
+          dv[1] = f.y;
+        } else {
+          float2 f = __ldg(reinterpret_cast<const float2*>(reinterpret_cast<const float*>(p.dn) + di));
+          dv[0] = f.x;
+          dv[1] = f.y;
+        }
+        const int disty = min(p.ny - 1 - y, y);
+#pragma unroll
+        for (int q = 0; q < 2; q++) {
+          float d = (-p.unit_k) * (dv[q] - dn0);
+          float s, c;
+          sincosf(d, &s, &c);
+          float2 r2 = cmul(v[q], make_float2(c, s));
+          const int xx = x + q;
+          const int dist = min(min(N - 1 - xx, xx), disty);
+          if (dist < p.absorb) {
+            const float a = p.taper[dist];
+            r2.x *= a;
+            r2.y *= a;
+          }
+          v[q] = r2;
+        }
+      }
+      tile[tile_idx(x, r)] = v[0];
+      tile[tile_idx(x + 1, r)] = v[1];
+    }
+    if (p.out_kind == BPM_OUT_FIELD) {
+      float4* o = reinterpret_cast<float4*>(reinterpret_cast<float2*>(p.out) + gl * p.out_bstride + zoff + pix);
+      __stcs(o, make_float4(v[0].x, v[0].y, v[1].x, v[1].y));
+    } else if (p.out_kind == BPM_OUT_INTENSITY) {
+      float2* o = reinterpret_cast<float2*>(reinterpret_cast<float*>(p.out) + gl * p.out_bstride + zoff + pix);
+      __stcs(o, make_float2(cabs2(v[0]), cabs2(v[1])));
+    }
+    if (last && p.last_plane) {
+      float4* o = reinterpret_cast<float4*>(p.last_plane + gl * plane + pix);
+      *o = make_float4(v[0].x, v[0].y, v[1].x, v[1].y);
+    }
+  }
+
+  // scattering sums of this step: finished by one thread of the first block per field
+  if (p.scat_p && blockIdx.x == 0 && tid == 0) {
+    float* prow = p.scat_p + (size_t)gl * p.nz;
+    float* grow = p.scat_g ? p.scat_g + (size_t)gl * p.nz : nullptr;
+    if (p.z == 0) {
+      prow[0] = 0.f;
+      if (grow) grow[0] = __fdiv_rn(0.f, 0.f);
+    } else {
+      const float* part = p.scat_part + (size_t)gl * p.n_ctiles * 2;
+      float S = 0.f, G = 0.f;
+      for (int t = 0; t < p.n_ctiles; t++) {
+        S += part[2 * t];
+        G += part[2 * t + 1];
+      }
+      float pv = p.prefac_f * S;
+      prow[p.z] = pv;
+      if (grow) grow[p.z] = __fdiv_rn(p.prefac_f * G, pv);
+    }
+  }
+
+  if (!p.do_fwd) return;
+  __syncthreads();
+  tile_fft<N, R, false>(tile, tw);
+  float4* d4 = reinterpret_cast<float4*>(p.W + gl * plane + (size_t)y0 * N);
+  for (int e = tid; e < 8 * N; e += T) {
+    const int r = e / (N / 2);
+    const int x = 2 * (e - r * (N / 2));
+    float2 a = tile[tile_idx(x, r)], b = tile[tile_idx(x + 1, r)];
+    d4[e] = make_float4(a.x, a.y, b.x, b.y);
+  }
+}
+
+struct ColParams {
+  float2* W;
+  int nx, ny, nz, z;         // z = step index: the field goes from plane z to z+1
+  int prop_mode;             // 0 = table H, 1 = FP32 recipe with slice_n[z+1], 2 = weighted
+  const float2* H;
+  const float* kx2;
+  const float* ky2;
+  float k0f, dzf, n00f;
+  const float* slice_n;
+  float scale;               // 1/(nx*ny)
+  const void* dn;            // weighted: dn of field 0 of the group (slice 0 is used)
+  int dn_dtype;
+  long long dn_bstride;
+  float* red_part;           // [G][ntiles][2]
+  float* dn0_field;          // [G]
+  int scat;
+  const float* sw;
+  const float* gw;
+  float* scat_part;          // [G][ntiles][2]
+  double plain_phase;        // k0*n0*dz
+  int spi;                   // scattering_plane_ind
+  const float2* tw;
+};
+
+template <int T>
+__device__ __forceinline__ void block_sum2(float& a, float& b, float* red) {
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) {
+    a += __shfl_xor_sync(0xffffffffu, a, o);
+    b += __shfl_xor_sync(0xffffffffu, b, o);
+  }
+  constexpr int NW = (T + 31) / 32;
+  const int w = threadIdx.x >> 5, l = threadIdx.x & 31;
+  if (l == 0) {
+    red[2 * w] = a;
+    red[2 * w + 1] = b;
+  }
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    float s = 0.f, t = 0.f;
+    for (int i = 0; i < NW; i++) {
+      s += red[2 * i];
+      t += red[2 * i + 1];
+    }
+    a = s;
+    b = t;
+  }
+}
+
+template <int N>
+__device__ __forceinline__ void col_load(float2* tile, const float2* Wp, int nx, int x0) {
+  constexpr int T = TileCfg<N>::THREADS;
+  for (int e = threadIdx.x; e < 8 * N; e += T) {
+    const int n = e >> 3;
+    const int c = (e & 7) * 2;
+    float4 f = *reinterpret_cast<const float4*>(Wp + (size_t)n * nx + x0 + c);
+    tile[tile_idx(n, c)] = make_float2(f.x, f.y);
+    tile[tile_idx(n, c + 1)] = make_float2(f.z, f.w);
+  }
+}
+
+template <int N>
+__device__ __forceinline__ void col_store(const float2* tile, float2* Wp, int nx, int x0) {
+  constexpr int T = TileCfg<N>::THREADS;
+  for (int e = threadIdx.x; e < 8 * N; e += T) {
+    const int n = e >> 3;
+    const int c = (e & 7) * 2;
+    float2 a = tile[tile_idx(n, c)], b = tile[tile_idx(n, c + 1)];
+    *reinterpret_cast<float4*>(Wp + (size_t)n * nx + x0 + c) = make_float4(a.x, a.y, b.x, b.y);
+  }
+}
+
+// multiply the k-space column tile by the propagator (+ scattering partial sums)
+template <int N>
+__device__ __forceinline__ void col_propagate(float2* tile, const ColParams& p, float n_eff, int x0,
+                                              int gl, float* red) {
+  constexpr int T = TileCfg<N>::THREADS;
+  const float nk = __fmul_rn(__fmul_rn(__fmul_rn(n_eff, n_eff), p.k0f), p.k0f);
+  float S = 0.f, G = 0.f;
+  float2 plain = make_float2(0.f, 0.f);
+  if (p.scat && x0 == 0) {
+    // plain_wave_dct[z+1] = nx*ny*exp(-i k0 n0 (spi + z+1) dz), FP64 then complex64
+    double ph = -p.plain_phase * (double)(p.spi + p.z + 1);
+    double s, c;
+    sincos(ph, &s, &c);
+    double m = (double)p.nx * (double)p.ny;
+    plain = make_float2((float)(m * c), (float)(m * s));
+  }
+  for (int e = threadIdx.x; e < 16 * N; e += T) {
+    const int y = e >> 4;
+    const int c = e & 15;
+    const int x = x0 + c;
+    float2 v = tile[tile_idx(y, c)];
+    float2 h;
+    if (p.prop_mode == 0) {
+      h = __ldg(p.H + (size_t)y * p.nx + x);
+    } else {
+      const float tmp = __fsub_rn(__fsub_rn(nk, __ldg(p.kx2 + x)), __ldg(p.ky2 + y));
+      if (tmp >= 0.f) {
+        const float ph = __fmul_rn(-p.dzf, __fsqrt_rn(tmp));
+        sincosf(ph, &h.y, &h.x);
+      } else {
+        h = make_float2(0.f, 0.f);
+      }
+    }
+    v = cmul(v, h);
+    if (p.scat) {
+      float2 d = v;
+      if (x == 0 && y == 0) d = csub(d, plain);
+      const float a2 = cabs2(d);
+      const size_t k = (size_t)y * p.nx + x;
+      S += __ldg(p.sw + k) * a2;
+      G += __ldg(p.gw + k) * a2;
+    }
+    tile[tile_idx(y, c)] = cscale(v, p.scale);
+  }
+  if (p.scat) {
+    block_sum2<T>(S, G, red);
+    if (threadIdx.x == 0) {
+      float* o = p.scat_part + ((size_t)gl * (p.nx / 16) + blockIdx.x) * 2;
+      o[0] = S;
+      o[1] = G;
+    }
+  }
+  __syncthreads();
+}
+
+// non-weighted column pass: forward FFT, propagator, inverse FFT
+template <int N>
+__global__ void __launch_bounds__(TileCfg<N>::THREADS)
+col_pass_kernel(ColParams p) {
+  constexpr int R = TileCfg<N>::R;
+  extern __shared__ float2 smem[];
+  float2* tile = smem;
+  float2* tw = smem + N * 16;
+  __shared__ float red[64];
+  const int gl = blockIdx.y;
+  const int x0 = blockIdx.x * 16;
+  float2* Wp = p.W + (size_t)gl * p.nx * N;
+  for (int k = threadIdx.x; k < N; k += TileCfg<N>::THREADS) tw[k] = p.tw[k];
+  col_load<N>(tile, Wp, p.nx, x0);
+  __syncthreads();
+  tile_fft<N, R, false>(tile, tw);
+  float n_eff = p.n00f;
+  if (p.prop_mode == 1) n_eff = p.slice_n[p.z + 1];
+  col_propagate<N>(tile, p, n_eff, x0, gl, red);
+  tile_fft<N, R, true>(tile, tw);
+  col_store<N>(tile, Wp, p.nx, x0);
+}
+
+// weighted mode, part 1: forward column FFT and the partial sums of |u_hat|*dn0, |u_hat|
+template <int N>
+__global__ void __launch_bounds__(TileCfg<N>::THREADS)
+col_fwd_reduce_kernel(ColParams p) {
+  constexpr int T = TileCfg<N>::THREADS;
+  constexpr int R = TileCfg<N>::R;
+  extern __shared__ float2 smem[];
+  float2* tile = smem;
+  float2* tw = smem + N * 16;
+  __shared__ float red[64];
+  const int gl = blockIdx.y;
+  const int x0 = blockIdx.x * 16;
+  float2* Wp = p.W + (size_t)gl * p.nx * N;
+  for (int k = threadIdx.x; k < N; k += T) tw[k] = p.tw[k];
+  col_load<N>(tile, Wp, p.nx, x0);
+  __syncthreads();
+  tile_fft<N, R, false>(tile, tw);
+  float sdn = 0.f, su = 0.f;
+  for (int e = threadIdx.x; e < 16 * N; e += T) {
+    const int y = e >> 4;
+    const int c = e & 15;
+    const float2 v = tile[tile_idx(y, c)];
+    const float a = __fsqrt_rn(cabs2(v));
+    su += a;
+    if (p.dn) sdn += a * load_dn_real(p.dn, p.dn_dtype, gl * p.dn_bstride + (size_t)y * p.nx + x0 + c);
+  }
+  block_sum2<T>(sdn, su, red);
+  if (threadIdx.x == 0) {
+    float* o = p.red_part + ((size_t)gl * (p.nx / 16) + blockIdx.x) * 2;
+    o[0] = sdn;
+    o[1] = su;
+  }
+  col_store<N>(tile, Wp, p.nx, x0);
+}
+
+// weighted mode, part 2: n = n00 + dn_sum/u_sum, propagator, inverse column FFT
+template <int N>
+__global__ void __launch_bounds__(TileCfg<N>::THREADS)
+col_inv_kernel(ColParams p) {
+  constexpr int R = TileCfg<N>::R;
+  extern __shared__ float2 smem[];
+  float2* tile = smem;
+  float2* tw = smem + N * 16;
+  __shared__ float red[64];
+  __shared__ float s_n;
+  const int gl = blockIdx.y;
+  const int x0 = blockIdx.x * 16;
+  float2* Wp = p.W + (size_t)gl * p.nx * N;
+  if (threadIdx.x == 0) {
+    // every block of the field sums the partials in the same order: identical results
+    const float* part = p.red_part + (size_t)gl * (p.nx / 16) * 2;
+    float dn_sum = 0.f, u_sum = 0.f;
+    for (int t = 0; t < p.nx / 16; t++) {
+      dn_sum += part[2 * t];
+      u_sum += part[2 * t + 1];
+    }
+    const float dn0 = dn_sum / u_sum;  // mult_dn_mean_buff, bpm_3d_kernels.cl:117
+    s_n = p.n00f + dn0;                // mult_propagator_buff, bpm_3d_kernels.cl:482
+    if (blockIdx.x == 0) p.dn0_field[gl] = dn0;
+  }
+  for (int k = threadIdx.x; k < N; k += TileCfg<N>::THREADS) tw[k] = p.tw[k];
+  col_load<N>(tile, Wp, p.nx, x0);
+  __syncthreads();
+  col_propagate<N>(tile, p, s_n, x0, gl, red);
+  tile_fft<N, R, true>(tile, tw);
+  col_store<N>(tile, Wp, p.nx, x0);
+}
+
+// ---------------------------------------------------------------------------------------
+// dispatch over power-of-two sizes
+// ---------------------------------------------------------------------------------------
+template <template <int> class K>
+struct SizeDispatch;
+
+template <int N>
+struct RowK {
+  static void prepare() {
+    static bool attr = false;
+    if (!attr) {
+      cudaFuncSetAttribute(row_pass_kernel<N>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)TileCfg<N>::SMEM);
+      attr = true;
+    }
+  }
+  static int launch(dim3 g, cudaStream_t s, const RowParams& p) {
+    prepare();
+    row_pass_kernel<N><<<g, TileCfg<N>::THREADS, TileCfg<N>::SMEM, s>>>(p);
+    BPM_LAUNCH_CHECK("row_pass_kernel");
+    return BPM_OK;
+  }
+};
+
+template <int N, int WHICH>
+struct ColK {
+  static void (*fn())(ColParams) {
+    return WHICH == 0 ? col_pass_kernel<N> : (WHICH == 1 ? col_fwd_reduce_kernel<N> : col_inv_kernel<N>);
+  }
+  static void prepare() {
+    static bool attr = false;
+    if (!attr) {
+      cudaFuncSetAttribute(fn(), cudaFuncAttributeMaxDynamicSharedMemorySize, (int)TileCfg<N>::SMEM);
+      attr = true;
+    }
+  }
+  static int launch(dim3 g, cudaStream_t s, const ColParams& p) {
+    prepare();
+    fn()<<<g, TileCfg<N>::THREADS, TileCfg<N>::SMEM, s>>>(p);
+    BPM_LAUNCH_CHECK("col_pass_kernel");
+    return BPM_OK;
+  }
+};
+
+int launch_row(int N, dim3 g, cudaStream_t s, const RowParams& p) {
+  switch (N) {
+    case 16: return RowK<16>::launch(g, s, p);
+    case 32: return RowK<32>::launch(g, s, p);
+    case 64: return RowK<64>::launch(g, s, p);
+    case 128: return RowK<128>::launch(g, s, p);
+    case 256: return RowK<256>::launch(g, s, p);
+    case 512: return RowK<512>::launch(g, s, p);
+    case 1024: return RowK<1024>::launch(g, s, p);
+  }
+  set_error("unsupported nx");
+  return BPM_ERR_SHAPE;
+}
+
+template <int WHICH>
+int launch_col(int N, dim3 g, cudaStream_t s, const ColParams& p) {
+  switch (N) {
+    case 16: return ColK<16, WHICH>::launch(g, s, p);
+    case 32: return ColK<32, WHICH>::launch(g, s, p);
+    case 64: return ColK<64, WHICH>::launch(g, s, p);
+    case 128: return ColK<128, WHICH>::launch(g, s, p);
+    case 256: return ColK<256, WHICH>::launch(g, s, p);
+    case 512: return ColK<512, WHICH>::launch(g, s, p);
+    case 1024: return ColK<1024, WHICH>::launch(g, s, p);
+  }
+  set_error("unsupported ny");
+  return BPM_ERR_SHAPE;
+}
+
+// raise the dynamic shared-memory limit of every kernel a plan will launch (outside any
+// stream capture)
+template <int N>
+void prepare_size() {
+  RowK<N>::prepare();
+  ColK<N, 0>::prepare();
+  ColK<N, 1>::prepare();
+  ColK<N, 2>::prepare();
+}
+
+void prepare_kernels(int nx, int ny) {
+  for (int n : {nx, ny}) {
+    switch (n) {
+      case 16: prepare_size<16>(); break;
+      case 32: prepare_size<32>(); break;
+      case 64: prepare_size<64>(); break;
+      case 128: prepare_size<128>(); break;
+      case 256: prepare_size<256>(); break;
+      case 512: prepare_size<512>(); break;
+      case 1024: prepare_size<1024>(); break;
+    }
+  }
+}
+
+int default_group(const bpm_plan* pl, int batch) {
+  const int nx = pl->d.nx, ny = pl->d.ny;
+  const size_t plane_bytes = (size_t)nx * ny * 8;
+  // keep the group's planes well inside L2 (129 MB) and give each pass >= ~4 waves of blocks
+  int g_l2 = (int)std::max<size_t>(1, (48u << 20) / plane_bytes);
+  int g_fill = std::max(1, (152 * 4) / std::max(1, nx / 16));
+  int g = std::min(g_l2, g_fill);
+  return std::max(1, std::min(g, batch));
+}
+
+struct WsLayout {
+  size_t w, red, dn0, scat, total;
+};
+
+WsLayout ws_layout(const bpm_plan* pl, int G) {
+  WsLayout L;
+  const int ntiles = pl->d.nx / 16;
+  size_t off = 0;
+  L.w = off;
+  off += align256((size_t)G * pl->d.nx * pl->d.ny * sizeof(float2));
+  L.red = off;
+  off += align256((size_t)G * ntiles * 2 * sizeof(float));
+  L.dn0 = off;
+  off += align256((size_t)G * sizeof(float));
+  L.scat = off;
+  off += align256((size_t)G * ntiles * 2 * sizeof(float));
+  L.total = off;
+  return L;
+}
+
+int check_request(const bpm_plan* pl, const bpm_request* r) {
+  if (!r) { set_error("request is NULL"); return BPM_ERR_ARG; }
+  if (r->batch < 1) { set_error("batch must be >= 1"); return BPM_ERR_ARG; }
+  if (!r->u0) { set_error("u0 is NULL"); return BPM_ERR_ARG; }
+  if (r->dn_dtype < BPM_DN_NONE || r->dn_dtype > BPM_DN_C64) { set_error("bad dn_dtype"); return BPM_ERR_ARG; }
+  if (r->dn_dtype != BPM_DN_NONE && !r->dn) { set_error("dn is NULL but dn_dtype is set"); return BPM_ERR_ARG; }
+  if (r->dn_dtype == BPM_DN_C64 && pl->d.mean_mode != BPM_MEAN_IGNORE) {
+    set_error("complex dn is only defined for mean_mode='ignore'");
+    return BPM_ERR_UNSUPPORTED;
+  }
+  if (pl->d.mean_mode == BPM_MEAN_SIMPLE && (!r->slice_n || !r->slice_dn0)) {
+    set_error("mean_mode='simple' needs slice_n and slice_dn0");
+    return BPM_ERR_ARG;
+  }
+  if (r->out_kind < BPM_OUT_NONE || r->out_kind > BPM_OUT_INTENSITY) { set_error("bad out_kind"); return BPM_ERR_ARG; }
+  if (r->out_kind != BPM_OUT_NONE && !r->out) { set_error("out is NULL but out_kind is set"); return BPM_ERR_ARG; }
+  if (r->scatter_g && !r->scatter_p) { set_error("scatter_g needs scatter_p"); return BPM_ERR_ARG; }
+  if (r->group < 0) { set_error("group must be >= 0"); return BPM_ERR_ARG; }
+  // 16-byte alignment of the vectorised accesses
+  auto mis = [](const void* q) { return ((uintptr_t)q & 15) != 0; };
+  if (mis(r->u0) || (r->out && mis(r->out)) || (r->last_plane && mis(r->last_plane))) {
+    set_error("u0/out/last_plane must be 16-byte aligned");
+    return BPM_ERR_ARG;
+  }
+  if (r->dn && (mis(r->dn) || (r->dn_batch_stride & 1))) {
+    set_error("dn must be 16-byte aligned with an even dn_batch_stride");
+    return BPM_ERR_ARG;
+  }
+  return BPM_OK;
+}
+
+// launch parameters of one group of fields [b0, b0+Gc) of a request
+struct MarchCtx {
+  RowParams rp;
+  ColParams cp;
+  dim3 grow, gcol;
+};
+
+int group_size(const bpm_plan* pl, const bpm_request* r) {
+  return r->group > 0 ? std::min(r->group, r->batch) : default_group(pl, r->batch);
+}
+
+int check_workspace(const bpm_plan* pl, const bpm_request* r, const void* ws, size_t ws_bytes) {
+  WsLayout L = ws_layout(pl, group_size(pl, r));
+  if (!ws || ws_bytes < L.total) {
+    set_error("workspace too small: need " + std::to_string(L.total) + " bytes");
+    return BPM_ERR_OOM;
+  }
+  if ((uintptr_t)ws & 15) {
+    set_error("workspace must be 16-byte aligned");
+    return BPM_ERR_ARG;
+  }
+  return BPM_OK;
+}
+
+MarchCtx make_ctx(const bpm_plan* pl, const bpm_request* r, void* ws, int b0, int Gc) {
+  const bpm_grid_desc& d = pl->d;
+  const int nx = d.nx, ny = d.ny, nz = d.nz;
+  WsLayout L = ws_layout(pl, group_size(pl, r));
+  char* wsb = static_cast<char*>(ws);
+  float2* W = reinterpret_cast<float2*>(wsb + L.w);
+  float* red = reinterpret_cast<float*>(wsb + L.red);
+  float* dn0f = reinterpret_cast<float*>(wsb + L.dn0);
+  float* scatp = reinterpret_cast<float*>(wsb + L.scat);
+  const size_t plane = (size_t)nx * ny;
+  const bool has_dn = r->dn_dtype != BPM_DN_NONE;
+  const size_t dn_esize = r->dn_dtype == BPM_DN_C64 ? 8 : (r->dn_dtype == BPM_DN_F16 ? 2 : 4);
+  const size_t out_esize = r->out_kind == BPM_OUT_FIELD ? 8 : 4;
+
+  MarchCtx c;
+  RowParams& rp = c.rp;
+  memset(&rp, 0, sizeof(rp));
+  rp.W = W;
+  rp.nx = nx; rp.ny = ny; rp.nz = nz;
+  rp.dn = has_dn ? static_cast<const char*>(r->dn) + (size_t)b0 * r->dn_batch_stride * dn_esize : nullptr;
+  rp.dn_dtype = r->dn_dtype;
+  rp.dn_bstride = r->dn_batch_stride;
+  rp.unit_k = pl->unit_k;
+  rp.absorb = d.absorbing_width;
+  rp.taper = pl->taper;
+  rp.mean_mode = d.mean_mode;
+  rp.dn0_field = dn0f;
+  rp.slice_dn0 = r->slice_dn0;
+  rp.out = r->out ? static_cast<char*>(r->out) + (size_t)b0 * r->out_batch_stride * out_esize : nullptr;
+  rp.out_kind = r->out ? r->out_kind : BPM_OUT_NONE;
+  rp.out_bstride = r->out_batch_stride;
+  rp.last_plane = r->last_plane ? static_cast<float2*>(r->last_plane) + (size_t)b0 * plane : nullptr;
+  rp.scat_part = scatp;
+  rp.n_ctiles = nx / 16;
+  rp.scat_p = r->scatter_p ? r->scatter_p + (size_t)b0 * nz : nullptr;
+  rp.scat_g = r->scatter_g ? r->scatter_g + (size_t)b0 * nz : nullptr;
+  rp.prefac_f = (float)(1. / nx / ny * d.dx * d.dy);
+  rp.tw = pl->tw_x;
+  rp.src = W;
+  rp.src_bstride = plane;
+
+  ColParams& cp = c.cp;
+  memset(&cp, 0, sizeof(cp));
+  cp.W = W;
+  cp.nx = nx; cp.ny = ny; cp.nz = nz;
+  cp.prop_mode = d.mean_mode == BPM_MEAN_IGNORE ? 0 : (d.mean_mode == BPM_MEAN_SIMPLE ? 1 : 2);
+  cp.H = pl->H;
+  cp.kx2 = pl->kx2;
+  cp.ky2 = pl->ky2;
+  cp.k0f = pl->k0f;
+  cp.dzf = pl->dzf;
+  cp.n00f = pl->n0f;
+  cp.slice_n = r->slice_n;
+  cp.scale = 1.f / (float)plane;
+  cp.dn = rp.dn;
+  cp.dn_dtype = r->dn_dtype;
+  cp.dn_bstride = r->dn_batch_stride;
+  cp.red_part = red;
+  cp.dn0_field = dn0f;
+  cp.scat = r->scatter_p != nullptr;
+  cp.sw = pl->sw;
+  cp.gw = pl->gw;
+  cp.scat_part = scatp;
+  cp.plain_phase = pl->k0 * d.n0 * d.dz;
+  cp.spi = r->scattering_plane_ind;
+  cp.tw = pl->tw_y;
+
+  c.grow = dim3(ny / 16, Gc);
+  c.gcol = dim3(nx / 16, Gc);
+  return c;
+}
+
+// the first row pass: plane 0 is the input itself, then the forward row FFT of step 0
+int launch_first_row(const bpm_plan* pl, const bpm_request* r, MarchCtx& c, int b0, cudaStream_t s) {
+  RowParams rp = c.rp;
+  rp.src = static_cast<const float2*>(r->u0) + (size_t)b0 * pl->d.nx * pl->d.ny;
+  rp.z = 0;
+  rp.do_inv = 0;
+  rp.do_fwd = pl->d.nz > 1;
+  rp.do_mask = 0;
+  return launch_row(pl->d.nx, c.grow, s, rp);
+}
+
+// the column pass(es) of step i (plane i -> plane i+1)
+int launch_cols(const bpm_plan* pl, MarchCtx& c, int i, int which, cudaStream_t s) {
+  c.cp.z = i;
+  if (pl->d.mean_mode == BPM_MEAN_WEIGHTED) {
+    if (which != 2) {
+      int rc = launch_col<1>(pl->d.ny, c.gcol, s, c.cp);
+      if (rc || which == 1) return rc;
+    }
+    return launch_col<2>(pl->d.ny, c.gcol, s, c.cp);
+  }
+  return launch_col<0>(pl->d.ny, c.gcol, s, c.cp);
+}
+
+// the row pass producing plane z >= 1
+int launch_row_z(const bpm_plan* pl, const bpm_request* r, MarchCtx& c, int z, cudaStream_t s) {
+  RowParams rp = c.rp;
+  rp.z = z;
+  rp.do_inv = 1;
+  rp.do_fwd = (z + 1 < pl->d.nz);
+  rp.do_mask = r->dn_dtype != BPM_DN_NONE;
+  return launch_row(pl->d.nx, c.grow, s, rp);
+}
+
+int enqueue_march(bpm_plan* pl, const bpm_request* r, void* ws, size_t ws_bytes, cudaStream_t s) {
+  int rc = check_workspace(pl, r, ws, ws_bytes);
+  if (rc) return rc;
+  const int G = group_size(pl, r);
+  const int nz = pl->d.nz;
+  for (int b0 = 0; b0 < r->batch; b0 += G) {
+    const int Gc = std::min(G, r->batch - b0);
+    MarchCtx c = make_ctx(pl, r, ws, b0, Gc);
+    if ((rc = launch_first_row(pl, r, c, b0, s))) return rc;
+    for (int i = 0; i + 1 < nz; i++) {
+      if ((rc = launch_cols(pl, c, i, 0, s))) return rc;
+      if ((rc = launch_row_z(pl, r, c, i + 1, s))) return rc;
+    }
+  }
+  return BPM_OK;
+}
+
+}  // namespace
+
+// ---------------------------------------------------------------------------------------
+// C ABI
+// ---------------------------------------------------------------------------------------
+extern "C" int bpm_grid_check(const bpm_grid_desc* d) {
+  clear_error();
+  if (!d) { set_error("grid description is NULL"); return BPM_ERR_ARG; }
+  if (!is_pow2(d->nx) || !is_pow2(d->ny) || d->nx < 16 || d->ny < 16 || d->nx > 1024 || d->ny > 1024) {
+    set_error("nx and ny must be powers of two in [16, 1024] (got " + std::to_string(d->nx) + ", " +
+              std::to_string(d->ny) + ")");
+    return BPM_ERR_SHAPE;
+  }
+  if (d->nz < 1) { set_error("nz must be >= 1"); return BPM_ERR_SHAPE; }
+  if (!(d->dx > 0) || !(d->dy > 0) || !(d->dz > 0)) { set_error("units must be positive"); return BPM_ERR_ARG; }
+  if (!(d->lam > 0)) { set_error("lam must be positive"); return BPM_ERR_ARG; }
+  if (!(d->n0 > 0)) { set_error("n0 must be positive"); return BPM_ERR_ARG; }
+  if (d->absorbing_width < 0) { set_error("absorbing_width must be >= 0"); return BPM_ERR_ARG; }
+  if (d->mean_mode < BPM_MEAN_IGNORE || d->mean_mode > BPM_MEAN_WEIGHTED) {
+    set_error("mean_mode unknown");
+    return BPM_ERR_SHAPE;
+  }
+  if (d->prop_kind != BPM_PROP_FUNCTIONAL && d->prop_kind != BPM_PROP_CLASS) {
+    set_error("prop_kind unknown");
+    return BPM_ERR_ARG;
+  }
+  return BPM_OK;
+}
+
+extern "C" int bpm_plan_create(const bpm_grid_desc* d, bpm_plan** out) {
+  int rc = bpm_grid_check(d);
+  if (rc) return rc;
+  if (!out) { set_error("out is NULL"); return BPM_ERR_ARG; }
+  *out = nullptr;
+  bpm_plan* pl = new bpm_plan();
+  memset(pl, 0, sizeof(*pl));
+  pl->d = *d;
+  const int nx = d->nx, ny = d->ny;
+  pl->k0 = 2. * M_PI / d->lam;
+  pl->k0f = (float)pl->k0;
+  pl->dzf = (float)d->dz;
+  pl->n0f = (float)d->n0;
+  pl->unit_k = (float)(pl->k0 * d->dz);
+  cudaGetDevice(&pl->device);
+
+  std::vector<float2> twx(nx), twy(ny);
+  for (int k = 0; k < nx; k++) {
+    double a = -2. * M_PI * k / nx;
+    twx[k] = make_float2((float)cos(a), (float)sin(a));
+  }
+  for (int k = 0; k < ny; k++) {
+    double a = -2. * M_PI * k / ny;
+    twy[k] = make_float2((float)cos(a), (float)sin(a));
+  }
+  std::vector<float> kx2(nx), ky2(ny);
+  const float twopi_f = 2.f * PI_F;
+  for (int i = 0; i < nx; i++) {
+    float k = twopi_f * fftfreq_f32(i, nx, (float)d->dx);
+    kx2[i] = k * k;
+  }
+  for (int j = 0; j < ny; j++) {
+    float k = twopi_f * fftfreq_f32(j, ny, (float)d->dy);
+    ky2[j] = k * k;
+  }
+  const int aw = d->absorbing_width;
+  std::vector<float> taper(std::max(aw, 1), 1.f);
+  for (int i = 0; i < aw; i++) taper[i] = taper_value(i, aw);
+
+  auto fail = [&](cudaError_t e, const char* what) {
+    int r = cuda_fail(e, what);
+    bpm_plan_destroy(pl);
+    return r;
+  };
+  cudaError_t e;
+  if ((e = cudaMalloc(&pl->tw_x, nx * sizeof(float2)))) return fail(e, "cudaMalloc");
+  if ((e = cudaMalloc(&pl->tw_y, ny * sizeof(float2)))) return fail(e, "cudaMalloc");
+  if ((e = cudaMalloc(&pl->kx2, nx * sizeof(float)))) return fail(e, "cudaMalloc");
+  if ((e = cudaMalloc(&pl->ky2, ny * sizeof(float)))) return fail(e, "cudaMalloc");
+  if ((e = cudaMalloc(&pl->taper, taper.size() * sizeof(float)))) return fail(e, "cudaMalloc");
+  if ((e = cudaMalloc(&pl->H, (size_t)nx * ny * sizeof(float2)))) return fail(e, "cudaMalloc");
+  if ((e = cudaMalloc(&pl->sw, (size_t)nx * ny * sizeof(float)))) return fail(e, "cudaMalloc");
+  if ((e = cudaMalloc(&pl->gw, (size_t)nx * ny * sizeof(float)))) return fail(e, "cudaMalloc");
+  if ((e = cudaMemcpy(pl->tw_x, twx.data(), nx * sizeof(float2), cudaMemcpyHostToDevice))) return fail(e, "cudaMemcpy");
+  if ((e = cudaMemcpy(pl->tw_y, twy.data(), ny * sizeof(float2), cudaMemcpyHostToDevice))) return fail(e, "cudaMemcpy");
+  if ((e = cudaMemcpy(pl->kx2, kx2.data(), nx * sizeof(float), cudaMemcpyHostToDevice))) return fail(e, "cudaMemcpy");
+  if ((e = cudaMemcpy(pl->ky2, ky2.data(), ny * sizeof(float), cudaMemcpyHostToDevice))) return fail(e, "cudaMemcpy");
+  if ((e = cudaMemcpy(pl->taper, taper.data(), taper.size() * sizeof(float), cudaMemcpyHostToDevice)))
+    return fail(e, "cudaMemcpy");
+  dim3 tb(128), tg((nx + 127) / 128, ny);
+  build_tables_kernel<<<tg, tb>>>(nx, ny, d->dx, d->dy, d->dz, d->n0, pl->k0, pl->n0f, pl->k0f, d->prop_kind,
+                                  d->use_fresnel_approx, pl->kx2, pl->ky2, pl->H, pl->sw, pl->gw);
+  if ((e = cudaGetLastError())) return fail(e, "build_tables_kernel");
+  count_launch();
+  if ((e = cudaDeviceSynchronize())) return fail(e, "build_tables_kernel");
+  prepare_kernels(nx, ny);
+  *out = pl;
+  return BPM_OK;
+}
+
+extern "C" int bpm_plan_destroy(bpm_plan* pl) {
+  if (!pl) return BPM_OK;
+  cudaFree(pl->tw_x);
+  cudaFree(pl->tw_y);
+  cudaFree(pl->kx2);
+  cudaFree(pl->ky2);
+  cudaFree(pl->taper);
+  cudaFree(pl->H);
+  cudaFree(pl->sw);
+  cudaFree(pl->gw);
+  delete pl;
+  return BPM_OK;
+}
+
+extern "C" size_t bpm_workspace_bytes(const bpm_plan* pl, int batch, int group) {
+  if (!pl || batch < 1) return 0;
+  const int G = group > 0 ? std::min(group, batch) : default_group(pl, batch);
+  return ws_layout(pl, G).total;
+}
+
+extern "C" int bpm_propagate(bpm_plan* pl, const bpm_request* r, void* ws, size_t ws_bytes, void* stream) {
+  clear_error();
+  if (!pl) { set_error("plan is NULL"); return BPM_ERR_ARG; }
+  int rc = check_request(pl, r);
+  if (rc) return rc;
+  return enqueue_march(pl, r, ws, ws_bytes, static_cast<cudaStream_t>(stream));
+}
+
+extern "C" int bpm_launch_pass(bpm_plan* pl, const bpm_request* r, void* ws, size_t ws_bytes, int pass, int z,
+                               void* stream) {
+  clear_error();
+  if (!pl) { set_error("plan is NULL"); return BPM_ERR_ARG; }
+  int rc = check_request(pl, r);
+  if (rc) return rc;
+  if ((rc = check_workspace(pl, r, ws, ws_bytes))) return rc;
+  cudaStream_t s = static_cast<cudaStream_t>(stream);
+  const int Gc = group_size(pl, r);
+  MarchCtx c = make_ctx(pl, r, ws, 0, Gc);
+  switch (pass) {
+    case BPM_PASS_FIRST_ROW:
+      return launch_first_row(pl, r, c, 0, s);
+    case BPM_PASS_COLUMN:
+    case BPM_PASS_COLUMN_REDUCE:
+    case BPM_PASS_COLUMN_PROPAGATE: {
+      if (z < 0 || z + 1 >= pl->d.nz) { set_error("column pass needs 0 <= z < nz-1"); return BPM_ERR_ARG; }
+      const bool w = pl->d.mean_mode == BPM_MEAN_WEIGHTED;
+      if (w == (pass == BPM_PASS_COLUMN)) { set_error("pass kind does not match the mean mode"); return BPM_ERR_ARG; }
+      return launch_cols(pl, c, z, pass == BPM_PASS_COLUMN ? 0 : (pass == BPM_PASS_COLUMN_REDUCE ? 1 : 2), s);
+    }
+    case BPM_PASS_ROW:
+      if (z < 1 || z >= pl->d.nz) { set_error("row pass needs 1 <= z < nz"); return BPM_ERR_ARG; }
+      return launch_row_z(pl, r, c, z, s);
+  }
+  set_error("unknown pass kind");
+  return BPM_ERR_ARG;
+}
+
+extern "C" int bpm_exec_create(bpm_plan* pl, const bpm_request* r, void* ws, size_t ws_bytes, bpm_exec** out) {
+  clear_error();
+  if (!pl || !out) { set_error("plan/out is NULL"); return BPM_ERR_ARG; }
+  int rc = check_request(pl, r);
+  if (rc) return rc;
+  cudaStream_t s;
+  BPM_CUDA_TRY(cudaStreamCreateWithFlags(&s, cudaStreamNonBlocking));
+  unsigned long long before = g_launches.load();
+  cudaError_t e = cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal);
+  if (e) {
+    cudaStreamDestroy(s);
+    return cuda_fail(e, "cudaStreamBeginCapture");
+  }
+  rc = enqueue_march(pl, r, ws, ws_bytes, s);
+  cudaGraph_t g = nullptr;
+  e = cudaStreamEndCapture(s, &g);
+  cudaStreamDestroy(s);
+  // captured launches do not run now: take them back off the counter
+  unsigned long long n = g_launches.load() - before;
+  g_launches.fetch_sub(n);
+  if (rc) {
+    if (g) cudaGraphDestroy(g);
+    return rc;
+  }
+  if (e) return cuda_fail(e, "cudaStreamEndCapture");
+  bpm_exec* x = new bpm_exec();
+  x->graph = g;
+  x->launches = n;
+  e = cudaGraphInstantiate(&x->exec, g, 0);
+  if (e) {
+    cudaGraphDestroy(g);
+    delete x;
+    return cuda_fail(e, "cudaGraphInstantiate");
+  }
+  *out = x;
+  return BPM_OK;
+}
+
+extern "C" int bpm_exec_launch(bpm_exec* x, void* stream) {
+  clear_error();
+  if (!x) { set_error("exec is NULL"); return BPM_ERR_ARG; }
+  BPM_CUDA_TRY(cudaGraphLaunch(x->exec, static_cast<cudaStream_t>(stream)));
+  count_launch(x->launches);
+  return BPM_OK;
+}
+
+extern "C" int bpm_exec_destroy(bpm_exec* x) {
+  if (!x) return BPM_OK;
+  cudaGraphExecDestroy(x->exec);
+  cudaGraphDestroy(x->graph);
+  delete x;
+  return BPM_OK;
+}

@@ -1,0 +1,192 @@
+/*
+ * bpm_gb300 -- C ABI of the GB300 (sm_103a) implementation of bpm's two hot paths:
+ *   (1) the split-step beam-propagation z-march (bpm_3d / Bpm3d), and
+ *   (2) the vectorial Debye-Wolf focus field (focus_field_debye / psf / psf_u0).
+ *
+ * The reference (maweigert/bpm) has no C ABI: its boundary is the Python API, which
+ * JIT-compiles OpenCL kernels and launches them through gputools/pyopencl. Each entry
+ * point below replaces one such Python-level driver, cited per function. Buffers are
+ * plain device pointers owned by the caller; the library allocates only plan-private
+ * tables (at plan creation) and takes scratch from a caller-sized workspace.
+ * All calls are stream-ordered on the `stream` argument (a cudaStream_t; NULL = legacy
+ * default stream) and never synchronise the host, except plan creation, which uploads
+ * its tables synchronously. A plan may be used from one host thread at a time.
+ *
+ * Arrays use the reference's layouts (numpy C order): a field plane is (ny, nx)
+ * complex64 (interleaved float re, im), a volume (nz, ny, nx), a batch of fields
+ * (batch, ny, nx); element (x, y, z) sits at x + nx*y + nx*ny*z.
+ *
+ * Return value: BPM_OK (0) or a negative bpm_status; bpm_last_error() gives the text
+ * of the last error raised on the calling thread.
+ */
+#ifndef BPM_GB300_H
+#define BPM_GB300_H
+
+#include <stddef.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define BPM_GB300_VERSION 1
+
+typedef enum {
+  BPM_OK = 0,
+  BPM_ERR_ARG = -1,        /* invalid argument (the reference raises ValueError)            */
+  BPM_ERR_SHAPE = -2,      /* unsupported shape (the reference raises NotImplementedError)  */
+  BPM_ERR_OOM = -3,        /* device allocation failed or workspace too small               */
+  BPM_ERR_CUDA = -4,       /* a CUDA runtime call failed                                    */
+  BPM_ERR_TIMEOUT = -5,    /* a bounded device-side wait gave up                            */
+  BPM_ERR_UNSUPPORTED = -6 /* combination the reference leaves undefined                    */
+} bpm_status;
+
+/* mean-index correction of the propagator, bpm/bpm/bpm_3d.py:53 mean_mode */
+typedef enum {
+  BPM_MEAN_IGNORE = 0,   /* fixed propagator at n0                                           */
+  BPM_MEAN_SIMPLE = 1,   /* n0 + mean(dn[z]) per slice, given by the caller (slice tables)   */
+  BPM_MEAN_WEIGHTED = 2  /* n0 + sum|u_hat|*dn0 / sum|u_hat| per step, reduced on the device */
+} bpm_mean_mode;
+
+/* which propagator recipe the plan reproduces */
+typedef enum {
+  BPM_PROP_FUNCTIONAL = 0, /* bpm_3d: FP32 FFTFREQ evanescent mask of compute_propagator
+                              (bpm/bpm/kernels/bpm_3d_kernels.cl:408-432), FP64 kz phase  */
+  BPM_PROP_CLASS = 1       /* Bpm3d: host FP64 propagator, NaN-mask (bpm/bpmclass/bpm3d.py:87-109) */
+} bpm_prop_kind;
+
+typedef enum {
+  BPM_DN_NONE = 0,  /* free propagation, no phase mask and no taper                      */
+  BPM_DN_F32 = 1,   /* real dn, float32                                                   */
+  BPM_DN_F16 = 2,   /* real dn stored as IEEE half (store_dn_as_half)                     */
+  BPM_DN_C64 = 3    /* complex dn, complex64: exp(-i k0 dz dn), no taper (reference Q7)  */
+} bpm_dn_dtype;
+
+typedef enum {
+  BPM_OUT_NONE = 0,      /* no volume output (last plane only)                              */
+  BPM_OUT_FIELD = 1,     /* complex64 field volume (return_field=True)                      */
+  BPM_OUT_INTENSITY = 2  /* float32 |u|^2 volume (return_field=False)                       */
+} bpm_out_kind;
+
+typedef struct {
+  int nx, ny, nz;          /* grid; nx, ny powers of two in [16, 1024]; nz >= 1              */
+  double dx, dy, dz;       /* voxel size, microns                                            */
+  double lam;              /* vacuum wavelength, microns                                     */
+  double n0;               /* background refractive index                                    */
+  int absorbing_width;     /* taper width in pixels (0 = none)                               */
+  int mean_mode;           /* bpm_mean_mode                                                  */
+  int prop_kind;           /* bpm_prop_kind                                                  */
+  int use_fresnel_approx;  /* changes only the scattering weights (reference quirk Q1)       */
+} bpm_grid_desc;
+
+typedef struct bpm_plan bpm_plan;
+
+/* One propagation request over `batch` fields that share the plan's grid. */
+typedef struct {
+  int batch;                     /* number of fields (>= 1)                                     */
+  const void* u0;                /* device, (batch, ny, nx) complex64 input planes              */
+  const void* dn;                /* device dn volume(s) of dtype dn_dtype, (nz, ny, nx) each    */
+  int dn_dtype;                  /* bpm_dn_dtype                                                */
+  long long dn_batch_stride;     /* elements between fields' dn volumes; 0 = one shared volume  */
+  const float* slice_n;          /* BPM_MEAN_SIMPLE: device (nz) float32(n0 + mean(dn[z]))      */
+  const float* slice_dn0;        /* BPM_MEAN_SIMPLE: device (nz) float32(mean(dn[z]))           */
+  void* out;                     /* device output volume(s) of kind out_kind, or NULL           */
+  int out_kind;                  /* bpm_out_kind                                                */
+  long long out_batch_stride;    /* elements between fields' output volumes                     */
+  void* last_plane;              /* device (batch, ny, nx) complex64 exit fields, or NULL       */
+  float* scatter_p;              /* device (batch, nz) scattering cross-section, or NULL        */
+  float* scatter_g;              /* device (batch, nz) anisotropy g (needs scatter_p), or NULL  */
+  int scattering_plane_ind;      /* z offset of the plain-wave reference, bpm_3d.py:253         */
+  int group;                     /* fields marched together per pass (0 = library default)      */
+} bpm_request;
+
+/* Library version (BPM_GB300_VERSION). */
+int bpm_version(void);
+
+/* Text of the last error on the calling thread ("" if none). */
+const char* bpm_last_error(void);
+
+/* Number of kernels this library has launched in the calling process (all threads). */
+unsigned long long bpm_launch_count(void);
+
+/* Validate a grid description without touching the device (BPM_OK or an error). */
+int bpm_grid_check(const bpm_grid_desc* desc);
+
+/* Create a propagation plan: validates the grid and uploads the propagator, FFT twiddle,
+ * taper and scattering-weight tables for the current device.
+ * Replaces the setup half of bpm/bpm/bpm_3d.py:_bpm_3d (:140-278, propagator built by
+ * compute_propagator at :192) and of bpm/bpmclass/bpm3d.py:_Bpm3d_Base._setup (:64-115)
+ * + _bpm3d_ocl.py:_setup_impl (:35-56). */
+int bpm_plan_create(const bpm_grid_desc* desc, bpm_plan** out);
+
+/* Release a plan and its device tables. */
+int bpm_plan_destroy(bpm_plan* plan);
+
+/* Bytes of scratch bpm_propagate needs for a request of `batch` fields (256-aligned). */
+size_t bpm_workspace_bytes(const bpm_plan* plan, int batch, int group);
+
+/* March every field of the request through all nz slices.
+ * Replaces the hot loop of bpm/bpm/bpm_3d.py:_bpm_3d (:283-381, one fft / reduction /
+ * mult_propagator* / fft / mult_dn* / copy_intens sequence per z-step) and of
+ * bpm/bpmclass/_bpm3d_ocl.py:_propagate_single (:100-126), for `batch` fields at once.
+ * Plane 0 of `out` is u0 (unmasked); plane z>0 is the field after step z-1 with the
+ * mask of dn slice z (reference quirk Q8). */
+int bpm_propagate(bpm_plan* plan, const bpm_request* req, void* workspace, size_t workspace_bytes,
+                  void* stream);
+
+/* Kinds of pass for bpm_launch_pass. */
+typedef enum {
+  BPM_PASS_FIRST_ROW = 0,         /* plane 0 output + forward row FFT                         */
+  BPM_PASS_COLUMN = 1,            /* column FFT, propagator, inverse column FFT (ignore/simple) */
+  BPM_PASS_COLUMN_REDUCE = 2,     /* weighted: forward column FFT + |u_hat| partial sums      */
+  BPM_PASS_COLUMN_PROPAGATE = 3,  /* weighted: propagator + inverse column FFT                */
+  BPM_PASS_ROW = 4                /* inverse row FFT, mask, plane z output, forward row FFT   */
+} bpm_pass_kind;
+
+/* Launch exactly one pass of the march for the first group of fields of the request, for
+ * step / plane index z, on `stream`. Used to time individual kernels (each pass is one
+ * kernel launch); the passes in march order reproduce bpm_propagate. No reference
+ * counterpart: the reference's per-step launches are the kernels of bpm_3d_kernels.cl. */
+int bpm_launch_pass(bpm_plan* plan, const bpm_request* req, void* workspace, size_t workspace_bytes,
+                    int pass, int z, void* stream);
+
+/* Capture the launches of bpm_propagate for a fixed request and workspace into a CUDA
+ * graph; bpm_exec_launch replays it on any stream. The buffers named by `req` and the
+ * workspace must stay valid and unchanged in address while the exec lives. No reference
+ * counterpart (the reference re-enqueues every launch from Python each step). */
+typedef struct bpm_exec bpm_exec;
+int bpm_exec_create(bpm_plan* plan, const bpm_request* req, void* workspace, size_t workspace_bytes,
+                    bpm_exec** out);
+int bpm_exec_launch(bpm_exec* exec, void* stream);
+int bpm_exec_destroy(bpm_exec* exec);
+
+/* ---------------------------------------------------------------------------------- */
+/* Vectorial Debye-Wolf focus field                                                    */
+/* ---------------------------------------------------------------------------------- */
+
+typedef struct {
+  int nx, ny, nz;            /* full output shape (even), arrays (nz, ny, nx)                  */
+  double dx, dy, dz;         /* voxel size, microns                                            */
+  double lam;                /* vacuum wavelength, microns                                     */
+  double n0;                 /* refractive index of the immersion medium                      */
+  const double* na;          /* host array of aperture NAs: [0, NA] or annuli [a1, a2, ...]     */
+  int n_na;                  /* even, >= 2                                                     */
+  int n_integration_steps;   /* INT_STEPS: the rule uses INT_STEPS+1 nodes per annulus         */
+  double ex0, ey0;           /* input polarisation (the reference launches with 1, 0)          */
+} debye_desc;
+
+/* Bytes of scratch debye_focus_field needs for this description (256-aligned). */
+size_t debye_workspace_bytes(const debye_desc* desc);
+
+/* Compute the focus field on the full (nz, ny, nx) grid centred at index n/2.
+ * Replaces bpm/psf/_focus_fields_debye.py:focus_field_debye (:48-146): the debye_wolf
+ * octant launch (:102-109, kernel bpm/psf/kernels/psf_debye.cl:24-113) and the host-side
+ * spreading of the octant to the full volume (:116-144), fused into device kernels.
+ * u: float32 |E|^2 (may be NULL); ex, ey, ez: complex64 (each may be NULL). */
+int debye_focus_field(const debye_desc* desc, float* u, void* ex, void* ey, void* ez,
+                      void* workspace, size_t workspace_bytes, void* stream);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* BPM_GB300_H */

@@ -1,0 +1,157 @@
+"""CPU oracle for the vectorial Debye-Wolf focus field. TEST INFRASTRUCTURE ONLY.
+
+Restates bpm/psf/_focus_fields_debye.py:focus_field_debye (:48-146) with the kernel
+bpm/psf/kernels/psf_debye.cl:debye_wolf (:24-113), and the public wrappers
+bpm/psf/psf_functions.py:psf (:18-71), psf_u0 (:104-120) and psf_lightsheet (:75-98).
+
+The octant kernel is evaluated in FP64 with scipy's Bessel functions, from the float32
+parameters the reference passes to its kernel (octant extents x2,y2,z2, lam/n0, the
+aperture angles). Grid coordinates follow the kernel's FP32 recipe
+x = x1 + i*(x2-x1)/(Nx-1.f). The quadrature is the kernel's (quirk Q14): INT_STEPS+1
+nodes t = a1 + i*dt with dt = (a2-a1)/(INT_STEPS-1) (so the last node lies past a2),
+weight 1/2 at i=0 and i=INT_STEPS, prefactor dt*sqrt(cos t) without sin t.
+
+Mirroring to the full volume is the reference's literal slice loop (:116-144): x/y
+mirrors copy values unchanged, the z <= Nz0/2 half is conjugated (quirk Q15).
+"""
+import itertools
+
+import numpy as np
+from scipy.special import jv
+
+
+def octant_params(shape, units, lam, NA, n0):
+    """The float32 arguments of the debye_wolf launch (_focus_fields_debye.py:74-109)."""
+    if np.isscalar(NA):
+        NA = [0., NA]
+    Nx0, Ny0, Nz0 = shape
+    dx, dy, dz = units
+    if not Nx0 % 2 + Ny0 % 2 + Nz0 % 2 == 0:
+        raise NotImplementedError("odd shapes not supported yet")
+    alphas = np.arcsin(np.array(NA) / n0)
+    assert len(alphas) % 2 == 0
+    Nx, Ny, Nz = Nx0 // 2 + 1, Ny0 // 2 + 1, Nz0 // 2 + 1
+    return dict(Nx=Nx, Ny=Ny, Nz=Nz,
+                x2=np.float32(dx * (Nx - 1.)), y2=np.float32(dy * (Ny - 1.)),
+                z2=np.float32(dz * (Nz - 1.)), lam=np.float32(1. * lam / n0),
+                alphas=alphas.astype(np.float32))
+
+
+def coord_f32(N, x2):
+    """x = x1 + i*(x2-x1)/(N-1.f) in float32 with x1 = 0 (psf_debye.cl:46-48)."""
+    i = np.arange(N, dtype=np.float32)
+    x1 = np.float32(0)
+    return x1 + (i * (np.float32(x2) - x1)) / np.float32(N - 1.)
+
+
+def quadrature_nodes(alphas, int_steps):
+    """Nodes and end weights of the kernel's trapezoid rule per annulus (psf_debye.cl:62-78)."""
+    ts, ws = [], []
+    for a1, a2 in zip(alphas[0::2], alphas[1::2]):
+        a1 = float(a1)
+        a2 = float(a2)
+        dt = (a2 - a1) / (int_steps - 1.)
+        i = np.arange(int_steps + 1)
+        t = a1 + i * dt
+        w = np.where((i == 0) | (i == int_steps), .5, 1.) * dt
+        ts.append(t)
+        ws.append(w)
+    return np.concatenate(ts), np.concatenate(ws)
+
+
+def debye_octant(params, int_steps, Ex0=1., Ey0=0.):
+    """FP64 evaluation of debye_wolf over the octant. Returns (u, ex, ey, ez) of shape
+    (Nz, Ny, Nx) in float64/complex128."""
+    Nx, Ny, Nz = params["Nx"], params["Ny"], params["Nz"]
+    x = coord_f32(Nx, params["x2"]).astype(np.float64)
+    y = coord_f32(Ny, params["y2"]).astype(np.float64)
+    z = coord_f32(Nz, params["z2"]).astype(np.float64)
+    lam = float(params["lam"])
+    k = 2. * np.pi / lam
+    Y, X = np.meshgrid(y, x, indexing="ij")
+    kr = (k * np.sqrt(X ** 2 + Y ** 2)).ravel()
+    phi = np.arctan2(Y, X).ravel()
+    kz = k * z
+    t, w = quadrature_nodes(params["alphas"], int_steps)
+    co, si = np.cos(t), np.sin(t)
+    with np.errstate(invalid="ignore"):
+        pre = w * np.sqrt(co)
+    arg = kr[:, None] * si[None, :]
+    A0 = (pre * (co + 1.))[None, :] * jv(0, arg)
+    A1 = (pre * si)[None, :] * jv(1, arg)
+    A2 = (pre * (co - 1.))[None, :] * jv(2, arg)
+    E = np.exp(1j * kz[None, :] * co[:, None])          # (T, Z)
+    I0 = A0 @ E
+    I1 = A1 @ E
+    I2 = A2 @ E                                           # (R, Z)
+    c2 = np.cos(2 * phi)[:, None]
+    s2 = np.sin(2 * phi)[:, None]
+    ex = Ex0 * (I0 + I2 * c2) + Ey0 * s2 * I2
+    ey = Ey0 * (I0 - I2 * c2) + Ex0 * s2 * I2
+    ez = (-2j * I1) * (Ex0 * np.cos(phi) + Ey0 * np.sin(phi))[:, None]
+    u = np.abs(ex) ** 2 + np.abs(ey) ** 2 + np.abs(ez) ** 2
+
+    def vol(a):
+        return np.ascontiguousarray(a.T.reshape(Nz, Ny, Nx))
+    return vol(u), vol(ex), vol(ey), vol(ez)
+
+
+def mirror_octant(shape, u, ex, ey, ez, real_dtype=np.float32, complex_dtype=np.complex64):
+    """The reference's octant -> full volume spreading loop (_focus_fields_debye.py:116-144)."""
+    Nx0, Ny0, Nz0 = shape
+    Nz, Ny, Nx = u.shape
+    u_all = np.empty((Nz0, Ny0, Nx0), real_dtype)
+    ex_all = np.empty((Nz0, Ny0, Nx0), complex_dtype)
+    ey_all = np.empty((Nz0, Ny0, Nx0), complex_dtype)
+    ez_all = np.empty((Nz0, Ny0, Nx0), complex_dtype)
+    sx = [slice(0, Nx), slice(Nx, Nx0)]
+    sy = [slice(0, Ny), slice(Ny, Ny0)]
+    sz = [slice(0, Nz), slice(Nz, Nz0)]
+    for i, j, k in itertools.product([0, 1], [0, 1], [0, 1]):
+        src = (slice(1 - i, Nz - 1 + i), slice(1 - j, Ny - 1 + j), slice(1 - k, Nx - 1 + k))
+        flip = (slice(None, None, (-1) ** i), slice(None, None, (-1) ** j), slice(None, None, (-1) ** k))
+        dst = (sz[1 - i], sy[1 - j], sx[1 - k])
+        u_all[dst] = u[src][flip]
+        for a, a_all in ((ex, ex_all), (ey, ey_all), (ez, ez_all)):
+            v = a[src][flip]
+            a_all[dst] = v if i == 0 else np.conjugate(v)
+    return u_all, ex_all, ey_all, ez_all
+
+
+def mirror_index(N0):
+    """Index form of the same spreading along one axis: full index m -> octant |m - N0/2|."""
+    return np.abs(np.arange(N0) - N0 // 2)
+
+
+def focus_field_debye(shape, units, lam, NA, n0=1., n_integration_steps=200,
+                      real_dtype=np.float32, complex_dtype=np.complex64):
+    """FP64 restatement of focus_field_debye; returns (u, ex, ey, ez) on (Nz0, Ny0, Nx0)."""
+    params = octant_params(shape, units, lam, NA, n0)
+    oct_ = debye_octant(params, n_integration_steps)
+    return mirror_octant(shape, *oct_, real_dtype=real_dtype, complex_dtype=complex_dtype)
+
+
+def psf(shape, units, lam, NA, n0=1., n_integration_steps=200, return_field=False, **kw):
+    """bpm/psf/psf_functions.py:psf (:18-71)."""
+    u, ex, ey, ez = focus_field_debye(shape, units, lam, NA, n0, n_integration_steps, **kw)
+    return (u, ex, ey, ez) if return_field else u
+
+
+def psf_u0(shape, units, zfoc=0, NA=.4, lam=.5, n0=1., n_integration_steps=200, **kw):
+    """bpm/psf/psf_functions.py:psf_u0 (:104-120): ex[0] of a 4-plane PSF with dz = zfoc/2."""
+    Nx, Ny = shape
+    dx, dy = units
+    u, ex, ey, ez = psf((Nx, Ny, 4), (dx, dy, zfoc / 2.), n0=n0, lam=lam, NA=NA,
+                        n_integration_steps=n_integration_steps, return_field=True, **kw)
+    return ex[0, ...]
+
+
+def psf_lightsheet(shape, units, lam_illum, NA_illum, lam_detect, NA_detect, n0=1.,
+                   n_integration_steps=200, **kw):
+    """bpm/psf/psf_functions.py:psf_lightsheet (:75-98): detection PSF times the
+    illumination PSF computed on the reversed axes and transposed back."""
+    u_detect = psf(shape, units, lam=lam_detect, NA=NA_detect, n0=n0,
+                   n_integration_steps=n_integration_steps, **kw)
+    u_illum = psf(tuple(shape)[::-1], tuple(units)[::-1], lam=lam_illum, NA=NA_illum, n0=n0,
+                  n_integration_steps=n_integration_steps, **kw)
+    return u_detect * u_illum.transpose((2, 1, 0))

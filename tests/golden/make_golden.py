@@ -1,0 +1,235 @@
+"""Generate the golden vectors in tests/golden/*.npz from the reference's own kernels.
+
+Run here, where the reference checkout exists:
+    make -C oracle REF=/root/reference && python tests/golden/make_golden.py
+
+Golden outputs come from the reference's OpenCL kernel sources compiled as host C++
+(oracle/_ref/libref_cl.so, see oracle/Makefile):
+  * Debye-Wolf: debye_wolf (bpm/psf/kernels/psf_debye.cl:24-113) run over the octant with
+    the launch arguments of bpm/psf/_focus_fields_debye.py:102-109, spread to the full
+    volume by the reference's mirroring loop (:116-144, restated in oracle.debye_ref).
+  * BPM: the per-step kernel sequence of bpm/bpm/bpm_3d.py:_bpm_3d (:283-381) and of
+    bpm/bpmclass/_bpm3d_ocl.py:_propagate_single (:100-126), each elementwise kernel the
+    reference's own, with a single-precision scipy FFT standing in for the third-party
+    gputools FFT (forward unnormalised, inverse 1/(Nx*Ny)).
+  * Masks: compute_propagator's evanescent mask and the mult_dn taper, straight from the
+    kernels, for bit-exact comparisons.
+Inputs are seeded and stored next to the outputs, so the fixtures are self-contained.
+"""
+import os
+import sys
+
+import numpy as np
+import scipy.fft as sfft
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, os.path.dirname(os.path.dirname(HERE)))
+
+from oracle import reflib  # noqa: E402
+from oracle import debye_ref  # noqa: E402
+from oracle.reflib import ptr, f32  # noqa: E402
+
+
+def ref_debye(shape, units, lam, NA, n0, steps):
+    lib = reflib.load()
+    p = debye_ref.octant_params(shape, units, lam, NA, n0)
+    Nx, Ny, Nz = p["Nx"], p["Ny"], p["Nz"]
+    u = np.zeros((Nz, Ny, Nx), np.float32)
+    ex = np.zeros((Nz, Ny, Nx), np.complex64)
+    ey = np.zeros_like(ex)
+    ez = np.zeros_like(ex)
+    al = np.ascontiguousarray(p["alphas"], np.float32)
+    lib.ref_debye_wolf(ptr(ex), ptr(ey), ptr(ez), ptr(u), f32(1.), f32(0.), f32(0.), f32(p["x2"]),
+                       f32(0.), f32(p["y2"]), f32(0.), f32(p["z2"]), f32(p["lam"]), ptr(al),
+                       len(al), Nx, Ny, Nz, steps)
+    return debye_ref.mirror_octant(shape, u, ex, ey, ez)
+
+
+def ref_march(size, units, lam, n0, u0, dn, mean_mode, absorbing_width, return_field, store_half=False):
+    """The reference's _bpm_3d step sequence with its own kernels (return_full=True)."""
+    lib = reflib.load()
+    Nx, Ny, Nz = size
+    dx, dy, dz = units
+    k0 = 2. * np.pi / lam
+    plane = np.ascontiguousarray(u0, np.complex64).copy()
+    h = np.zeros((Ny, Nx), np.complex64)
+    lib.ref_compute_propagator(ptr(h), f32(n0), f32(k0), f32(dx), f32(dy), f32(dz), Nx, Ny)
+    is_c = np.iscomplexobj(dn)
+    if is_c:
+        dng = np.ascontiguousarray(dn, np.complex64)
+    elif store_half:
+        dng = np.ascontiguousarray(dn, np.float16)
+    else:
+        dng = np.ascontiguousarray(dn, np.float32)
+    dn_mean = np.mean(dn, axis=(1, 2))
+    out = np.empty((Nz, Ny, Nx), np.complex64 if return_field else np.float32)
+    if return_field:
+        out[0] = plane
+    else:
+        tmp = np.empty((Ny, Nx), np.float32)
+        lib.ref_copy_intens(ptr(plane), ptr(tmp), 0, Nx * Ny)
+        out[0] = tmp
+    dn_sum = np.zeros(1, np.float32)
+    u_sum = np.zeros(1, np.float32)
+    dn_flat0 = (np.asarray(dng, np.float32) if store_half else dng).reshape(-1)[:Nx * Ny]
+    for i in range(Nz - 1):
+        plane = np.ascontiguousarray(sfft.fft2(plane), np.complex64)
+        if mean_mode == "simple":
+            dn0 = dn_mean[i + 1]
+            lib.ref_mult_propagator(ptr(plane), f32(n0 + dn0), f32(k0), f32(dx), f32(dy), f32(dz), Nx, Ny)
+        elif mean_mode == "weighted":
+            a = np.abs(plane).astype(np.float64)
+            dn_sum[0] = np.float32(np.sum(a * dn_flat0.reshape(Ny, Nx).astype(np.float64)))
+            u_sum[0] = np.float32(np.sum(a))
+            lib.ref_mult_propagator_buff(ptr(plane), ptr(dn_sum), ptr(u_sum), f32(n0), f32(k0),
+                                         f32(dx), f32(dy), f32(dz), Nx, Ny)
+        else:
+            dn0 = 0.
+            lib.ref_mult(ptr(plane), ptr(h), Nx * Ny)
+        plane = np.ascontiguousarray(sfft.ifft2(plane), np.complex64)
+        stride = Nx * Ny * (i + 1)
+        if is_c:
+            lib.ref_mult_dn_complex(ptr(plane), ptr(dng), f32(k0 * dz), stride, absorbing_width, Nx, Ny)
+        elif mean_mode == "weighted":
+            fn = lib.ref_mult_dn_mean_half_buff if store_half else lib.ref_mult_dn_mean_buff
+            fn(ptr(plane), ptr(dng), ptr(dn_sum), ptr(u_sum), f32(k0 * dz), stride, absorbing_width, Nx, Ny)
+        else:
+            fn = lib.ref_mult_dn_mean_half if store_half else lib.ref_mult_dn_mean
+            fn(ptr(plane), ptr(dng), f32(k0 * dz), f32(dn0), stride, absorbing_width, Nx, Ny)
+        if return_field:
+            out[i + 1] = plane
+        else:
+            tmp = np.empty((Ny, Nx), np.float32)
+            lib.ref_copy_intens(ptr(plane), ptr(tmp), 0, Nx * Ny)
+            out[i + 1] = tmp
+    return out
+
+
+def ref_class_march(size, units, lam, n0, u0, dn, absorbing_width, H):
+    """_propagate_single's step sequence (bpm/bpmclass/_bpm3d_ocl.py:100-126), field volume."""
+    lib = reflib.load()
+    Nx, Ny, Nz = size
+    dx, dy, dz = units
+    k0 = 2. * np.pi / lam
+    plane = np.ascontiguousarray(u0, np.complex64).copy()
+    Hc = np.ascontiguousarray(H, np.complex64)
+    is_c = np.iscomplexobj(dn)
+    dng = np.ascontiguousarray(dn, np.complex64 if is_c else np.float32)
+    out = np.empty((Nz, Ny, Nx), np.complex64)
+    out[0] = plane
+    for i in range(Nz - 1):
+        plane = np.ascontiguousarray(sfft.fft2(plane), np.complex64)
+        lib.ref_mult(ptr(plane), ptr(Hc), Nx * Ny)
+        plane = np.ascontiguousarray(sfft.ifft2(plane), np.complex64)
+        stride = Nx * Ny * (i + 1)
+        if is_c:
+            lib.ref_mult_dn_complex(ptr(plane), ptr(dng), f32(k0 * dz), stride, absorbing_width, Nx, Ny)
+        else:
+            lib.ref_mult_dn(ptr(plane), ptr(dng), f32(k0 * dz), stride, absorbing_width, Nx, Ny)
+        out[i + 1] = plane
+    return out
+
+
+def sphere_dn(Nx, Ny, Nz, center, radius, value, dtype=np.float32):
+    z, y, x = np.meshgrid(np.arange(Nz), np.arange(Ny), np.arange(Nx), indexing="ij")
+    r2 = (x - center[0]) ** 2 + (y - center[1]) ** 2 + (z - center[2]) ** 2
+    return np.where(r2 <= radius ** 2, value, 0).astype(dtype)
+
+
+def random_spheres_dn(Nx, Ny, Nz, n, rng, rmin, rmax, re_rng, im_rng=None):
+    z, y, x = np.meshgrid(np.arange(Nz), np.arange(Ny), np.arange(Nx), indexing="ij")
+    dn = np.zeros((Nz, Ny, Nx), np.complex64 if im_rng else np.float32)
+    for _ in range(n):
+        c = rng.uniform(0, 1, 3) * np.array([Nx, Ny, Nz])
+        r = rng.uniform(rmin, rmax)
+        v = rng.uniform(*re_rng)
+        if im_rng:
+            v = v + 1j * rng.uniform(*im_rng)
+        m = (x - c[0]) ** 2 + (y - c[1]) ** 2 + (z - c[2]) ** 2 <= r * r
+        dn[m] = v
+    return dn
+
+
+def main():
+    lib = reflib.load()
+    if lib is None:
+        raise SystemExit("oracle/_ref/libref_cl.so missing: run make -C oracle first")
+    rng = np.random.default_rng(0)
+    out = {}
+
+    # --- masks -------------------------------------------------------------------------
+    for (Nx, Ny, dx, dy, lam, n0) in [(64, 32, .1, .13, .5, 1.33), (128, 128, .05, .05, .5, 1.0),
+                                      (32, 64, .2, .1, .633, 1.52)]:
+        k0 = 2. * np.pi / lam
+        h = np.zeros((Ny, Nx), np.complex64)
+        lib.ref_compute_propagator(ptr(h), f32(n0), f32(k0), f32(dx), f32(dy), f32(.1), Nx, Ny)
+        out["mask_%dx%d" % (Nx, Ny)] = (h != 0)
+        out["mask_%dx%d_args" % (Nx, Ny)] = np.array([dx, dy, lam, n0, .1])
+    for absorb in (0, 1, 5, 12):
+        Nx, Ny = 40, 36
+        pl = np.ones((Ny, Nx), np.complex64)
+        dn = np.zeros((2, Ny, Nx), np.float32)
+        lib.ref_mult_dn(ptr(pl), ptr(dn), f32(1.), Nx * Ny, absorb, Nx, Ny)
+        out["taper_%d" % absorb] = pl.real.copy()
+
+    # --- BPM marches (reference kernels + fp32 FFT) -------------------------------------
+    cases = []
+    Nx, Ny, Nz = 32, 32, 12
+    dn = sphere_dn(Nx, Ny, Nz, (16, 16, 6), 6, .05)
+    for mode in ("weighted", "simple", "ignore"):
+        cases.append(("bpm_sphere_%s" % mode, (Nx, Ny, Nz), (.1, .1, .1), .5, 1.33,
+                      np.ones((Ny, Nx), np.complex64), dn, mode, 0, True, False))
+    x = .1 * np.arange(64)
+    u_tilt = np.exp(-2j * np.pi * (.6 * x[None, :] + .3 * .1 * np.arange(32)[:, None])).astype(np.complex64)
+    dn2 = random_spheres_dn(64, 32, 10, 6, rng, 2, 6, (.01, .05)).astype(np.float32)
+    cases.append(("bpm_tilt_taper_weighted", (64, 32, 10), (.1, .1, .1), .5, 1.0, u_tilt, dn2,
+                  "weighted", 6, False, False))
+    cases.append(("bpm_tilt_taper_ignore_half", (64, 32, 10), (.1, .1, .1), .5, 1.0, u_tilt, dn2,
+                  "ignore", 6, True, True))
+    for (name, size, units, lam, n0, u0, dn_, mode, aw, rf, half) in cases:
+        o = ref_march(size, units, lam, n0, u0, dn_, mode, aw, rf, store_half=half)
+        out[name + "_out"] = o
+        out[name + "_u0"] = u0
+        out[name + "_dn"] = dn_
+        out[name + "_args"] = np.array([size[0], size[1], size[2], units[0], units[1], units[2],
+                                        lam, n0, aw, int(rf), int(half)], np.float64)
+        out[name + "_mode"] = np.array(mode)
+
+    # class path, complex dn (absorbing: negative imaginary part), field volume
+    from oracle.bpm_ref import class_propagator
+    size, units, lam, n0 = (32, 32, 10), (.1, .1, .1), .5, 1.33
+    dnc = random_spheres_dn(32, 32, 10, 4, rng, 3, 7, (.01, .05), (-1e-2, 0.))
+    H = class_propagator(size, units, lam, n0)
+    out["class_complex_out"] = ref_class_march(size, units, lam, n0, np.ones((32, 32), np.complex64), dnc, 0, H)
+    out["class_complex_dn"] = dnc
+    out["class_real_out"] = ref_class_march(size, units, lam, n0, np.ones((32, 32), np.complex64),
+                                            dnc.real.astype(np.float32), 4, H)
+
+    # --- Debye-Wolf ---------------------------------------------------------------------
+    dcases = [("psf_16_NA08", (16, 16, 16), (.1, .1, .1), .5, .8, 1.0, 50),
+              ("psf_24x20x12_NA11", (24, 20, 12), (.08, .1, .12), .5, 1.1, 1.33, 64),
+              ("psf_annulus", (16, 16, 8), (.1, .1, .1), .5, [.1, .3, .5, .7], 1.0, 40),
+              ("psf_u0_like", (32, 32, 4), (.1, .1, 1.6), .5, .4, 1.33, 100)]
+    for (name, shape, units, lam, NA, n0, steps) in dcases:
+        u, ex, ey, ez = ref_debye(shape, units, lam, NA, n0, steps)
+        out[name + "_u"] = u
+        out[name + "_ex"] = ex
+        out[name + "_ey"] = ey
+        out[name + "_ez"] = ez
+        out[name + "_args"] = np.array(list(shape) + list(units) + [lam, n0, steps], np.float64)
+        out[name + "_NA"] = np.atleast_1d(np.array(NA, np.float64))
+
+    xs = np.linspace(0, 30, 301).astype(np.float32)
+    for n in (0, 1, 2):
+        r = np.zeros_like(xs)
+        lib.ref_bessel_jn(n, ptr(xs), ptr(r), len(xs))
+        out["bessel_j%d" % n] = r
+    out["bessel_x"] = xs
+
+    path = os.path.join(HERE, "golden.npz")
+    np.savez_compressed(path, **out)
+    print("wrote", path, os.path.getsize(path), "bytes,", len(out), "arrays")
+
+
+if __name__ == "__main__":
+    main()

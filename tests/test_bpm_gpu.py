@@ -1,0 +1,254 @@
+"""Parity of the CUDA split-step march with the reference (golden vectors from the
+reference's own kernels) and with the CPU oracle, plus the reference's own physics
+checks. Tolerance: relative L2 <= 1e-4 against the FP64 oracle and against the
+reference-faithful FP32 oracle; evanescent mask and taper bit-exact."""
+import numpy as np
+import pytest
+
+from conftest import BPM_GOLDEN, golden_case, rel_l2
+from oracle import bpm_ref
+
+pytestmark = pytest.mark.gpu
+
+TOL = 1e-4
+
+
+@pytest.fixture(scope="module")
+def bpm():
+    import torch
+    if not torch.cuda.is_available():
+        pytest.skip("no CUDA device")
+    import bpm_gb300
+    return bpm_gb300
+
+
+def sphere_dn(Nx, Ny, Nz, r, val, center=None, dtype=np.float32):
+    c = center or (Nx / 2, Ny / 2, Nz / 2)
+    z, y, x = np.meshgrid(np.arange(Nz), np.arange(Ny), np.arange(Nx), indexing="ij")
+    return (val * (((x - c[0]) ** 2 + (y - c[1]) ** 2 + (z - c[2]) ** 2) <= r * r)).astype(dtype)
+
+
+def random_spheres(Nx, Ny, Nz, n, seed, im=False):
+    rng = np.random.default_rng(seed)
+    z, y, x = np.meshgrid(np.arange(Nz), np.arange(Ny), np.arange(Nx), indexing="ij")
+    dn = np.zeros((Nz, Ny, Nx), np.complex64 if im else np.float32)
+    for _ in range(n):
+        c = rng.uniform(0, 1, 3) * (Nx, Ny, Nz)
+        r = rng.uniform(3, 10)
+        v = rng.uniform(.01, .05) + (1j * rng.uniform(-1e-3, 1e-3) if im else 0)
+        dn[(x - c[0]) ** 2 + (y - c[1]) ** 2 + (z - c[2]) ** 2 <= r * r] = v
+    return dn
+
+
+@pytest.mark.parametrize("name", BPM_GOLDEN)
+def test_golden_reference_kernels(bpm, golden, name):
+    c = golden_case(golden, name)
+    u = bpm.bpm_3d(c["size"], c["units"], lam=c["lam"], n0=c["n0"], u0=c["u0"], dn=c["dn"],
+                   mean_mode=c["mean_mode"], absorbing_width=c["absorbing_width"],
+                   return_field=c["return_field"], store_dn_as_half=c["store_dn_as_half"])
+    assert u.dtype == (np.complex64 if c["return_field"] else np.float32)
+    assert rel_l2(u, c["out"]) < TOL
+
+
+def test_golden_class_path(bpm, golden):
+    dnc = golden["class_complex_dn"]
+    m = bpm.Bpm3d((32, 32, 10), (.1, .1, .1), lam=.5, n0=1.33, dn=dnc)
+    assert rel_l2(m._propagate_single(), golden["class_complex_out"]) < TOL
+    m.set_dn(dnc.real.astype(np.float32))
+    assert rel_l2(m.propagate(absorbing_width=4), golden["class_real_out"]) < TOL
+
+
+@pytest.mark.parametrize("size,mode", [
+    ((128, 128, 64), "weighted"), ((128, 128, 64), "simple"), ((128, 128, 64), "ignore"),
+    ((256, 128, 24), "weighted"), ((16, 16, 8), "weighted"), ((32, 1024, 6), "ignore"),
+    ((1024, 32, 6), "simple"), ((512, 512, 12), "weighted"),
+])
+def test_oracle_parity(bpm, size, mode):
+    Nx, Ny, Nz = size
+    dn = sphere_dn(Nx, Ny, Nz, min(Nx, Ny) / 6, .05)
+    rng = np.random.default_rng(1)
+    x = .1 * np.arange(Nx)
+    u0 = np.exp(2j * np.pi * .3 * x)[None, :].repeat(Ny, 0).astype(np.complex64)
+    kw = dict(lam=.5, n0=1.33, dn=dn, u0=u0, mean_mode=mode, absorbing_width=4)
+    u = bpm.bpm_3d(size, (.1, .1, .1), **kw)
+    o32 = bpm_ref.bpm_3d(size, (.1, .1, .1), precision="fp32", **kw)
+    o64 = bpm_ref.bpm_3d(size, (.1, .1, .1), precision="fp64", **kw)
+    assert rel_l2(u, o64) < TOL
+    assert rel_l2(u, o32) < TOL
+    del rng
+
+
+def test_config1_plain(bpm):
+    """128^3, dx=dz=0.1, lam 0.5, n0 1.33, plane wave, one centred sphere r=20 px dn=0.05;
+    exit field and |u|^2 volume."""
+    size = (128, 128, 128)
+    dn = sphere_dn(128, 128, 128, 20, .05, center=(64, 64, 64))
+    u = bpm.bpm_3d(size, (.1, .1, .1), lam=.5, n0=1.33, dn=dn, return_field=False)
+    last = bpm.bpm_3d(size, (.1, .1, .1), lam=.5, n0=1.33, dn=dn, return_full=False)
+    o = bpm_ref.bpm_3d(size, (.1, .1, .1), lam=.5, n0=1.33, dn=dn, return_field=True, precision="fp64")
+    assert rel_l2(u, np.abs(o) ** 2) < TOL
+    assert rel_l2(last, o[-1]) < TOL
+
+
+def test_complex_dn_ignore_and_errors(bpm):
+    size = (64, 64, 16)
+    dn = random_spheres(64, 64, 16, 5, 3, im=True)
+    u = bpm.bpm_3d(size, (.1, .1, .1), lam=.5, n0=1.33, dn=dn, mean_mode="ignore")
+    o = bpm_ref.bpm_3d(size, (.1, .1, .1), lam=.5, n0=1.33, dn=dn, mean_mode="ignore", precision="fp64")
+    assert rel_l2(u, o) < TOL
+    with pytest.raises(NotImplementedError):
+        bpm.bpm_3d(size, (.1, .1, .1), dn=dn)           # weighted + complex: undefined upstream
+    with pytest.raises(NotImplementedError):
+        bpm.bpm_3d((100, 64, 4), (.1, .1, .1))           # non power-of-two grid
+    with pytest.raises(NotImplementedError):
+        bpm.bpm_3d(size, (.1, .1, .1), mean_mode="nope")
+    with pytest.raises(ValueError):
+        bpm.bpm_3d(size, (.1, .1, .1), dn=np.zeros((3, 64, 64), np.float32))
+
+
+def test_scattering_outputs(bpm):
+    size = (64, 64, 24)
+    dn = sphere_dn(64, 64, 24, 8, .04)
+    for mode in ("weighted", "ignore"):
+        u, p, g = bpm.bpm_3d(size, (.1, .1, .1), lam=.5, n0=1.0, dn=dn, mean_mode=mode,
+                             return_scattering=True, return_g=True)
+        uo, po, go = bpm_ref.bpm_3d(size, (.1, .1, .1), lam=.5, n0=1.0, dn=dn, mean_mode=mode,
+                                    return_scattering=True, return_g=True, precision="fp64")
+        assert p[0] == 0 and np.isnan(g[0])
+        assert rel_l2(u, uo) < TOL
+        assert rel_l2(p[1:], po[1:]) < 1e-3
+        assert rel_l2(g[1:], go[1:]) < 1e-3
+
+
+def test_split_matches_oracle_and_field_intensity(bpm):
+    """n_volumes=2 z-chunking (bpm_3d.py:863-992) and tests/test_field_intens.py:29-43."""
+    size = (64, 64, 40)
+    dn = sphere_dn(64, 64, 40, 10, .05)
+    u1 = bpm.bpm_3d(size, (.05, .05, .05), dn=dn, n_volumes=2, return_field=True)
+    u2 = bpm.bpm_3d(size, (.05, .05, .05), dn=dn, n_volumes=2, return_field=False)
+    o = bpm_ref.bpm_3d(size, (.05, .05, .05), dn=dn, n_volumes=2, return_field=True, precision="fp64")
+    assert rel_l2(u1, o) < TOL
+    assert np.allclose(np.abs(u1) ** 2, u2, rtol=1e-4, atol=1e-6)
+
+
+def _kspace_mask_from_one_step(bpm, size, mode, n0, lam, units, prop_class=False):
+    """March a delta (flat spectrum) one step with dn = 0: FFT of plane 1 * Nx*Ny is the
+    propagator, zero exactly where the evanescent mask cuts."""
+    Nx, Ny, _ = size
+    u0 = np.zeros((Ny, Nx), np.complex64)
+    u0[0, 0] = 1.
+    if prop_class:
+        m = bpm.Bpm3d((Nx, Ny, 2), units, lam=lam, n0=n0)
+        u = m._propagate_single(u0)
+    else:
+        u = bpm.bpm_3d((Nx, Ny, 2), units, lam=lam, n0=n0, u0=u0, mean_mode=mode,
+                       dn=np.zeros((2, Ny, Nx), np.float32))
+    H = np.fft.fft2(u[1].astype(np.complex128))
+    return np.abs(H) > .5
+
+
+@pytest.mark.parametrize("mode", ["ignore", "simple", "weighted"])
+def test_evanescent_mask_bit_exact(bpm, golden, mode):
+    for key in [k for k in golden.files if k.startswith("mask_") and not k.endswith("_args")]:
+        Nx, Ny = map(int, key[5:].split("x"))
+        dx, dy, lam, n0, dz = golden[key + "_args"]
+        m = _kspace_mask_from_one_step(bpm, (Nx, Ny, 2), mode, n0, lam, (dx, dy, dz))
+        assert np.array_equal(m, golden[key]), key
+
+
+def test_class_mask_is_fp64(bpm):
+    Nx, Ny, dx, dy, lam, n0 = 64, 64, .1, .1, .5, 1.33
+    m = _kspace_mask_from_one_step(bpm, (Nx, Ny, 2), None, n0, lam, (dx, dy, .1), prop_class=True)
+    H = bpm_ref.class_propagator((Nx, Ny, 2), (dx, dy, .1), lam, n0, precision="fp64")
+    assert np.array_equal(m, H != 0)
+
+
+@pytest.mark.parametrize("absorb", [1, 5, 12])
+def test_taper_bit_exact(bpm, absorb):
+    """dn = 0 and u0 = 1: plane 1 is exactly H(0,0) * taper (FFT of a constant is exact)."""
+    Nx, Ny = 64, 32
+    u = bpm.bpm_3d((Nx, Ny, 2), (.1, .1, .1), lam=.5, n0=1.33, dn=np.zeros((2, Ny, Nx), np.float32),
+                   absorbing_width=absorb, mean_mode="ignore")
+    h00 = u[1, Ny // 2, Nx // 2]
+    t = bpm_ref.taper_f32(Nx, Ny, absorb)
+    exp_re = (np.float32(h00.real) * t).astype(np.float32)
+    exp_im = (np.float32(h00.imag) * t).astype(np.float32)
+    assert np.array_equal(u[1].real, exp_re)
+    assert np.array_equal(u[1].imag, exp_im)
+
+
+def test_batched_equals_single_and_deterministic(bpm):
+    size = (128, 64, 20)
+    dn = random_spheres(128, 64, 20, 6, 7)
+    rng = np.random.default_rng(2)
+    u0s = np.exp(2j * np.pi * rng.uniform(-.2, .2, (5, 1, 1)) * np.arange(128)[None, None, :]
+                 ).repeat(64, 1).astype(np.complex64)
+    for mode in ("weighted", "simple", "ignore"):
+        ub = bpm.bpm_3d_batched(size, (.1, .1, .1), u0=u0s, dn=dn, mean_mode=mode, return_field=False,
+                                group=2)
+        ub2 = bpm.bpm_3d_batched(size, (.1, .1, .1), u0=u0s, dn=dn, mean_mode=mode, return_field=False)
+        assert np.array_equal(ub, ub2)
+        for b in range(5):
+            us = bpm.bpm_3d(size, (.1, .1, .1), u0=u0s[b], dn=dn, mean_mode=mode, return_field=False)
+            assert np.array_equal(ub[b], us)
+
+
+def test_graph_replay_equals_direct(bpm):
+    import torch
+    size = (64, 64, 16)
+    dn = random_spheres(64, 64, 16, 4, 9)
+    m = bpm.BatchedMarch(size, (.1, .1, .1), .5, 1.33, 3, dn=dn, out_kind="field")
+    m.u0.copy_(torch.from_numpy(np.exp(1j * np.linspace(0, 3, 64 * 64 * 3)).reshape(3, 64, 64)
+                                .astype(np.complex64)))
+    m.run()
+    torch.cuda.synchronize()
+    direct = bpm.bpm_3d_batched(size, (.1, .1, .1), u0=m.u0.cpu().numpy(), dn=dn)
+    assert np.array_equal(m.out.cpu().numpy(), direct)
+    n0 = bpm.launch_count()
+    m.run()
+    torch.cuda.synchronize()
+    assert bpm.launch_count() - n0 == 1 + 2 * 15 + 15  # row + (2 col + 1 row) per step
+
+
+def test_plane_wave_analytic(bpm):
+    """tests/test_plane.py: a plane wave in a homogeneous medium n = n0 + dn."""
+    Nx, Ny, Nz = 128, 64, 64
+    dx = dz = .05
+    lam, n0, n = .5, 1., 1.2
+    z = dz * np.arange(Nz)
+    u_plane = np.exp(-2j * np.pi * n / lam * z)[:, None, None] * np.ones((1, Ny, Nx))
+    dn = (n - n0) * np.ones((Nz, Ny, Nx), np.float32)
+    u = bpm.bpm_3d((Nx, Ny, Nz), (dx, dx, dz), lam=lam, n0=n0, dn=dn, u0=u_plane[0].astype(np.complex64))
+    assert np.mean(np.abs(u_plane - u) ** 2) < 1e-6
+
+
+def test_absorbing_plane_wave_analytic(bpm):
+    """tests/test_complex.py:50: absorbing medium n = n0 - 0.01j, mean|du|^2 ~ 0 (2 decimals)."""
+    Nx, Nz = 128, 128
+    dx = dz = .05
+    lam, n0 = .5, 1.5
+    n = n0 - .01j
+    z = dz * np.arange(Nz)
+    u_plane = np.exp(-2j * np.pi * np.sqrt(n ** 2 / lam ** 2) * z)[:, None, None] * np.ones((1, Nx, Nx))
+    dn = ((n - n0) * np.ones((Nz, Nx, Nx))).astype(np.complex64)
+    u = bpm.bpm_3d((Nx, Nx, Nz), (dx, dx, dz), lam=lam, n0=n0, dn=dn, u0=u_plane[0].astype(np.complex64),
+                   mean_mode="ignore")
+    np.testing.assert_almost_equal(np.mean(np.abs(u_plane - u) ** 2), 0, decimal=2)
+    assert np.mean(np.abs(u_plane - u) ** 2) < 1e-8
+
+
+def test_linearity_at_full_size(bpm):
+    """Size-independent property at the batched workload's grid (512^2 x 256, 4 fields):
+    the march is linear in u0 (weighted dn0 is scale-invariant)."""
+    import torch
+    size = (512, 512, 256)
+    g = torch.Generator(device="cuda").manual_seed(0)
+    dn = (torch.rand((256, 512, 512), device="cuda", generator=g) * .04 - .02).float()
+    x = torch.arange(512, device="cuda", dtype=torch.float32) * .1
+    u0 = torch.exp(2j * np.pi * .2 * x).to(torch.complex64)[None, None, :].expand(2, 512, 512).contiguous()
+    a = bpm.bpm_3d_batched(size, (.1, .1, .1), u0=u0, dn=dn, return_full=False)
+    b = bpm.bpm_3d_batched(size, (.1, .1, .1), u0=(3 * u0).contiguous(), dn=dn, return_full=False)
+    r = (b - 3 * a).abs().norm() / (3 * a).abs().norm()
+    assert float(r) < 1e-5
+    s = bpm.bpm_3d(size, (.1, .1, .1), u0=u0[1], dn=dn, return_full=False)
+    assert torch.equal(s, a[1])

@@ -1,0 +1,93 @@
+"""The C ABI library loads, exports every symbol include/bpm_gb300.h declares, and
+validates its arguments on the host (no kernel launches: these run without a GPU)."""
+import ctypes
+import os
+import re
+
+import pytest
+
+from conftest import ROOT
+
+HEADER = os.path.join(ROOT, "include", "bpm_gb300.h")
+
+
+@pytest.fixture(scope="module")
+def native():
+    from bpm_gb300 import build, _native
+    build.build(verbose=False)
+    return _native
+
+
+def header_functions():
+    src = open(HEADER).read()
+    src = re.sub(r"/\*.*?\*/", "", src, flags=re.S)
+    return sorted(set(re.findall(r"^\s*(?:const\s+)?[a-z_ ]+\*?\s*\**\s*(bpm_\w+|debye_\w+)\s*\(", src, flags=re.M)))
+
+
+def test_header_declares_entry_points():
+    names = header_functions()
+    for n in ["bpm_version", "bpm_plan_create", "bpm_propagate", "debye_focus_field"]:
+        assert n in names
+
+
+def test_library_exports_every_declared_symbol(native):
+    L = ctypes.CDLL(native.LIB_PATH)
+    for n in header_functions():
+        assert hasattr(L, n), n
+    assert set(header_functions()) <= set(native.SIGNATURES)
+
+
+def test_version_and_error_text(native):
+    L = native.lib()
+    assert L.bpm_version() == 1
+    assert isinstance(native.last_error(), str)
+
+
+def desc(native, **kw):
+    d = dict(nx=64, ny=32, nz=8, dx=.1, dy=.1, dz=.1, lam=.5, n0=1.33, absorbing_width=0,
+             mean_mode=2, prop_kind=0, use_fresnel_approx=0)
+    d.update(kw)
+    return native.GridDesc(**d)
+
+
+@pytest.mark.parametrize("kw,code", [
+    (dict(), 0),
+    (dict(nx=100), -2), (dict(ny=8), -2), (dict(nx=2048), -2), (dict(nz=0), -2),
+    (dict(dx=0.), -1), (dict(lam=-1.), -1), (dict(n0=0.), -1), (dict(absorbing_width=-1), -1),
+    (dict(mean_mode=7), -2), (dict(prop_kind=3), -1),
+])
+def test_grid_check(native, kw, code):
+    rc = native.lib().bpm_grid_check(ctypes.byref(desc(native, **kw)))
+    assert rc == code
+    if code:
+        assert native.last_error()
+
+
+def test_status_to_exception(native):
+    with pytest.raises(NotImplementedError):
+        native.check(native.BPM_ERR_SHAPE)
+    with pytest.raises(ValueError):
+        native.check(native.BPM_ERR_ARG)
+    with pytest.raises(MemoryError):
+        native.check(native.BPM_ERR_OOM)
+    with pytest.raises(RuntimeError):
+        native.check(native.BPM_ERR_CUDA)
+
+
+def test_debye_workspace_rejects_bad_shapes(native):
+    na = (ctypes.c_double * 2)(0., .8)
+    d = native.DebyeDesc(16, 16, 15, .1, .1, .1, .5, 1., ctypes.cast(na, ctypes.POINTER(ctypes.c_double)),
+                         2, 50, 1., 0.)
+    assert native.lib().debye_workspace_bytes(ctypes.byref(d)) == 0
+    d.nz = 16
+    assert native.lib().debye_workspace_bytes(ctypes.byref(d)) > 0
+    d.n_integration_steps = 1
+    assert native.lib().debye_workspace_bytes(ctypes.byref(d)) == 0
+
+
+def test_null_plan_calls(native):
+    L = native.lib()
+    assert L.bpm_workspace_bytes(None, 1, 0) == 0
+    assert L.bpm_propagate(None, None, None, 0, None) == native.BPM_ERR_ARG
+    assert L.bpm_plan_destroy(None) == 0
+    assert L.bpm_exec_destroy(None) == 0
