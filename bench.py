@@ -247,7 +247,7 @@ def bench_ours(args, rank, world, local_rank):
     torch.cuda.synchronize()
     t_plain = a.elapsed_time(b) / n_plain
     plain_value = NX * NY * (NZ - 1) / (t_plain * 1e-3)
-    same = bool(torch.equal(plain.out[0], march.out[0]))
+    same = bool(torch.equal(plain.last[0], march.last[0]))
     del plain
 
     # e2e through the public API with pinned host buffers
@@ -309,6 +309,77 @@ def bench_ours(args, rank, world, local_rank):
         "clocks": clocks,
     }
     return res
+
+
+def sphere_pool(side, nz, seed, n=50):
+    """Complex random-sphere dn on the device: 50 spheres, radius U[3,15] px,
+    Re dn U[0.01,0.05], Im dn U[0,1e-3] (input synthesis only)."""
+    import torch
+    rng = np.random.default_rng(seed)
+    dn = torch.zeros((nz, side, side), dtype=torch.complex64, device="cuda")
+    z = torch.arange(nz, device="cuda", dtype=torch.float32)[:, None, None]
+    y = torch.arange(side, device="cuda", dtype=torch.float32)[None, :, None]
+    x = torch.arange(side, device="cuda", dtype=torch.float32)[None, None, :]
+    for _ in range(n):
+        c = rng.uniform(0, 1, 3) * (side, side, nz)
+        r = rng.uniform(3, 15)
+        v = complex(rng.uniform(.01, .05), rng.uniform(0, 1e-3))
+        m = ((x - c[0]) ** 2 + (y - c[1]) ** 2 + (z - c[2]) ** 2) <= r * r
+        dn[m] = v
+    return dn
+
+
+def serve_trace(n=2000, rate=200., seed=0):
+    """Config-5 trace: Poisson arrivals; 70% BPM requests (side in {128,256,512,1024}, Nz
+    U[64,512], complex random-sphere dn, plane or Gaussian input of NA U[0.2,0.8],
+    |u|^2 volume kept on the device), 30% vectorial PSFs (NA U[0.3,1.3], n0 in
+    {1.33,1.52}, lambda U[0.4,0.7], cube side U{128..256} even). Complex dn is defined for
+    mean_mode "ignore" only, which the BPM requests use."""
+    import torch
+    from bpm_gb300.serve import BpmRequest, PsfRequest, Server
+    rng = np.random.default_rng(seed)
+    pools = {s: sphere_pool(s, 512, seed + s) for s in (128, 256, 512, 1024)}
+    t_arr = np.cumsum(rng.exponential(1. / rate, n))
+    reqs = []
+    for i in range(n):
+        if rng.uniform() < .7:
+            side = int(rng.choice([128, 256, 512, 1024]))
+            nz = int(rng.integers(64, 513))
+            na = rng.uniform(.2, .8)
+            x = (np.arange(side) - side / 2) * .1
+            if rng.uniform() < .5:
+                u0 = None
+            else:
+                w0 = LAM / np.pi / np.arcsin(na)
+                g = np.exp(-(x[None, :] ** 2 + x[:, None] ** 2) / w0 ** 2).astype(np.complex64)
+                u0 = torch.from_numpy(g).cuda()
+            reqs.append(BpmRequest((side, side, nz), UNITS, lam=LAM, n0=N0, u0=u0, dn=pools[side][:nz],
+                                   mean_mode="ignore", return_field=False, return_full=True))
+        else:
+            s = 2 * int(rng.integers(64, 129))
+            reqs.append(PsfRequest((s, s, s), UNITS, lam=float(rng.uniform(.4, .7)), NA=float(rng.uniform(.3, 1.3)),
+                                   n0=float(rng.choice([1.33, 1.52])), n_integration_steps=200))
+    torch.cuda.synchronize()
+    srv = Server(max_inflight=8, max_batch=16)
+    done = []
+    t0 = time.perf_counter()
+    for i, r in enumerate(reqs):
+        dt = t0 + t_arr[i] - time.perf_counter()
+        if dt > 0:
+            time.sleep(dt)
+        f = srv.submit(r)
+        f.add_done_callback(lambda fu: done.append(fu.exception() is None))
+    srv.close(wait=True)
+    wall = time.perf_counter() - t0
+    st = srv.stats()
+    bpm_n = sum(isinstance(r, BpmRequest) for r in reqs)
+    del pools, reqs
+    torch.cuda.empty_cache()
+    return {"requests": n, "rate_per_s": rate, "bpm_requests": bpm_n, "psf_requests": n - bpm_n,
+            "ok": int(sum(done)), "p50_ms": st["p50_ms"], "p99_ms": st["p99_ms"], "mean_ms": st["mean_ms"],
+            "wall_s": wall, "voxel_updates_per_s": st["voxel_updates"] / wall, "requests_per_s": n / wall,
+            "peak_hbm_gb": st["peak_hbm_bytes"] / 1e9, "budget_gb": st["budget_bytes"] / 1e9,
+            "workload": "config-5 trace, seeded Poisson arrivals, all requests latency-measured"}
 
 
 def profile_run(args):

@@ -45,7 +45,8 @@ class Request(ctypes.Structure):
                 ("dn_batch_stride", c_ll), ("slice_n", c_vp), ("slice_dn0", c_vp),
                 ("out", c_vp), ("out_kind", c_int), ("out_batch_stride", c_ll),
                 ("last_plane", c_vp), ("scatter_p", c_vp), ("scatter_g", c_vp),
-                ("scattering_plane_ind", c_int), ("group", c_int)]
+                ("scattering_plane_ind", c_int), ("group", c_int),
+                ("ckpt", c_vp), ("ckpt_every", c_int)]
 
 
 class DebyeDesc(ctypes.Structure):
@@ -67,6 +68,8 @@ SIGNATURES = {
     "bpm_workspace_bytes": (c_size, [c_vp, c_int, c_int]),
     "bpm_propagate": (c_int, [c_vp, ctypes.POINTER(Request), c_vp, c_size, c_vp]),
     "bpm_launch_pass": (c_int, [c_vp, ctypes.POINTER(Request), c_vp, c_size, c_int, c_int, c_vp]),
+    "bpm_backward_workspace_bytes": (c_size, [c_vp, c_int, c_int, c_int]),
+    "bpm_backward": (c_int, [c_vp, ctypes.POINTER(Request), c_vp, c_vp, c_vp, c_vp, c_size, c_vp]),
     "bpm_exec_create": (c_int, [c_vp, ctypes.POINTER(Request), c_vp, c_size, ctypes.POINTER(c_vp)]),
     "bpm_exec_launch": (c_int, [c_vp, c_vp]),
     "bpm_exec_destroy": (c_int, [c_vp]),

@@ -1,0 +1,93 @@
+"""Differentiable split-step march: d(loss)/d(dn) by the hand-written adjoint.
+
+`propagate_exit(dn, u0, ...)` marches a batch of fields (illumination angles) through one
+refractive-index volume and returns their exit planes; it is a torch.autograd.Function
+whose backward is bpm_backward in libbpm_gb300.so: the forward march stores the field
+every `ckpt_every` planes, the backward recomputes each segment from its checkpoint and
+marches the adjoint field back with the conjugate propagator and conjugate phase masks,
+writing k0 dz Im(conj(G) u) per plane. The propagator must not depend on dn, so this is
+the "ignore" mean mode (the Bpm3d class semantics with prop="class", or bpm_3d's
+mean_mode="ignore" with prop="functional"). The reference has no gradient
+(bpm/bpm/bpm_3d_inverse.py is a non-functional sketch).
+"""
+import ctypes
+
+import torch
+
+from . import _native as N
+from .bpm3d import _ptr, _stream_ptr, get_plan
+
+__all__ = ["propagate_exit"]
+
+
+class _ExitMarch(torch.autograd.Function):
+
+    @staticmethod
+    def forward(ctx, dn, u0, plan, ckpt_every, group):
+        B, Ny, Nx = u0.shape
+        Nz = plan.size[2]
+        dev = u0.device
+        u0c = u0.detach().to(torch.complex64).contiguous()
+        dnc = dn.detach().to(torch.float32).contiguous() if dn is not None else None
+        n_ckpt = (Nz - 1) // ckpt_every + 1
+        ckpt = torch.empty((B, n_ckpt, Ny, Nx), dtype=torch.complex64, device=dev)
+        last = torch.empty((B, Ny, Nx), dtype=torch.complex64, device=dev)
+        kind = N.DN_F32 if dnc is not None else N.DN_NONE
+        bstride = Nz * Ny * Nx if (dnc is not None and dnc.dim() == 4) else 0
+        req = N.Request(B, _ptr(u0c), _ptr(dnc), kind, bstride, None, None, None, N.OUT_NONE, 0,
+                        _ptr(last), None, None, 0, int(group), _ptr(ckpt), int(ckpt_every))
+        wsb = plan.workspace_bytes(B, group)
+        ws = torch.empty(wsb, dtype=torch.uint8, device=dev)
+        N.check(N.lib().bpm_propagate(plan.handle, ctypes.byref(req), _ptr(ws), wsb, _stream_ptr()),
+                "bpm_propagate")
+        ctx.save_for_backward(u0c, dnc if dnc is not None else torch.empty(0, device=dev), ckpt)
+        ctx.plan = plan
+        ctx.k = ckpt_every
+        ctx.group = group
+        ctx.has_dn = dnc is not None
+        ctx.bstride = bstride
+        ctx.dn_dtype = dn.dtype if dn is not None else None
+        return last
+
+    @staticmethod
+    def backward(ctx, grad_last):
+        u0c, dnc, ckpt = ctx.saved_tensors
+        plan = ctx.plan
+        B, Ny, Nx = u0c.shape
+        Nz = plan.size[2]
+        dev = u0c.device
+        g = grad_last.to(torch.complex64).contiguous()
+        kind = N.DN_F32 if ctx.has_dn else N.DN_NONE
+        req = N.Request(B, _ptr(u0c), _ptr(dnc) if ctx.has_dn else None, kind, ctx.bstride, None, None,
+                        None, N.OUT_NONE, 0, None, None, None, 0, int(ctx.group), _ptr(ckpt), int(ctx.k))
+        grad_dn = torch.zeros((B, Nz, Ny, Nx), dtype=torch.float32, device=dev) if ctx.has_dn else None
+        grad_u0 = torch.empty((B, Ny, Nx), dtype=torch.complex64, device=dev) if ctx.needs_input_grad[1] else None
+        wsb = int(N.lib().bpm_backward_workspace_bytes(plan.handle, B, int(ctx.group), int(ctx.k)))
+        ws = torch.empty(wsb, dtype=torch.uint8, device=dev)
+        N.check(N.lib().bpm_backward(plan.handle, ctypes.byref(req), _ptr(g), _ptr(grad_dn), _ptr(grad_u0),
+                                     _ptr(ws), wsb, _stream_ptr()), "bpm_backward")
+        gdn = None
+        if ctx.has_dn and ctx.needs_input_grad[0]:
+            gdn = grad_dn if ctx.bstride else grad_dn.sum(dim=0)
+            gdn = gdn.to(ctx.dn_dtype)
+        return gdn, grad_u0, None, None, None
+
+
+def propagate_exit(dn, u0, size, units, lam=.5, n0=1., absorbing_width=0, ckpt_every=16,
+                   prop="functional", group=0):
+    """Exit planes (B, Ny, Nx) complex64 of the fields u0 (B, Ny, Nx) marched through dn
+    (Nz, Ny, Nx) real, shared by all fields, or (B, Nz, Ny, Nx) per field. Differentiable
+    in dn and u0 (torch autograd). prop = "functional" (bpm_3d, mean_mode="ignore") or
+    "class" (Bpm3d's FP64 propagator)."""
+    kind = {"functional": N.PROP_FUNCTIONAL, "class": N.PROP_CLASS}[prop]
+    plan = get_plan(size, units, lam, n0, absorbing_width, "ignore", kind)
+    if u0.dim() == 2:
+        u0 = u0.unsqueeze(0)
+    Nx, Ny, Nz = plan.size
+    if tuple(u0.shape[-2:]) != (Ny, Nx):
+        raise ValueError("u0 must have shape (B, %d, %d)" % (Ny, Nx))
+    if dn is not None and tuple(dn.shape[-3:]) != (Nz, Ny, Nx):
+        raise ValueError("dn must have shape (..., %d, %d, %d)" % (Nz, Ny, Nx))
+    if dn is not None and dn.is_complex():
+        raise NotImplementedError("the adjoint needs real dn")
+    return _ExitMarch.apply(dn, u0, plan, int(ckpt_every), int(group))

@@ -124,7 +124,7 @@ struct RowParams {
   const float2* src;        // group's input planes (u0 + b0*plane, or W)
   long long src_bstride;    // float2 elements between fields
   float2* W;                // group workspace planes
-  int nx, ny, nz, z;        // z = plane produced by this pass
+  int nx, ny, nz, z;        // z = plane produced by this pass (dn slice index)
   int do_inv, do_fwd, do_mask;
   const void* dn;           // dn of field 0 of the group
   int dn_dtype;
@@ -138,13 +138,22 @@ struct RowParams {
   void* out;                // output of field 0 of the group
   int out_kind;
   long long out_bstride;    // elements
+  int zout0;                // output plane index = z - zout0
   float2* last_plane;       // group's exit planes or NULL
+  float2* ckpt;             // group's checkpoint planes (G, n_ckpt, ny, nx) or NULL
+  int ckpt_every, n_ckpt;
   const float* scat_part;   // [G][ntiles][2]
   int n_ctiles;
   float* scat_p;            // group's (nz) rows
   float* scat_g;
   float prefac_f;
   const float2* tw;
+  // adjoint passes only
+  const float2* seg;        // forward fields of the current segment (G, planes, ny, nx)
+  long long seg_bstride;    // float2 elements between fields
+  int seg_z0;               // plane index of the segment's first plane
+  float* grad_dn;           // group's (nz, ny, nx) dn gradients
+  float2* grad_u0;          // group's (ny, nx) u0 gradients or NULL
 };
 
 __device__ __forceinline__ float load_dn_real(const void* dn, int dtype, size_t idx) {
@@ -152,8 +161,20 @@ __device__ __forceinline__ float load_dn_real(const void* dn, int dtype, size_t 
   return __ldg(reinterpret_cast<const float*>(dn) + idx);
 }
 
-template <int N>
-__global__ void __launch_bounds__(TileCfg<N>::THREADS)
+// two consecutive real dn values (x even)
+__device__ __forceinline__ float2 load_dn_pair(const void* dn, int dtype, size_t idx) {
+  if (dtype == BPM_DN_F16)
+    return __half22float2(*reinterpret_cast<const __half2*>(reinterpret_cast<const __half*>(dn) + idx));
+  return __ldg(reinterpret_cast<const float2*>(reinterpret_cast<const float*>(dn) + idx));
+}
+
+// Row pass over 16 rows of one field. Forward (ADJ = false): [inverse row FFT], phase mask
+// of slice z with taper, plane-z outputs, [forward row FFT]. Adjoint (ADJ = true): [inverse
+// row FFT] of the adjoint field, dn gradient k0 dz Im(conj(G) u_z) against the forward field
+// u_z of the segment, conjugate mask, [forward row FFT]; at plane 0 the adjoint is the u0
+// gradient.
+template <int N, bool ADJ>
+__global__ void __launch_bounds__(TileCfg<N>::THREADS, TileCfg<N>::MINB)
 row_pass_kernel(RowParams p) {
   constexpr int T = TileCfg<N>::THREADS;
   constexpr int R = TileCfg<N>::R;
@@ -165,16 +186,20 @@ row_pass_kernel(RowParams p) {
   const int y0 = blockIdx.x * 16;
   const size_t plane = (size_t)N * p.ny;
 
+  // the 16 rows are contiguous in memory: element e = r*N + x; each thread holds R of them
+  constexpr int PER = 16 * N / T;
   if (p.do_inv || p.do_fwd)
     for (int k = tid; k < N; k += T) tw[k] = p.tw[k];
-
-  const float4* s4 = reinterpret_cast<const float4*>(p.src + gl * p.src_bstride + (size_t)y0 * N);
-  for (int e = tid; e < 8 * N; e += T) {
-    const int r = e / (N / 2);
-    const int x = 2 * (e - r * (N / 2));
-    float4 f = s4[e];
-    tile[tile_idx(x, r)] = make_float2(f.x, f.y);
-    tile[tile_idx(x + 1, r)] = make_float2(f.z, f.w);
+  {
+    const float2* src = p.src + gl * p.src_bstride + (size_t)y0 * N;
+    float2 buf[PER];
+#pragma unroll
+    for (int i = 0; i < PER; i++) buf[i] = src[tid + i * T];
+#pragma unroll
+    for (int i = 0; i < PER; i++) {
+      const int e = tid + i * T;
+      tile[tile_idx(e % N, e / N)] = buf[i];
+    }
   }
   __syncthreads();
 
@@ -186,72 +211,73 @@ row_pass_kernel(RowParams p) {
   else if (p.mean_mode == BPM_MEAN_SIMPLE && p.slice_dn0) dn0 = p.slice_dn0[p.z];
   const bool last = (p.z == p.nz - 1);
   const size_t zoff = (size_t)p.z * plane;
-  for (int e = tid; e < 8 * N; e += T) {
-    const int r = e / (N / 2);
-    const int x = 2 * (e - r * (N / 2));
+  const size_t ooff = (size_t)(p.z - p.zout0) * plane;
+  float2* ckp = nullptr;
+  if (!ADJ && p.ckpt && p.z % p.ckpt_every == 0)
+    ckp = p.ckpt + ((size_t)gl * p.n_ckpt + p.z / p.ckpt_every) * plane;
+  // one element per thread and iteration, consecutive x across a warp: coalesced global
+  // accesses and conflict-free tile accesses
+#pragma unroll 4
+  for (int i = 0; i < PER; i++) {
+    const int e = tid + i * T;
+    const int r = e / N;
+    const int x = e % N;
     const int y = y0 + r;
     const size_t pix = (size_t)y * N + x;
-    float2 v[2] = {tile[tile_idx(x, r)], tile[tile_idx(x + 1, r)]};
+    float2 v = tile[tile_idx(x, r)];
+    if (ADJ) {
+      if (p.z == 0) {
+        if (p.grad_u0) p.grad_u0[gl * plane + pix] = v;
+        continue;
+      }
+      if (p.do_mask) {
+        const float2 u = p.seg[gl * p.seg_bstride + (size_t)(p.z - p.seg_z0) * plane + pix];
+        const float dv = load_dn_real(p.dn, p.dn_dtype, gl * p.dn_bstride + zoff + pix);
+        p.grad_dn[(size_t)gl * p.nz * plane + zoff + pix] = p.unit_k * (v.x * u.y - v.y * u.x);
+        float s, c;
+        sincosf((-p.unit_k) * (dv - dn0), &s, &c);
+        v = cmul(v, make_float2(c, -s));
+        const int dist = min(min(N - 1 - x, x), min(p.ny - 1 - y, y));
+        if (dist < p.absorb) {
+          const float a = p.taper[dist];
+          v.x *= a;
+          v.y *= a;
+        }
+        tile[tile_idx(x, r)] = v;
+      }
+      continue;
+    }
     if (p.do_mask) {
       if (p.dn_dtype == BPM_DN_C64) {
-        const float4 d = __ldg(reinterpret_cast<const float4*>(
-            reinterpret_cast<const float2*>(p.dn) + gl * p.dn_bstride + zoff + pix));
-        const float dre[2] = {d.x, d.z}, dim[2] = {d.y, d.w};
-#pragma unroll
-        for (int q = 0; q < 2; q++) {
-          float m = expf(p.unit_k * dim[q]);
-          float s, c;
-          sincosf((-p.unit_k) * dre[q], &s, &c);
-          v[q] = cmul(v[q], make_float2(m * c, m * s));
-        }
+        const float2 d = __ldg(reinterpret_cast<const float2*>(p.dn) + gl * p.dn_bstride + zoff + pix);
+        const float m = expf(p.unit_k * d.y);
+        float s, c;
+        sincosf((-p.unit_k) * d.x, &s, &c);
+        v = cmul(v, make_float2(m * c, m * s));
       } else {
-        const size_t di = gl * p.dn_bstride + zoff + pix;
-        float dv[2];
-        if (p.dn_dtype == BPM_DN_F16) {
-          __half2 h = *reinterpret_cast<const __half2*>(reinterpret_cast<const __half*>(p.dn) + di);
-          float2 f = __half22float2(h);
-          dv[0] = f.x;
-          dv[1] = f.y;
-        } else {
-          float2 f = __ldg(reinterpret_cast<const float2*>(reinterpret_cast<const float*>(p.dn) + di));
-          dv[0] = f.x;
-          dv[1] = f.y;
-        }
-        const int disty = min(p.ny - 1 - y, y);
-#pragma unroll
-        for (int q = 0; q < 2; q++) {
-          float d = (-p.unit_k) * (dv[q] - dn0);
-          float s, c;
-          sincosf(d, &s, &c);
-          float2 r2 = cmul(v[q], make_float2(c, s));
-          const int xx = x + q;
-          const int dist = min(min(N - 1 - xx, xx), disty);
-          if (dist < p.absorb) {
-            const float a = p.taper[dist];
-            r2.x *= a;
-            r2.y *= a;
-          }
-          v[q] = r2;
+        const float dv = load_dn_real(p.dn, p.dn_dtype, gl * p.dn_bstride + zoff + pix);
+        float s, c;
+        sincosf((-p.unit_k) * (dv - dn0), &s, &c);
+        v = cmul(v, make_float2(c, s));
+        const int dist = min(min(N - 1 - x, x), min(p.ny - 1 - y, y));
+        if (dist < p.absorb) {
+          const float a = p.taper[dist];
+          v.x *= a;
+          v.y *= a;
         }
       }
-      tile[tile_idx(x, r)] = v[0];
-      tile[tile_idx(x + 1, r)] = v[1];
+      tile[tile_idx(x, r)] = v;
     }
-    if (p.out_kind == BPM_OUT_FIELD) {
-      float4* o = reinterpret_cast<float4*>(reinterpret_cast<float2*>(p.out) + gl * p.out_bstride + zoff + pix);
-      __stcs(o, make_float4(v[0].x, v[0].y, v[1].x, v[1].y));
-    } else if (p.out_kind == BPM_OUT_INTENSITY) {
-      float2* o = reinterpret_cast<float2*>(reinterpret_cast<float*>(p.out) + gl * p.out_bstride + zoff + pix);
-      __stcs(o, make_float2(cabs2(v[0]), cabs2(v[1])));
-    }
-    if (last && p.last_plane) {
-      float4* o = reinterpret_cast<float4*>(p.last_plane + gl * plane + pix);
-      *o = make_float4(v[0].x, v[0].y, v[1].x, v[1].y);
-    }
+    if (p.out_kind == BPM_OUT_FIELD)
+      __stcs(reinterpret_cast<float2*>(p.out) + gl * p.out_bstride + ooff + pix, v);
+    else if (p.out_kind == BPM_OUT_INTENSITY)
+      __stcs(reinterpret_cast<float*>(p.out) + gl * p.out_bstride + ooff + pix, cabs2(v));
+    if (last && p.last_plane) p.last_plane[gl * plane + pix] = v;
+    if (ckp) ckp[pix] = v;
   }
 
   // scattering sums of this step: finished by one thread of the first block per field
-  if (p.scat_p && blockIdx.x == 0 && tid == 0) {
+  if (!ADJ && p.scat_p && blockIdx.x == 0 && tid == 0) {
     float* prow = p.scat_p + (size_t)gl * p.nz;
     float* grow = p.scat_g ? p.scat_g + (size_t)gl * p.nz : nullptr;
     if (p.z == 0) {
@@ -273,12 +299,11 @@ row_pass_kernel(RowParams p) {
   if (!p.do_fwd) return;
   __syncthreads();
   tile_fft<N, R, false>(tile, tw);
-  float4* d4 = reinterpret_cast<float4*>(p.W + gl * plane + (size_t)y0 * N);
-  for (int e = tid; e < 8 * N; e += T) {
-    const int r = e / (N / 2);
-    const int x = 2 * (e - r * (N / 2));
-    float2 a = tile[tile_idx(x, r)], b = tile[tile_idx(x + 1, r)];
-    d4[e] = make_float4(a.x, a.y, b.x, b.y);
+  float2* dst = p.W + gl * plane + (size_t)y0 * N;
+#pragma unroll
+  for (int i = 0; i < PER; i++) {
+    const int e = tid + i * T;
+    dst[e] = tile[tile_idx(e % N, e / N)];
   }
 }
 
@@ -303,6 +328,7 @@ struct ColParams {
   float* scat_part;          // [G][ntiles][2]
   double plain_phase;        // k0*n0*dz
   int spi;                   // scattering_plane_ind
+  int conj_h;                // adjoint: multiply by conj(H)
   const float2* tw;
 };
 
@@ -334,23 +360,28 @@ __device__ __forceinline__ void block_sum2(float& a, float& b, float* red) {
 template <int N>
 __device__ __forceinline__ void col_load(float2* tile, const float2* Wp, int nx, int x0) {
   constexpr int T = TileCfg<N>::THREADS;
-  for (int e = threadIdx.x; e < 8 * N; e += T) {
-    const int n = e >> 3;
-    const int c = (e & 7) * 2;
-    float4 f = *reinterpret_cast<const float4*>(Wp + (size_t)n * nx + x0 + c);
-    tile[tile_idx(n, c)] = make_float2(f.x, f.y);
-    tile[tile_idx(n, c + 1)] = make_float2(f.z, f.w);
+  constexpr int PER = 16 * N / T;
+  float2 buf[PER];
+#pragma unroll
+  for (int i = 0; i < PER; i++) {
+    const int e = threadIdx.x + i * T;
+    buf[i] = Wp[(size_t)(e >> 4) * nx + x0 + (e & 15)];
+  }
+#pragma unroll
+  for (int i = 0; i < PER; i++) {
+    const int e = threadIdx.x + i * T;
+    tile[tile_idx(e >> 4, e & 15)] = buf[i];
   }
 }
 
 template <int N>
 __device__ __forceinline__ void col_store(const float2* tile, float2* Wp, int nx, int x0) {
   constexpr int T = TileCfg<N>::THREADS;
-  for (int e = threadIdx.x; e < 8 * N; e += T) {
-    const int n = e >> 3;
-    const int c = (e & 7) * 2;
-    float2 a = tile[tile_idx(n, c)], b = tile[tile_idx(n, c + 1)];
-    *reinterpret_cast<float4*>(Wp + (size_t)n * nx + x0 + c) = make_float4(a.x, a.y, b.x, b.y);
+  constexpr int PER = 16 * N / T;
+#pragma unroll
+  for (int i = 0; i < PER; i++) {
+    const int e = threadIdx.x + i * T;
+    Wp[(size_t)(e >> 4) * nx + x0 + (e & 15)] = tile[tile_idx(e >> 4, e & 15)];
   }
 }
 
@@ -378,6 +409,7 @@ __device__ __forceinline__ void col_propagate(float2* tile, const ColParams& p, 
     float2 h;
     if (p.prop_mode == 0) {
       h = __ldg(p.H + (size_t)y * p.nx + x);
+      if (p.conj_h) h.y = -h.y;
     } else {
       const float tmp = __fsub_rn(__fsub_rn(nk, __ldg(p.kx2 + x)), __ldg(p.ky2 + y));
       if (tmp >= 0.f) {
@@ -411,7 +443,7 @@ __device__ __forceinline__ void col_propagate(float2* tile, const ColParams& p, 
 
 // non-weighted column pass: forward FFT, propagator, inverse FFT
 template <int N>
-__global__ void __launch_bounds__(TileCfg<N>::THREADS)
+__global__ void __launch_bounds__(TileCfg<N>::THREADS, TileCfg<N>::MINB)
 col_pass_kernel(ColParams p) {
   constexpr int R = TileCfg<N>::R;
   extern __shared__ float2 smem[];
@@ -434,7 +466,7 @@ col_pass_kernel(ColParams p) {
 
 // weighted mode, part 1: forward column FFT and the partial sums of |u_hat|*dn0, |u_hat|
 template <int N>
-__global__ void __launch_bounds__(TileCfg<N>::THREADS)
+__global__ void __launch_bounds__(TileCfg<N>::THREADS, TileCfg<N>::MINB)
 col_fwd_reduce_kernel(ColParams p) {
   constexpr int T = TileCfg<N>::THREADS;
   constexpr int R = TileCfg<N>::R;
@@ -469,7 +501,7 @@ col_fwd_reduce_kernel(ColParams p) {
 
 // weighted mode, part 2: n = n00 + dn_sum/u_sum, propagator, inverse column FFT
 template <int N>
-__global__ void __launch_bounds__(TileCfg<N>::THREADS)
+__global__ void __launch_bounds__(TileCfg<N>::THREADS, TileCfg<N>::MINB)
 col_inv_kernel(ColParams p) {
   constexpr int R = TileCfg<N>::R;
   extern __shared__ float2 smem[];
@@ -511,13 +543,19 @@ struct RowK {
   static void prepare() {
     static bool attr = false;
     if (!attr) {
-      cudaFuncSetAttribute(row_pass_kernel<N>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)TileCfg<N>::SMEM);
+      cudaFuncSetAttribute(row_pass_kernel<N, false>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                           (int)TileCfg<N>::SMEM);
+      cudaFuncSetAttribute(row_pass_kernel<N, true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                           (int)TileCfg<N>::SMEM);
       attr = true;
     }
   }
-  static int launch(dim3 g, cudaStream_t s, const RowParams& p) {
+  static int launch(dim3 g, cudaStream_t s, const RowParams& p, bool adj) {
     prepare();
-    row_pass_kernel<N><<<g, TileCfg<N>::THREADS, TileCfg<N>::SMEM, s>>>(p);
+    if (adj)
+      row_pass_kernel<N, true><<<g, TileCfg<N>::THREADS, TileCfg<N>::SMEM, s>>>(p);
+    else
+      row_pass_kernel<N, false><<<g, TileCfg<N>::THREADS, TileCfg<N>::SMEM, s>>>(p);
     BPM_LAUNCH_CHECK("row_pass_kernel");
     return BPM_OK;
   }
@@ -543,15 +581,15 @@ struct ColK {
   }
 };
 
-int launch_row(int N, dim3 g, cudaStream_t s, const RowParams& p) {
+int launch_row(int N, dim3 g, cudaStream_t s, const RowParams& p, bool adj = false) {
   switch (N) {
-    case 16: return RowK<16>::launch(g, s, p);
-    case 32: return RowK<32>::launch(g, s, p);
-    case 64: return RowK<64>::launch(g, s, p);
-    case 128: return RowK<128>::launch(g, s, p);
-    case 256: return RowK<256>::launch(g, s, p);
-    case 512: return RowK<512>::launch(g, s, p);
-    case 1024: return RowK<1024>::launch(g, s, p);
+    case 16: return RowK<16>::launch(g, s, p, adj);
+    case 32: return RowK<32>::launch(g, s, p, adj);
+    case 64: return RowK<64>::launch(g, s, p, adj);
+    case 128: return RowK<128>::launch(g, s, p, adj);
+    case 256: return RowK<256>::launch(g, s, p, adj);
+    case 512: return RowK<512>::launch(g, s, p, adj);
+    case 1024: return RowK<1024>::launch(g, s, p, adj);
   }
   set_error("unsupported nx");
   return BPM_ERR_SHAPE;
@@ -644,6 +682,8 @@ int check_request(const bpm_plan* pl, const bpm_request* r) {
   if (r->out_kind != BPM_OUT_NONE && !r->out) { set_error("out is NULL but out_kind is set"); return BPM_ERR_ARG; }
   if (r->scatter_g && !r->scatter_p) { set_error("scatter_g needs scatter_p"); return BPM_ERR_ARG; }
   if (r->group < 0) { set_error("group must be >= 0"); return BPM_ERR_ARG; }
+  if (r->ckpt && r->ckpt_every < 1) { set_error("ckpt_every must be >= 1 with ckpt"); return BPM_ERR_ARG; }
+  if (r->ckpt && ((uintptr_t)r->ckpt & 15)) { set_error("ckpt must be 16-byte aligned"); return BPM_ERR_ARG; }
   // 16-byte alignment of the vectorised accesses
   auto mis = [](const void* q) { return ((uintptr_t)q & 15) != 0; };
   if (mis(r->u0) || (r->out && mis(r->out)) || (r->last_plane && mis(r->last_plane))) {
@@ -721,6 +761,12 @@ MarchCtx make_ctx(const bpm_plan* pl, const bpm_request* r, void* ws, int b0, in
   rp.tw = pl->tw_x;
   rp.src = W;
   rp.src_bstride = plane;
+  rp.zout0 = 0;
+  if (r->ckpt) {
+    rp.ckpt_every = r->ckpt_every;
+    rp.n_ckpt = (nz - 1) / r->ckpt_every + 1;
+    rp.ckpt = static_cast<float2*>(r->ckpt) + (size_t)b0 * rp.n_ckpt * plane;
+  }
 
   ColParams& cp = c.cp;
   memset(&cp, 0, sizeof(cp));
@@ -800,6 +846,149 @@ int enqueue_march(bpm_plan* pl, const bpm_request* r, void* ws, size_t ws_bytes,
       if ((rc = launch_cols(pl, c, i, 0, s))) return rc;
       if ((rc = launch_row_z(pl, r, c, i + 1, s))) return rc;
     }
+  }
+  return BPM_OK;
+}
+
+// ---------------------------------------------------------------------------------------
+// adjoint march
+// ---------------------------------------------------------------------------------------
+struct BwLayout {
+  size_t fwd, adj, seg, total;
+};
+
+BwLayout bw_layout(const bpm_plan* pl, int G, int k) {
+  BwLayout L;
+  const size_t plane = (size_t)pl->d.nx * pl->d.ny;
+  size_t off = 0;
+  L.fwd = off;
+  off += ws_layout(pl, G).total;
+  L.adj = off;
+  off += ws_layout(pl, G).total;
+  L.seg = off;
+  off += align256((size_t)G * (k + 1) * plane * sizeof(float2));
+  L.total = off;
+  return L;
+}
+
+int check_backward(const bpm_plan* pl, const bpm_request* r, const void* grad_last, const float* grad_dn) {
+  if (pl->d.mean_mode != BPM_MEAN_IGNORE) {
+    set_error("the adjoint is defined for mean_mode='ignore' (the propagator must not depend on dn)");
+    return BPM_ERR_UNSUPPORTED;
+  }
+  if (r->dn_dtype == BPM_DN_C64) {
+    set_error("the adjoint needs real dn");
+    return BPM_ERR_UNSUPPORTED;
+  }
+  if (!r->ckpt || r->ckpt_every < 1) {
+    set_error("the adjoint needs the forward checkpoints (req->ckpt, req->ckpt_every)");
+    return BPM_ERR_ARG;
+  }
+  if (!grad_last || ((uintptr_t)grad_last & 15)) { set_error("grad_last must be a 16-byte aligned pointer"); return BPM_ERR_ARG; }
+  if (r->dn_dtype != BPM_DN_NONE && (!grad_dn || ((uintptr_t)grad_dn & 15))) {
+    set_error("grad_dn must be a 16-byte aligned pointer");
+    return BPM_ERR_ARG;
+  }
+  return BPM_OK;
+}
+
+int enqueue_backward(bpm_plan* pl, const bpm_request* r, const void* grad_last, float* grad_dn, void* grad_u0,
+                     void* ws, size_t ws_bytes, cudaStream_t s) {
+  const bpm_grid_desc& d = pl->d;
+  const int nz = d.nz, k = r->ckpt_every;
+  const int G = group_size(pl, r);
+  BwLayout L = bw_layout(pl, G, k);
+  if (!ws || ws_bytes < L.total || ((uintptr_t)ws & 15)) {
+    set_error("workspace too small or misaligned: need " + std::to_string(L.total) + " bytes");
+    return BPM_ERR_OOM;
+  }
+  char* wsb = static_cast<char*>(ws);
+  const size_t plane = (size_t)d.nx * d.ny;
+  const int n_ckpt = (nz - 1) / k + 1;
+  const int nseg = (nz - 1 + k - 1) / k;  // segments (s*k, min(s*k+k, nz-1)]
+  float2* seg = reinterpret_cast<float2*>(wsb + L.seg);
+  int rc;
+  for (int b0 = 0; b0 < r->batch; b0 += G) {
+    const int Gc = std::min(G, r->batch - b0);
+    // forward recompute context on its own workspace, writing fields into the segment buffer
+    MarchCtx cf = make_ctx(pl, r, wsb + L.fwd, b0, Gc);
+    cf.rp.out = seg;
+    cf.rp.out_kind = BPM_OUT_FIELD;
+    cf.rp.out_bstride = (long long)(k + 1) * plane;
+    cf.rp.last_plane = nullptr;
+    cf.rp.ckpt = nullptr;
+    cf.rp.scat_p = cf.rp.scat_g = nullptr;
+    cf.cp.scat = 0;
+    // adjoint context
+    MarchCtx ca = make_ctx(pl, r, wsb + L.adj, b0, Gc);
+    ca.rp.out = nullptr;
+    ca.rp.out_kind = BPM_OUT_NONE;
+    ca.rp.last_plane = nullptr;
+    ca.rp.ckpt = nullptr;
+    ca.rp.scat_p = ca.rp.scat_g = nullptr;
+    ca.rp.seg = seg;
+    ca.rp.seg_bstride = (long long)(k + 1) * plane;
+    ca.rp.grad_dn = grad_dn ? grad_dn + (size_t)b0 * nz * plane : nullptr;
+    ca.rp.grad_u0 = grad_u0 ? static_cast<float2*>(grad_u0) + (size_t)b0 * plane : nullptr;
+    ca.cp.scat = 0;
+    ca.cp.conj_h = 1;
+    const float2* ck = static_cast<const float2*>(r->ckpt) + (size_t)b0 * n_ckpt * plane;
+    const float2* gl = static_cast<const float2*>(grad_last) + (size_t)b0 * plane;
+    for (int sgi = nseg - 1; sgi >= 0; sgi--) {
+      const int zs = sgi * k, ze = std::min(zs + k, nz - 1);
+      // recompute planes zs..ze of the forward march from checkpoint sgi
+      RowParams rp = cf.rp;
+      rp.src = ck + (size_t)sgi * plane;
+      rp.src_bstride = (long long)n_ckpt * plane;
+      rp.z = zs;
+      rp.zout0 = zs;
+      rp.do_inv = 0;
+      rp.do_fwd = 1;
+      rp.do_mask = 0;
+      if ((rc = launch_row(d.nx, cf.grow, s, rp))) return rc;
+      for (int i = zs; i < ze; i++) {
+        cf.cp.z = i;
+        if ((rc = launch_col<0>(d.ny, cf.gcol, s, cf.cp))) return rc;
+        rp = cf.rp;
+        rp.z = i + 1;
+        rp.zout0 = zs;
+        rp.do_inv = 1;
+        rp.do_fwd = (i + 1 < ze);
+        rp.do_mask = r->dn_dtype != BPM_DN_NONE;
+        if ((rc = launch_row(d.nx, cf.grow, s, rp))) return rc;
+      }
+      // march the adjoint from plane ze down to plane zs
+      for (int z = ze; z > zs; z--) {
+        RowParams ra = ca.rp;
+        ra.z = z;
+        ra.seg_z0 = zs;
+        ra.do_mask = r->dn_dtype != BPM_DN_NONE;
+        ra.do_fwd = 1;
+        if (z == nz - 1) {
+          ra.src = gl;
+          ra.src_bstride = plane;
+          ra.do_inv = 0;
+        } else {
+          ra.do_inv = 1;
+        }
+        if ((rc = launch_row(d.nx, ca.grow, s, ra, true))) return rc;
+        ca.cp.z = z - 1;
+        if ((rc = launch_col<0>(d.ny, ca.gcol, s, ca.cp))) return rc;
+      }
+    }
+    // plane 0: the adjoint there is the u0 gradient
+    RowParams ra = ca.rp;
+    ra.z = 0;
+    ra.do_mask = 0;
+    ra.do_fwd = 0;
+    if (nz == 1) {
+      ra.src = gl;
+      ra.src_bstride = plane;
+      ra.do_inv = 0;
+    } else {
+      ra.do_inv = 1;
+    }
+    if ((rc = launch_row(d.nx, ca.grow, s, ra, true))) return rc;
   }
   return BPM_OK;
 }
@@ -958,6 +1147,23 @@ extern "C" int bpm_launch_pass(bpm_plan* pl, const bpm_request* r, void* ws, siz
   }
   set_error("unknown pass kind");
   return BPM_ERR_ARG;
+}
+
+extern "C" size_t bpm_backward_workspace_bytes(const bpm_plan* pl, int batch, int group, int ckpt_every) {
+  if (!pl || batch < 1 || ckpt_every < 1) return 0;
+  const int G = group > 0 ? std::min(group, batch) : default_group(pl, batch);
+  return bw_layout(pl, G, ckpt_every).total;
+}
+
+extern "C" int bpm_backward(bpm_plan* pl, const bpm_request* r, const void* grad_last, float* grad_dn,
+                            void* grad_u0, void* ws, size_t ws_bytes, void* stream) {
+  clear_error();
+  if (!pl) { set_error("plan is NULL"); return BPM_ERR_ARG; }
+  int rc = check_request(pl, r);
+  if (rc) return rc;
+  if ((rc = check_backward(pl, r, grad_last, grad_dn))) return rc;
+  if (grad_u0 && ((uintptr_t)grad_u0 & 15)) { set_error("grad_u0 must be 16-byte aligned"); return BPM_ERR_ARG; }
+  return enqueue_backward(pl, r, grad_last, grad_dn, grad_u0, ws, ws_bytes, static_cast<cudaStream_t>(stream));
 }
 
 extern "C" int bpm_exec_create(bpm_plan* pl, const bpm_request* r, void* ws, size_t ws_bytes, bpm_exec** out) {

@@ -175,6 +175,8 @@ struct TileCfg {
   static constexpr int R = (N <= 8) ? N : (N <= 256 ? 8 : 16);
   static constexpr int THREADS = 16 * N / R;
   static constexpr size_t SMEM = (size_t)N * 16 * sizeof(float2) + (size_t)N * sizeof(float2);
+  // blocks per SM the register budget must allow: 2048 threads per SM, i.e. 64 registers
+  static constexpr int MINB = THREADS >= 1024 ? 1 : 1024 / THREADS;
 };
 
 }  // namespace bpmgb

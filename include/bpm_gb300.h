@@ -97,6 +97,9 @@ typedef struct {
   float* scatter_g;              /* device (batch, nz) anisotropy g (needs scatter_p), or NULL  */
   int scattering_plane_ind;      /* z offset of the plain-wave reference, bpm_3d.py:253         */
   int group;                     /* fields marched together per pass (0 = library default)      */
+  void* ckpt;                    /* device (batch, (nz-1)/ckpt_every+1, ny, nx) complex64: the
+                                    field at planes z = 0, k, 2k, ... (k = ckpt_every), or NULL  */
+  int ckpt_every;                /* checkpoint spacing k (>= 1 when ckpt is set)                */
 } bpm_request;
 
 /* Library version (BPM_GB300_VERSION). */
@@ -158,6 +161,23 @@ int bpm_exec_create(bpm_plan* plan, const bpm_request* req, void* workspace, siz
                     bpm_exec** out);
 int bpm_exec_launch(bpm_exec* exec, void* stream);
 int bpm_exec_destroy(bpm_exec* exec);
+
+/* Bytes of scratch bpm_backward needs (256-aligned). */
+size_t bpm_backward_workspace_bytes(const bpm_plan* plan, int batch, int group, int ckpt_every);
+
+/* Adjoint of the march for mean_mode "ignore" with real (f32 / f16) or no dn: given
+ * grad_last = dL/dRe(u_last) + i dL/dIm(u_last) for the exit planes, (batch, ny, nx)
+ * complex64, write the gradient of L with respect to each field's dn into grad_dn
+ * (batch, nz, ny, nx) float32 (plane z >= 1 written; plane 0 left untouched: plane 0 of
+ * the march is u0, which dn does not reach) and, if grad_u0 is not NULL, the gradient
+ * with respect to u0 into grad_u0 (batch, ny, nx) complex64. The request must be the one
+ * the forward bpm_propagate ran with, including its checkpoints (req->ckpt,
+ * req->ckpt_every): each segment between checkpoints is recomputed forward, then marched
+ * backward with the conjugate propagator and conjugate phase masks.
+ * No reference counterpart (the reference has no gradient; bpm/bpm/bpm_3d_inverse.py is a
+ * non-functional sketch). */
+int bpm_backward(bpm_plan* plan, const bpm_request* req, const void* grad_last, float* grad_dn,
+                 void* grad_u0, void* workspace, size_t workspace_bytes, void* stream);
 
 /* ---------------------------------------------------------------------------------- */
 /* Vectorial Debye-Wolf focus field                                                    */

@@ -190,13 +190,15 @@ def _bpm_3d(size, units, lam=.5, u0=None, dn=None, subsample=1, n0=1.,
     dn_dev = None
     if dn is not None:
         dn = np.asarray(dn)
+        # the reference uploads dn as complex64 / float16 / float32 (bpm_3d.py:198-211); the
+        # FP64 flavour keeps the caller's values (finite differences need them unrounded)
         if dn.dtype.type in (np.complex64, np.complex128):
             is_complex_dn = True
-            dn_dev = dn.astype(np.complex64).astype(ctype)
+            dn_dev = dn.astype(np.complex64).astype(ctype) if fp32 else dn.astype(ctype)
         elif store_dn_as_half:
             dn_dev = half_to_f32(dn).astype(rtype)
         else:
-            dn_dev = dn.astype(np.float32).astype(rtype)
+            dn_dev = dn.astype(np.float32).astype(rtype) if fp32 else dn.astype(rtype)
         if is_complex_dn and mean_mode != "ignore":
             raise NotImplementedError("complex dn is only defined for mean_mode='ignore'")
     dn_mean = np.mean(dn, axis=(1, 2)) if dn is not None else np.zeros(Nz, np.float32)

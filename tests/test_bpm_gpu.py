@@ -117,7 +117,11 @@ def test_scattering_outputs(bpm):
         assert p[0] == 0 and np.isnan(g[0])
         assert rel_l2(u, uo) < TOL
         assert rel_l2(p[1:], po[1:]) < 1e-3
-        assert rel_l2(g[1:], go[1:]) < 1e-3
+        # g = G/p is 0/0 where nothing has scattered yet (p at rounding level): compare
+        # where the scattered power is resolved in FP32
+        sel = po > 1e-3 * po.max()
+        assert sel.sum() > 5
+        assert rel_l2(g[sel], go[sel]) < 1e-3
 
 
 def test_split_matches_oracle_and_field_intensity(bpm):
@@ -202,8 +206,8 @@ def test_graph_replay_equals_direct(bpm):
                                 .astype(np.complex64)))
     m.run()
     torch.cuda.synchronize()
-    direct = bpm.bpm_3d_batched(size, (.1, .1, .1), u0=m.u0.cpu().numpy(), dn=dn)
-    assert np.array_equal(m.out.cpu().numpy(), direct)
+    direct = bpm.bpm_3d_batched(size, (.1, .1, .1), lam=.5, n0=1.33, u0=m.u0.cpu().numpy(), dn=dn)
+    assert bool(np.array_equal(m.out.cpu().numpy(), direct))
     n0 = bpm.launch_count()
     m.run()
     torch.cuda.synchronize()
