@@ -464,6 +464,7 @@ def main():
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--group", type=int, default=0, help="fields per pass (0 = library default)")
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-serve", action="store_true", help="skip the serving trace")
     ap.add_argument("--batch", type=int, default=BATCH, help="fields per GPU (smaller for profiling)")
     ap.add_argument("--nz", type=int, default=NZ, help="z planes (smaller for profiling)")
     ap.add_argument("--profile", action="store_true",
@@ -493,6 +494,8 @@ def main():
         torch.distributed.init_process_group("nccl")
     res = bench_ours(args, rank, world, local_rank)
     if rank == 0:
+        if not args.no_serve:
+            res["serve"] = serve_trace()
         if not args.no_cpu_baseline:
             v, t, sample = cpu_sample(4, NZ - 1)
             res["cpu_baseline"] = {"value": v, "unit": "voxel-updates/s", "cores": host_cores(), "kind": "port",
