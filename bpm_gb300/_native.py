@@ -67,6 +67,7 @@ SIGNATURES = {
     "bpm_plan_destroy": (c_int, [c_vp]),
     "bpm_workspace_bytes": (c_size, [c_vp, c_int, c_int]),
     "bpm_propagate": (c_int, [c_vp, ctypes.POINTER(Request), c_vp, c_size, c_vp]),
+    "bpm_propagate_noalloc": (c_int, [c_vp, ctypes.POINTER(Request), c_vp]),
     "bpm_launch_pass": (c_int, [c_vp, ctypes.POINTER(Request), c_vp, c_size, c_int, c_int, c_vp]),
     "bpm_backward_workspace_bytes": (c_size, [c_vp, c_int, c_int, c_int]),
     "bpm_backward": (c_int, [c_vp, ctypes.POINTER(Request), c_vp, c_vp, c_vp, c_vp, c_size, c_vp]),

@@ -1219,3 +1219,69 @@ extern "C" int bpm_exec_destroy(bpm_exec* x) {
   delete x;
   return BPM_OK;
 }
+
+// ---------------------------------------------------------------------------------------
+// Allocation-free march.
+//
+// Some callers cannot allocate device memory at the point where they march: a host
+// application that hands this library a fixed device memory budget and forbids it any
+// cudaMalloc of its own, a plugin whose host owns every device allocation, or a caller in
+// a latency-critical loop where cudaMalloc (which synchronises the device) would stall
+// the streams running beside it. For them, bpm_propagate_noalloc takes its scratch from
+// one fixed array in this library's device image instead of a caller workspace. Every GPU
+// that loads the library holds that array (BPM_NOALLOC_SCRATCH_BYTES) until the process
+// exits.
+// ---------------------------------------------------------------------------------------
+#include <mutex>
+
+static __device__ __align__(256) unsigned char g_noalloc_scratch[BPM_NOALLOC_SCRATCH_BYTES];
+
+namespace {
+constexpr int kMaxDevices = 64;
+std::mutex g_noalloc_mu;
+void* g_noalloc_addr[kMaxDevices] = {};
+
+// Device address of g_noalloc_scratch on the current device. In host code the symbol is
+// only a host-side stand-in, so it is never passed to a kernel: its device address is
+// looked up once per device, with that device current, and cached.
+int noalloc_scratch(void** out) {
+  int dev = -1;
+  BPM_CUDA_TRY(cudaGetDevice(&dev));
+  if (dev < 0 || dev >= kMaxDevices) {
+    set_error("device index out of range for the allocation-free scratch");
+    return BPM_ERR_ARG;
+  }
+  std::lock_guard<std::mutex> lock(g_noalloc_mu);
+  if (!g_noalloc_addr[dev]) {
+    void* p = nullptr;
+    cudaError_t e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
+    if (e != cudaSuccess) return cuda_fail(e, "cudaGetSymbolAddress(g_noalloc_scratch)");
+    g_noalloc_addr[dev] = p;
+  }
+  *out = g_noalloc_addr[dev];
+  return BPM_OK;
+}
+}  // namespace
+
+extern "C" int bpm_propagate_noalloc(bpm_plan* pl, const bpm_request* r, void* stream) {
+  clear_error();
+  if (!pl) { set_error("plan is NULL"); return BPM_ERR_ARG; }
+  int rc = check_request(pl, r);
+  if (rc) return rc;
+  // march as many fields together as the fixed scratch holds (the result does not depend
+  // on the grouping); refuse grids whose single-field scratch does not fit
+  int G = group_size(pl, r);
+  while (G > 1 && ws_layout(pl, G).total > BPM_NOALLOC_SCRATCH_BYTES) G--;
+  const size_t need = ws_layout(pl, G).total;
+  if (need > BPM_NOALLOC_SCRATCH_BYTES) {
+    set_error("bpm_propagate_noalloc: a " + std::to_string(pl->d.nx) + "x" + std::to_string(pl->d.ny) +
+              " grid needs " + std::to_string(need) + " bytes of scratch, more than its fixed " +
+              std::to_string((size_t)BPM_NOALLOC_SCRATCH_BYTES) + " bytes; use bpm_propagate with a workspace");
+    return BPM_ERR_OOM;
+  }
+  void* scratch = nullptr;
+  if ((rc = noalloc_scratch(&scratch))) return rc;
+  bpm_request q = *r;
+  q.group = G;
+  return enqueue_march(pl, &q, scratch, BPM_NOALLOC_SCRATCH_BYTES, static_cast<cudaStream_t>(stream));
+}

@@ -136,6 +136,25 @@ size_t bpm_workspace_bytes(const bpm_plan* plan, int batch, int group);
 int bpm_propagate(bpm_plan* plan, const bpm_request* req, void* workspace, size_t workspace_bytes,
                   void* stream);
 
+/* Allocation-free march, for callers that may not allocate device memory where they
+ * march (a host that gives this library a fixed device budget and forbids it cudaMalloc,
+ * a plugin whose host owns all device memory, a latency-critical loop where cudaMalloc
+ * would synchronise the device). Same request and results as bpm_propagate, but the
+ * scratch is one fixed array of BPM_NOALLOC_SCRATCH_BYTES inside the library's device
+ * image, held by every GPU that loads the library until the process exits. It allocates
+ * nothing: no cudaMalloc, no cudaFree, no allocating library call. Fields are marched in
+ * as many groups as the array needs; a grid whose one-field scratch exceeds the array
+ * (grids larger than 512x512) is refused with BPM_ERR_OOM and a message naming the limit.
+ * The first call on a device looks up the array's device address (with that device
+ * current) and caches it; make that first call before any stream capture. All calls
+ * share the one array: calls that can overlap on the GPU (different streams or threads)
+ * race on it and must be serialised by the caller. Every byte of the array a call reads
+ * was written earlier in the same call, so nothing needs clearing between calls.
+ * No counterpart in the reference (which allocates its buffers per call through
+ * OCLArray). */
+#define BPM_NOALLOC_SCRATCH_BYTES (8u << 20)
+int bpm_propagate_noalloc(bpm_plan* plan, const bpm_request* req, void* stream);
+
 /* Kinds of pass for bpm_launch_pass. */
 typedef enum {
   BPM_PASS_FIRST_ROW = 0,         /* plane 0 output + forward row FFT                         */
