@@ -165,8 +165,9 @@ def bench_ours(args, rank, world, local_rank):
 
     dn = make_dn_device(NX, NY, NZ, SEED)
     u0 = torch.from_numpy(make_u0(BATCH, NX, NY, SEED + 1)).to(dev)
+    # fields per launch: the autotuner's choice (a short untimed probe march) unless --group
     march = bpm_gb300.BatchedMarch((NX, NY, NZ), UNITS, LAM, N0, BATCH, dn=dn, mean_mode=MODE,
-                                   out_kind="intensity", group=args.group)
+                                   out_kind="intensity", group=args.group or "auto")
     march.u0.copy_(u0)
     stream = torch.cuda.current_stream()
 
@@ -198,7 +199,7 @@ def bench_ours(args, rank, world, local_rank):
     # per-kernel times of one group (CUDA events around single passes)
     req, ws, wsb = march.req, march.ws, march.ws_bytes
     L = N.lib()
-    grp = args.group if args.group > 0 else default_group(NX, BATCH)
+    grp = march.group_used
 
     def time_pass(kind, z, reps=20):
         for _ in range(3):
@@ -229,7 +230,7 @@ def bench_ours(args, rank, world, local_rank):
     row_flops = vox * (2 * 5 * log2n + 12)           # inverse + forward row FFT, mask, |u|^2
     col_flops = vox * (2 * 5 * int(np.log2(NY)) + 8)  # forward + inverse column FFT, propagator
     fp32_peak = fp32_peak_tflops(clocks.get("sm_mhz"))
-    traffic = profile_traffic()
+    traffic = profile_traffic(grp)
 
     # plain: one field per request through the same library, no graph
     plain = bpm_gb300.BatchedMarch((NX, NY, NZ), UNITS, LAM, N0, 1, dn=dn, mean_mode=MODE,
@@ -260,12 +261,12 @@ def bench_ours(args, rank, world, local_rank):
     e2e_steps = max(1, min(args.steps, 3))
     for _ in range(1):
         bpm_gb300.bpm_3d_batched((NX, NY, NZ), UNITS, lam=LAM, u0=u0_h, dn=dn_h, n0=N0, return_field=False,
-                                 mean_mode=MODE, group=args.group, out=out_h)
+                                 mean_mode=MODE, group=grp, out=out_h)
     barrier()
     t0 = time.perf_counter()
     for _ in range(e2e_steps):
         bpm_gb300.bpm_3d_batched((NX, NY, NZ), UNITS, lam=LAM, u0=u0_h, dn=dn_h, n0=N0, return_field=False,
-                                 mean_mode=MODE, group=args.group, out=out_h)
+                                 mean_mode=MODE, group=grp, out=out_h)
     barrier()
     t_e2e = (time.perf_counter() - t0) / e2e_steps
     if world > 1:
@@ -397,20 +398,17 @@ def profile_run(args):
     print(json.dumps({"profile_run": True, "batch": BATCH, "nz": NZ, "launches": bpm_gb300.launch_count()}))
 
 
-def default_group(nx, batch):
-    plane = nx * nx * 8
-    g_l2 = max(1, (48 << 20) // plane)
-    g_fill = max(1, (152 * 4) // max(1, nx // 16))
-    return max(1, min(min(g_l2, g_fill), batch))
 
-
-def profile_traffic():
-    """DRAM bytes per row-pass launch from the committed ncu summary, if one exists."""
+def profile_traffic(fields):
+    """DRAM bytes of one row-pass launch over `fields` fields: the committed ncu capture's
+    per-field figure (dram__bytes_read.sum + dram__bytes_write.sum, captured on a smaller
+    batch of the same 512x512 kernel) scaled by the fields the bench's launch processes."""
     p = os.path.join(ROOT, "profiles", "row_pass_512_traffic.json")
     if os.path.exists(p):
         try:
-            return float(json.load(open(p))["dram_bytes_per_launch"])
-        except (KeyError, ValueError):
+            d = json.load(open(p))
+            return float(d["dram_bytes_per_launch"]) / float(d["fields_per_launch"]) * fields
+        except (KeyError, ValueError, ZeroDivisionError):
             return None
     return None
 

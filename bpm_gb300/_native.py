@@ -46,7 +46,7 @@ class Request(ctypes.Structure):
                 ("out", c_vp), ("out_kind", c_int), ("out_batch_stride", c_ll),
                 ("last_plane", c_vp), ("scatter_p", c_vp), ("scatter_g", c_vp),
                 ("scattering_plane_ind", c_int), ("group", c_int),
-                ("ckpt", c_vp), ("ckpt_every", c_int)]
+                ("ckpt", c_vp), ("ckpt_every", c_int), ("mask", c_vp)]
 
 
 class DebyeDesc(ctypes.Structure):
@@ -65,8 +65,10 @@ SIGNATURES = {
     "bpm_grid_check": (c_int, [ctypes.POINTER(GridDesc)]),
     "bpm_plan_create": (c_int, [ctypes.POINTER(GridDesc), ctypes.POINTER(c_vp)]),
     "bpm_plan_destroy": (c_int, [c_vp]),
+    "bpm_group_size": (c_int, [c_vp, c_int, c_int]),
     "bpm_workspace_bytes": (c_size, [c_vp, c_int, c_int]),
     "bpm_propagate": (c_int, [c_vp, ctypes.POINTER(Request), c_vp, c_size, c_vp]),
+    "bpm_mask_precompute": (c_int, [c_vp, c_vp, c_int, c_vp, c_vp]),
     "bpm_propagate_noalloc": (c_int, [c_vp, ctypes.POINTER(Request), c_vp]),
     "bpm_launch_pass": (c_int, [c_vp, ctypes.POINTER(Request), c_vp, c_size, c_int, c_int, c_vp]),
     "bpm_backward_workspace_bytes": (c_size, [c_vp, c_int, c_int, c_int]),

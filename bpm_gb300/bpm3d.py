@@ -167,8 +167,18 @@ def _slice_tables(dn, n0, dev):
             torch.from_numpy(np.ascontiguousarray(sd, np.float32)).to(dev))
 
 
+def precompute_mask(plan, dn_t, dn_kind):
+    """Phase masks (Nz, Ny, Nx) complex64 of a shared dn volume (bpm_mask_precompute), for
+    batches: every field then reads them instead of re-evaluating exp(-i k0 dz dn)."""
+    Nx, Ny, Nz = plan.size
+    mask = torch.empty((Nz, Ny, Nx), dtype=torch.complex64, device=dn_t.device)
+    N.check(N.lib().bpm_mask_precompute(plan.handle, _ptr(dn_t), dn_kind, _ptr(mask), _stream_ptr()),
+            "bpm_mask_precompute")
+    return mask
+
+
 def _run(plan, u0_t, dn_t, dn_kind, dn_bstride, out_kind, want_last=True, scattering=False,
-         return_g=False, scattering_plane_ind=0, slice_tabs=(None, None), group=0):
+         return_g=False, scattering_plane_ind=0, slice_tabs=(None, None), group=0, mask=None):
     """Launch bpm_propagate on the current stream. u0_t: (B, Ny, Nx) complex64 CUDA tensor."""
     Nx, Ny, Nz = plan.size
     B = u0_t.shape[0]
@@ -185,7 +195,7 @@ def _run(plan, u0_t, dn_t, dn_kind, dn_bstride, out_kind, want_last=True, scatte
     ws = torch.empty(wsb, dtype=torch.uint8, device=dev)
     req = N.Request(B, _ptr(u0_t), _ptr(dn_t), dn_kind, int(dn_bstride), _ptr(slice_tabs[0]),
                     _ptr(slice_tabs[1]), _ptr(out), out_kind, Nz * Ny * Nx, _ptr(last), _ptr(p),
-                    _ptr(g), int(scattering_plane_ind), int(group))
+                    _ptr(g), int(scattering_plane_ind), int(group), None, 0, _ptr(mask))
     N.check(N.lib().bpm_propagate(plan.handle, ctypes.byref(req), _ptr(ws), wsb, _stream_ptr()),
             "bpm_propagate")
     return out, last, p, g
@@ -389,7 +399,16 @@ def bpm_3d_batched(size, units, lam=.5, u0=None, dn=None, n0=1., return_full=Tru
     else:
         tabs = (None, None)
     out_kind = (N.OUT_FIELD if return_field else N.OUT_INTENSITY) if return_full else N.OUT_NONE
-    vol, last, _, _ = _run(plan, u0_t, dn_t, kind, bstride, out_kind, True, slice_tabs=tabs, group=group)
+    mask = precompute_mask(plan, dn_t, kind) if (dn_t is not None and bstride == 0 and B >= 2) else None
+    if out is not None and return_full:
+        host = torch.from_numpy(out) if isinstance(out, np.ndarray) else out
+        vdt = torch.complex64 if return_field else torch.float32
+        if tuple(host.shape) != (B, Nz, Ny, Nx) or host.dtype != vdt:
+            raise ValueError("out must have shape %s and dtype %s" % ((B, Nz, Ny, Nx), vdt))
+        _run_to_host(plan, u0_t, dn_t, kind, bstride, out_kind, tabs, group, mask, host)
+        return out
+    vol, last, _, _ = _run(plan, u0_t, dn_t, kind, bstride, out_kind, True, slice_tabs=tabs, group=group,
+                           mask=mask)
     res = vol if return_full else (last if return_field else last.abs() ** 2)
     if out is not None:
         host = torch.from_numpy(out) if isinstance(out, np.ndarray) else out
@@ -401,6 +420,47 @@ def bpm_3d_batched(size, units, lam=.5, u0=None, dn=None, n0=1., return_full=Tru
     return res if as_tensor else _d2h(res)
 
 
+def _run_to_host(plan, u0_t, dn_t, kind, bstride, out_kind, tabs, group, mask, host):
+    """March a batch in chunks of fields into two alternating device volumes while a copy
+    stream drains the previous chunk to the host buffer, so the device->host copy of the
+    output volumes overlaps the march of the next chunk."""
+    Nx, Ny, Nz = plan.size
+    B = u0_t.shape[0]
+    dev = u0_t.device
+    G = int(N.lib().bpm_group_size(plan.handle, B, int(group)))
+    chunk = max(G, -(-B // 4))
+    chunk = -(-chunk // G) * G
+    vdt = torch.complex64 if out_kind == N.OUT_FIELD else torch.float32
+    bufs = [torch.empty((min(chunk, B), Nz, Ny, Nx), dtype=vdt, device=dev) for _ in range(2 if B > chunk else 1)]
+    last = torch.empty((min(chunk, B), Ny, Nx), dtype=torch.complex64, device=dev)
+    wsb = plan.workspace_bytes(min(chunk, B), group)
+    ws = torch.empty(wsb, dtype=torch.uint8, device=dev)
+    cs = torch.cuda.current_stream()
+    copy_s = torch.cuda.Stream(device=dev)
+    copied = [None, None]
+    for k, b0 in enumerate(range(0, B, chunk)):
+        nb = min(chunk, B - b0)
+        buf = bufs[k % len(bufs)]
+        if copied[k % 2] is not None:
+            cs.wait_event(copied[k % 2])          # the copy out of this buffer has finished
+        dn_k = dn_t[b0:b0 + nb] if (dn_t is not None and bstride) else dn_t
+        req = N.Request(nb, _ptr(u0_t[b0:b0 + nb]), _ptr(dn_k), kind, int(bstride), _ptr(tabs[0]),
+                        _ptr(tabs[1]), _ptr(buf), out_kind, Nz * Ny * Nx, _ptr(last), None, None, 0,
+                        int(group), None, 0, _ptr(mask))
+        N.check(N.lib().bpm_propagate(plan.handle, ctypes.byref(req), _ptr(ws), wsb, _stream_ptr()),
+                "bpm_propagate")
+        done = torch.cuda.Event()
+        done.record(cs)
+        copy_s.wait_event(done)
+        with torch.cuda.stream(copy_s):
+            host[b0:b0 + nb].copy_(buf[:nb], non_blocking=True)
+            ev = torch.cuda.Event()
+            ev.record(copy_s)
+        copied[k % 2] = ev
+    copy_s.synchronize()
+    cs.synchronize()
+
+
 class BatchedMarch:
     """A fixed batched march with resident buffers, captured once as a CUDA graph
     (bpm_exec_create) and replayed by run(). Inputs u0 (B, Ny, Nx) and dn live on the
@@ -408,7 +468,7 @@ class BatchedMarch:
 
     def __init__(self, size, units, lam, n0, batch, dn=None, mean_mode="weighted", absorbing_width=0,
                  out_kind="intensity", prop_kind=N.PROP_FUNCTIONAL, group=0, store_dn_as_half=False,
-                 use_graph=True):
+                 use_graph=True, use_mask=True):
         dev = _device()
         Nx, Ny, Nz = (int(s) for s in size)
         self.size = (Nx, Ny, Nz)
@@ -428,12 +488,21 @@ class BatchedMarch:
         elif ok == N.OUT_INTENSITY:
             self.out = torch.empty((batch, Nz, Ny, Nx), dtype=torch.float32, device=dev)
         self.last = torch.empty((batch, Ny, Nx), dtype=torch.complex64, device=dev)
+        if group == "auto":
+            from .autotune import tune_group
+            group = tune_group(self.size, units, lam, n0, batch, dn if dn is None else self.dn, mean_mode,
+                               out_kind, absorbing_width)
         self.group = int(group)
+        self.group_used = int(N.lib().bpm_group_size(self.plan.handle, self.batch, self.group))
         self.ws_bytes = self.plan.workspace_bytes(batch, group)
         self.ws = torch.empty(self.ws_bytes, dtype=torch.uint8, device=dev)
+        # the phase masks of a shared dn are computed once and reused by every run
+        self.mask = (precompute_mask(self.plan, self.dn, kind)
+                     if (self.dn is not None and self.dn_bstride == 0 and use_mask) else None)
         self.req = N.Request(self.batch, _ptr(self.u0), _ptr(self.dn), kind, self.dn_bstride,
                              _ptr(self.tabs[0]), _ptr(self.tabs[1]), _ptr(self.out), ok,
-                             Nz * Ny * Nx, _ptr(self.last), None, None, 0, self.group)
+                             Nz * Ny * Nx, _ptr(self.last), None, None, 0, self.group, None, 0,
+                             _ptr(self.mask))
         self.exec = None
         if use_graph:
             torch.cuda.synchronize()

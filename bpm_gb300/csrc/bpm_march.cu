@@ -30,6 +30,7 @@
 
 #include "common.cuh"
 #include "fft_tile.cuh"
+#include "warp_fft.cuh"
 
 using namespace bpmgb;
 
@@ -40,6 +41,8 @@ struct bpm_plan {
   int device;
   float2* tw_x;     // W_nx^k
   float2* tw_y;     // W_ny^k
+  float2* wtw_x;    // stage-ordered twiddles of the warp FFT along x (128 <= nx <= 512)
+  float2* wtw_y;    // ... along y
   float* kx2;       // (2.f*M_PI*FFTFREQ(i,nx,dx))^2, FP32 recipe
   float* ky2;
   float2* H;        // unnormalised propagator table (IGNORE mean mode), (ny, nx)
@@ -48,7 +51,13 @@ struct bpm_plan {
   float* gw;        // g-factor weights cos(theta)^2
   float k0f, dzf, n0f, unit_k;
   double k0;
+  // streams on which groups of fields march concurrently, with their fork/join events
+  cudaStream_t aux[4];
+  cudaEvent_t ev_fork, ev_join[4];
 };
+
+// field groups a batch may march at the same time (one workspace slot each)
+constexpr int kMaxConcurrentGroups = 4;
 
 struct bpm_exec {
   cudaGraphExec_t exec;
@@ -68,6 +77,26 @@ float fftfreq_f32(int i, int N, float d) {  // FFTFREQ, bpm_3d_kernels.cl:6
   f = f / (float)N;
   f = f / d;
   return f;
+}
+
+// stage-ordered twiddle table of the warp FFT (layout documented at wtw_offset), FP64
+std::vector<float2> warp_twiddles(int N) {
+  std::vector<float2> w(wtw_size(N));
+  const int E = N / 32;
+  int ns = 1;
+  while (ns < N) {
+    const int rs = std::min(E, N / ns);
+    if (ns > 1) {
+      const int off = wtw_offset(N, ns);
+      for (int r = 1; r < rs; r++)
+        for (int jm = 0; jm < ns; jm++) {
+          const double a = -2. * M_PI * (double)((long)jm * r * (N / (ns * rs))) / N;
+          w[off + (r - 1) * ns + jm] = make_float2((float)cos(a), (float)sin(a));
+        }
+    }
+    ns *= rs;
+  }
+  return w;
 }
 
 float taper_value(int dist, int absorb) {  // bpm_3d_kernels.cl:36
@@ -148,12 +177,14 @@ struct RowParams {
   float* scat_g;
   float prefac_f;
   const float2* tw;
+  const float2* wtw;        // stage-ordered twiddles of the warp FFT
   // adjoint passes only
   const float2* seg;        // forward fields of the current segment (G, planes, ny, nx)
   long long seg_bstride;    // float2 elements between fields
   int seg_z0;               // plane index of the segment's first plane
   float* grad_dn;           // group's (nz, ny, nx) dn gradients
   float2* grad_u0;          // group's (ny, nx) u0 gradients or NULL
+  const float2* mask;       // precomputed masks of the shared dn, (nz, ny, nx), or NULL
 };
 
 __device__ __forceinline__ float load_dn_real(const void* dn, int dtype, size_t idx) {
@@ -166,6 +197,125 @@ __device__ __forceinline__ float2 load_dn_pair(const void* dn, int dtype, size_t
   if (dtype == BPM_DN_F16)
     return __half22float2(*reinterpret_cast<const __half2*>(reinterpret_cast<const __half*>(dn) + idx));
   return __ldg(reinterpret_cast<const float2*>(reinterpret_cast<const float*>(dn) + idx));
+}
+
+// The pointwise work of a row pass on one element v = u(x, y) of plane z, shared by the
+// tile and warp row kernels. Forward: phase mask of dn slice z (+ taper) and the plane-z
+// outputs. Adjoint: dn gradient against the forward field, conjugate mask; at plane 0 the
+// adjoint value is the u0 gradient.
+// Phase mask of dn slice z at (x, y): M = taper * exp(-i k0 dz dn) for real dn
+// (mult_dn*, bpm_3d_kernels.cl:20-81, 198-262), exp(k0 dz Im dn) * exp(-i k0 dz Re dn) with
+// no taper for complex dn (mult_dn*_complex, :84-101, :265-283). The mean-index shift dn0
+// enters as the separate factor exp(+i k0 dz dn0) (row_rot), so M depends on dn alone and
+// can be computed once per dn volume for a whole batch (bpm_mask_precompute); the on-the-fly
+// and precomputed masks are the same FP32 arithmetic, bit for bit.
+__device__ __forceinline__ float2 mask_value(const void* dn, int dtype, size_t idx, float unit_k, int x, int y,
+                                             int nx, int ny, int absorb, const float* taper) {
+  float s, c;
+  if (dtype == BPM_DN_C64) {
+    const float2 d = __ldg(reinterpret_cast<const float2*>(dn) + idx);
+    const float m = expf(unit_k * d.y);
+    sincosf((-unit_k) * d.x, &s, &c);
+    return make_float2(m * c, m * s);
+  }
+  sincosf((-unit_k) * load_dn_real(dn, dtype, idx), &s, &c);
+  float2 M = make_float2(c, s);
+  const int dist = min(min(nx - 1 - x, x), min(ny - 1 - y, y));
+  if (dist < absorb) {
+    const float a = taper[dist];
+    M.x *= a;
+    M.y *= a;
+  }
+  return M;
+}
+
+// PRE = 1: the masks come precomputed (p.mask); PRE = 0: formed on the fly from dn. The
+// two are compiled separately so the precomputed kernel carries no sincosf.
+template <int PRE>
+__device__ __forceinline__ float2 row_mask(const RowParams& p, int x, int y, int gl, size_t zoff, size_t pix) {
+  if constexpr (PRE == 1) {
+    return p.mask[zoff + pix];
+  } else {
+    return mask_value(p.dn, p.dn_dtype, gl * p.dn_bstride + zoff + pix, p.unit_k, x, y, p.nx, p.ny, p.absorb,
+                      p.taper);
+  }
+}
+
+// exp(+i k0 dz dn0), the mean-index shift of the mask (identity when dn0 = 0)
+__device__ __forceinline__ float2 row_rot(const RowParams& p, float dn0) {
+  float s, c;
+  sincosf(p.unit_k * dn0, &s, &c);
+  return make_float2(c, s);
+}
+
+template <bool ADJ, int PRE>
+__device__ __forceinline__ float2 row_point(const RowParams& p, float2 v, int x, int y, int gl, size_t plane,
+                                            size_t zoff, size_t ooff, float dn0, float2 rot, bool last,
+                                            float2* ckp) {
+  const size_t pix = (size_t)y * p.nx + x;
+  if (ADJ) {
+    if (p.z == 0) {
+      if (p.grad_u0) p.grad_u0[gl * plane + pix] = v;
+      return v;
+    }
+    if (p.do_mask) {
+      const float2 u = p.seg[gl * p.seg_bstride + (size_t)(p.z - p.seg_z0) * plane + pix];
+      p.grad_dn[(size_t)gl * p.nz * plane + zoff + pix] = p.unit_k * (v.x * u.y - v.y * u.x);
+      const float2 M = row_mask<PRE>(p, x, y, gl, zoff, pix);
+      v = cmul(v, make_float2(M.x, -M.y));
+      if (dn0 != 0.f) v = cmul(v, make_float2(rot.x, -rot.y));
+    }
+    return v;
+  }
+  if (p.do_mask) {
+    v = cmul(v, row_mask<PRE>(p, x, y, gl, zoff, pix));
+    if (dn0 != 0.f) v = cmul(v, rot);
+  }
+  if (p.out_kind == BPM_OUT_FIELD)
+    __stcs(reinterpret_cast<float2*>(p.out) + gl * p.out_bstride + ooff + pix, v);
+  else if (p.out_kind == BPM_OUT_INTENSITY)
+    __stcs(reinterpret_cast<float*>(p.out) + gl * p.out_bstride + ooff + pix, cabs2(v));
+  if (last && p.last_plane) p.last_plane[gl * plane + pix] = v;
+  if (ckp) ckp[pix] = v;
+  return v;
+}
+
+// precomputed phase masks of a shared dn volume, (nz, ny, nx) complex64
+__global__ void mask_precompute_kernel(const void* dn, int dtype, float unit_k, int nx, int ny, int absorb,
+                                       const float* taper, float2* mask) {
+  const int x = blockIdx.x * blockDim.x + threadIdx.x;
+  const int y = blockIdx.y, z = blockIdx.z;
+  if (x >= nx) return;
+  const size_t idx = ((size_t)z * ny + y) * nx + x;
+  __stcs(mask + idx, mask_value(dn, dtype, idx, unit_k, x, y, nx, ny, absorb, taper));
+}
+
+// dn0 of the current field and plane: the weighted-mode per-field value or the simple-mode
+// slice mean (0 in "ignore")
+__device__ __forceinline__ float row_dn0(const RowParams& p, int gl) {
+  if (p.mean_mode == BPM_MEAN_WEIGHTED && p.dn0_field) return p.dn0_field[gl];
+  if (p.mean_mode == BPM_MEAN_SIMPLE && p.slice_dn0) return p.slice_dn0[p.z];
+  return 0.f;
+}
+
+// the scattering sums of step z, finished by one thread of the first block of each field
+__device__ __forceinline__ void row_scatter_finish(const RowParams& p, int gl) {
+  float* prow = p.scat_p + (size_t)gl * p.nz;
+  float* grow = p.scat_g ? p.scat_g + (size_t)gl * p.nz : nullptr;
+  if (p.z == 0) {
+    prow[0] = 0.f;
+    if (grow) grow[0] = __fdiv_rn(0.f, 0.f);
+    return;
+  }
+  const float* part = p.scat_part + (size_t)gl * p.n_ctiles * 2;
+  float S = 0.f, G = 0.f;
+  for (int t = 0; t < p.n_ctiles; t++) {
+    S += part[2 * t];
+    G += part[2 * t + 1];
+  }
+  const float pv = p.prefac_f * S;
+  prow[p.z] = pv;
+  if (grow) grow[p.z] = __fdiv_rn(p.prefac_f * G, pv);
 }
 
 // Row pass over 16 rows of one field. Forward (ADJ = false): [inverse row FFT], phase mask
@@ -205,96 +355,26 @@ row_pass_kernel(RowParams p) {
 
   if (p.do_inv) tile_fft<N, R, true>(tile, tw);
 
-  // mask, outputs
-  float dn0 = 0.f;
-  if (p.mean_mode == BPM_MEAN_WEIGHTED && p.dn0_field) dn0 = p.dn0_field[gl];
-  else if (p.mean_mode == BPM_MEAN_SIMPLE && p.slice_dn0) dn0 = p.slice_dn0[p.z];
+  // pointwise work, one element per thread and iteration, consecutive x across a warp
+  const float dn0 = row_dn0(p, gl);
+  const float2 rot = row_rot(p, dn0);
   const bool last = (p.z == p.nz - 1);
   const size_t zoff = (size_t)p.z * plane;
   const size_t ooff = (size_t)(p.z - p.zout0) * plane;
   float2* ckp = nullptr;
   if (!ADJ && p.ckpt && p.z % p.ckpt_every == 0)
     ckp = p.ckpt + ((size_t)gl * p.n_ckpt + p.z / p.ckpt_every) * plane;
-  // one element per thread and iteration, consecutive x across a warp: coalesced global
-  // accesses and conflict-free tile accesses
 #pragma unroll 4
   for (int i = 0; i < PER; i++) {
     const int e = tid + i * T;
     const int r = e / N;
     const int x = e % N;
-    const int y = y0 + r;
-    const size_t pix = (size_t)y * N + x;
-    float2 v = tile[tile_idx(x, r)];
-    if (ADJ) {
-      if (p.z == 0) {
-        if (p.grad_u0) p.grad_u0[gl * plane + pix] = v;
-        continue;
-      }
-      if (p.do_mask) {
-        const float2 u = p.seg[gl * p.seg_bstride + (size_t)(p.z - p.seg_z0) * plane + pix];
-        const float dv = load_dn_real(p.dn, p.dn_dtype, gl * p.dn_bstride + zoff + pix);
-        p.grad_dn[(size_t)gl * p.nz * plane + zoff + pix] = p.unit_k * (v.x * u.y - v.y * u.x);
-        float s, c;
-        sincosf((-p.unit_k) * (dv - dn0), &s, &c);
-        v = cmul(v, make_float2(c, -s));
-        const int dist = min(min(N - 1 - x, x), min(p.ny - 1 - y, y));
-        if (dist < p.absorb) {
-          const float a = p.taper[dist];
-          v.x *= a;
-          v.y *= a;
-        }
-        tile[tile_idx(x, r)] = v;
-      }
-      continue;
-    }
-    if (p.do_mask) {
-      if (p.dn_dtype == BPM_DN_C64) {
-        const float2 d = __ldg(reinterpret_cast<const float2*>(p.dn) + gl * p.dn_bstride + zoff + pix);
-        const float m = expf(p.unit_k * d.y);
-        float s, c;
-        sincosf((-p.unit_k) * d.x, &s, &c);
-        v = cmul(v, make_float2(m * c, m * s));
-      } else {
-        const float dv = load_dn_real(p.dn, p.dn_dtype, gl * p.dn_bstride + zoff + pix);
-        float s, c;
-        sincosf((-p.unit_k) * (dv - dn0), &s, &c);
-        v = cmul(v, make_float2(c, s));
-        const int dist = min(min(N - 1 - x, x), min(p.ny - 1 - y, y));
-        if (dist < p.absorb) {
-          const float a = p.taper[dist];
-          v.x *= a;
-          v.y *= a;
-        }
-      }
-      tile[tile_idx(x, r)] = v;
-    }
-    if (p.out_kind == BPM_OUT_FIELD)
-      __stcs(reinterpret_cast<float2*>(p.out) + gl * p.out_bstride + ooff + pix, v);
-    else if (p.out_kind == BPM_OUT_INTENSITY)
-      __stcs(reinterpret_cast<float*>(p.out) + gl * p.out_bstride + ooff + pix, cabs2(v));
-    if (last && p.last_plane) p.last_plane[gl * plane + pix] = v;
-    if (ckp) ckp[pix] = v;
+    const float2 v = p.mask
+        ? row_point<ADJ, 1>(p, tile[tile_idx(x, r)], x, y0 + r, gl, plane, zoff, ooff, dn0, rot, last, ckp)
+        : row_point<ADJ, 0>(p, tile[tile_idx(x, r)], x, y0 + r, gl, plane, zoff, ooff, dn0, rot, last, ckp);
+    if (p.do_mask) tile[tile_idx(x, r)] = v;
   }
-
-  // scattering sums of this step: finished by one thread of the first block per field
-  if (!ADJ && p.scat_p && blockIdx.x == 0 && tid == 0) {
-    float* prow = p.scat_p + (size_t)gl * p.nz;
-    float* grow = p.scat_g ? p.scat_g + (size_t)gl * p.nz : nullptr;
-    if (p.z == 0) {
-      prow[0] = 0.f;
-      if (grow) grow[0] = __fdiv_rn(0.f, 0.f);
-    } else {
-      const float* part = p.scat_part + (size_t)gl * p.n_ctiles * 2;
-      float S = 0.f, G = 0.f;
-      for (int t = 0; t < p.n_ctiles; t++) {
-        S += part[2 * t];
-        G += part[2 * t + 1];
-      }
-      float pv = p.prefac_f * S;
-      prow[p.z] = pv;
-      if (grow) grow[p.z] = __fdiv_rn(p.prefac_f * G, pv);
-    }
-  }
+  if (!ADJ && p.scat_p && blockIdx.x == 0 && tid == 0) row_scatter_finish(p, gl);
 
   if (!p.do_fwd) return;
   __syncthreads();
@@ -330,6 +410,7 @@ struct ColParams {
   int spi;                   // scattering_plane_ind
   int conj_h;                // adjoint: multiply by conj(H)
   const float2* tw;
+  const float2* wtw;         // stage-ordered twiddles of the warp FFT
 };
 
 template <int T>
@@ -357,9 +438,8 @@ __device__ __forceinline__ void block_sum2(float& a, float& b, float* red) {
   }
 }
 
-template <int N>
+template <int N, int T = TileCfg<N>::THREADS>
 __device__ __forceinline__ void col_load(float2* tile, const float2* Wp, int nx, int x0) {
-  constexpr int T = TileCfg<N>::THREADS;
   constexpr int PER = 16 * N / T;
   float2 buf[PER];
 #pragma unroll
@@ -374,9 +454,8 @@ __device__ __forceinline__ void col_load(float2* tile, const float2* Wp, int nx,
   }
 }
 
-template <int N>
+template <int N, int T = TileCfg<N>::THREADS>
 __device__ __forceinline__ void col_store(const float2* tile, float2* Wp, int nx, int x0) {
-  constexpr int T = TileCfg<N>::THREADS;
   constexpr int PER = 16 * N / T;
 #pragma unroll
   for (int i = 0; i < PER; i++) {
@@ -385,59 +464,73 @@ __device__ __forceinline__ void col_store(const float2* tile, float2* Wp, int nx
   }
 }
 
+// plain_wave_dct[z+1] = nx*ny*exp(-i k0 n0 (spi + z+1) dz) of bpm_3d.py:253, FP64 then complex64
+__device__ __forceinline__ float2 plain_wave(const ColParams& p) {
+  double ph = -p.plain_phase * (double)(p.spi + p.z + 1);
+  double s, c;
+  sincos(ph, &s, &c);
+  double m = (double)p.nx * (double)p.ny;
+  return make_float2((float)(m * c), (float)(m * s));
+}
+
+// k-space element (kx index x, ky index y) times the propagator, with the scattering partial
+// sums of bpm_3d.py:335-341 and the 1/(nx*ny) inverse-FFT normalisation folded in
+__device__ __forceinline__ float2 prop_point(const ColParams& p, float2 v, int x, int y, float nk, float2 plain,
+                                             float& S, float& G) {
+  float2 h;
+  if (p.prop_mode == 0) {
+    h = __ldg(p.H + (size_t)y * p.nx + x);
+    if (p.conj_h) h.y = -h.y;
+  } else {
+    const float tmp = __fsub_rn(__fsub_rn(nk, __ldg(p.kx2 + x)), __ldg(p.ky2 + y));
+    if (tmp >= 0.f) {
+      const float ph = __fmul_rn(-p.dzf, __fsqrt_rn(tmp));
+      sincosf(ph, &h.y, &h.x);
+    } else {
+      h = make_float2(0.f, 0.f);
+    }
+  }
+  v = cmul(v, h);
+  if (p.scat) {
+    float2 d = v;
+    if (x == 0 && y == 0) d = csub(d, plain);
+    const float a2 = cabs2(d);
+    const size_t k = (size_t)y * p.nx + x;
+    S += __ldg(p.sw + k) * a2;
+    G += __ldg(p.gw + k) * a2;
+  }
+  return cscale(v, p.scale);
+}
+
+// n*n*k0*k0 in the FP32 order of the kernels (bpm_3d_kernels.cl:425), no contraction
+__device__ __forceinline__ float prop_nk(const ColParams& p, float n_eff) {
+  return __fmul_rn(__fmul_rn(__fmul_rn(n_eff, n_eff), p.k0f), p.k0f);
+}
+
+template <int T>
+__device__ __forceinline__ void scat_partials_store(const ColParams& p, float S, float G, int gl, float* red) {
+  block_sum2<T>(S, G, red);
+  if (threadIdx.x == 0) {
+    float* o = p.scat_part + ((size_t)gl * (p.nx / 16) + blockIdx.x) * 2;
+    o[0] = S;
+    o[1] = G;
+  }
+}
+
 // multiply the k-space column tile by the propagator (+ scattering partial sums)
 template <int N>
 __device__ __forceinline__ void col_propagate(float2* tile, const ColParams& p, float n_eff, int x0,
                                               int gl, float* red) {
   constexpr int T = TileCfg<N>::THREADS;
-  const float nk = __fmul_rn(__fmul_rn(__fmul_rn(n_eff, n_eff), p.k0f), p.k0f);
+  const float nk = prop_nk(p, n_eff);
   float S = 0.f, G = 0.f;
-  float2 plain = make_float2(0.f, 0.f);
-  if (p.scat && x0 == 0) {
-    // plain_wave_dct[z+1] = nx*ny*exp(-i k0 n0 (spi + z+1) dz), FP64 then complex64
-    double ph = -p.plain_phase * (double)(p.spi + p.z + 1);
-    double s, c;
-    sincos(ph, &s, &c);
-    double m = (double)p.nx * (double)p.ny;
-    plain = make_float2((float)(m * c), (float)(m * s));
-  }
+  const float2 plain = (p.scat && x0 == 0) ? plain_wave(p) : make_float2(0.f, 0.f);
   for (int e = threadIdx.x; e < 16 * N; e += T) {
     const int y = e >> 4;
     const int c = e & 15;
-    const int x = x0 + c;
-    float2 v = tile[tile_idx(y, c)];
-    float2 h;
-    if (p.prop_mode == 0) {
-      h = __ldg(p.H + (size_t)y * p.nx + x);
-      if (p.conj_h) h.y = -h.y;
-    } else {
-      const float tmp = __fsub_rn(__fsub_rn(nk, __ldg(p.kx2 + x)), __ldg(p.ky2 + y));
-      if (tmp >= 0.f) {
-        const float ph = __fmul_rn(-p.dzf, __fsqrt_rn(tmp));
-        sincosf(ph, &h.y, &h.x);
-      } else {
-        h = make_float2(0.f, 0.f);
-      }
-    }
-    v = cmul(v, h);
-    if (p.scat) {
-      float2 d = v;
-      if (x == 0 && y == 0) d = csub(d, plain);
-      const float a2 = cabs2(d);
-      const size_t k = (size_t)y * p.nx + x;
-      S += __ldg(p.sw + k) * a2;
-      G += __ldg(p.gw + k) * a2;
-    }
-    tile[tile_idx(y, c)] = cscale(v, p.scale);
+    tile[tile_idx(y, c)] = prop_point(p, tile[tile_idx(y, c)], x0 + c, y, nk, plain, S, G);
   }
-  if (p.scat) {
-    block_sum2<T>(S, G, red);
-    if (threadIdx.x == 0) {
-      float* o = p.scat_part + ((size_t)gl * (p.nx / 16) + blockIdx.x) * 2;
-      o[0] = S;
-      o[1] = G;
-    }
-  }
+  if (p.scat) scat_partials_store<T>(p, S, G, gl, red);
   __syncthreads();
 }
 
@@ -533,6 +626,145 @@ col_inv_kernel(ColParams p) {
 }
 
 // ---------------------------------------------------------------------------------------
+// warp-per-sequence kernels (128 <= N <= 512): each warp transforms one row or one column
+// entirely in registers, exchanging only through its own shared-memory buffer
+// ---------------------------------------------------------------------------------------
+constexpr int kRowWarps = 8;   // rows per block
+constexpr int kColWarps = 16;  // columns per block (16 columns = one 128-byte segment per row)
+
+template <int N>
+struct WarpCfg {
+  static constexpr size_t ROW_SMEM = ((size_t)N + (size_t)kRowWarps * WarpFft<N>::BUF) * sizeof(float2);
+  static constexpr size_t COL_SMEM = ((size_t)N + (size_t)kColWarps * WarpFft<N>::BUF) * sizeof(float2);
+};
+
+// Row pass, one warp per row: coalesced row load straight into registers, [inverse row
+// FFT], pointwise work, [forward row FFT], coalesced store. No block-level barrier after
+// the twiddle table is loaded.
+template <int N, bool ADJ, int PRE>
+__global__ void __launch_bounds__(kRowWarps * 32, PRE ? 4 : 3)
+row_warp_kernel(RowParams p) {
+  constexpr int E = N / 32;
+  constexpr int T = kRowWarps * 32;
+  extern __shared__ float2 smem[];
+  float2* tw = smem;
+  const int warp = threadIdx.x >> 5, t = threadIdx.x & 31;
+  float2* buf = smem + N + warp * WarpFft<N>::BUF;
+  const int gl = blockIdx.y;
+  const int y = blockIdx.x * kRowWarps + warp;
+  const size_t plane = (size_t)N * p.ny;
+  if (p.do_inv || p.do_fwd) {
+    for (int k = threadIdx.x; k < WarpFft<N>::TW; k += T) tw[k] = p.wtw[k];
+    __syncthreads();
+  }
+  float2 v[E];
+  const float2* src = p.src + gl * p.src_bstride + (size_t)y * N;
+#pragma unroll
+  for (int m = 0; m < E; m++) v[m] = src[t + 32 * m];
+  if (p.do_inv) warp_fft<N, true>(v, buf, tw, t);
+
+  const float dn0 = row_dn0(p, gl);
+  const float2 rot = row_rot(p, dn0);
+  const bool last = (p.z == p.nz - 1);
+  const size_t zoff = (size_t)p.z * plane;
+  const size_t ooff = (size_t)(p.z - p.zout0) * plane;
+  float2* ckp = nullptr;
+  if (!ADJ && p.ckpt && p.z % p.ckpt_every == 0)
+    ckp = p.ckpt + ((size_t)gl * p.n_ckpt + p.z / p.ckpt_every) * plane;
+#pragma unroll
+  for (int m = 0; m < E; m++)
+    v[m] = row_point<ADJ, PRE>(p, v[m], t + 32 * m, y, gl, plane, zoff, ooff, dn0, rot, last, ckp);
+  if (!ADJ && p.scat_p && blockIdx.x == 0 && threadIdx.x == 0) row_scatter_finish(p, gl);
+
+  if (!p.do_fwd) return;
+  warp_fft<N, false>(v, buf, tw, t);
+  float2* dst = p.W + gl * plane + (size_t)y * N;
+#pragma unroll
+  for (int m = 0; m < E; m++) dst[t + 32 * m] = v[m];
+}
+
+// Column pass, one warp per column of a 16-column tile: coalesced tile load into shared
+// memory, then every warp takes its column into registers. WHICH: 0 = forward FFT,
+// propagator, inverse FFT; 1 = forward FFT + weighted-mode partial sums (k-space stored
+// back); 2 = n from the partial sums, propagator, inverse FFT.
+template <int N, int WHICH>
+__global__ void __launch_bounds__(kColWarps * 32, 2)
+col_warp_kernel(ColParams p) {
+  constexpr int E = N / 32;
+  constexpr int T = kColWarps * 32;
+  extern __shared__ float2 smem[];
+  float2* tw = smem;
+  float2* tile = smem + N;  // the 16 x N tile, then the warps' exchange buffers
+  __shared__ float red[64];
+  __shared__ float s_n;
+  const int warp = threadIdx.x >> 5, t = threadIdx.x & 31;
+  const int gl = blockIdx.y;
+  const int x0 = blockIdx.x * kColWarps;
+  const int x = x0 + warp;
+  float2* Wp = p.W + (size_t)gl * p.nx * N;
+  for (int k = threadIdx.x; k < WarpFft<N>::TW; k += T) tw[k] = p.wtw[k];
+  if (WHICH == 2 && threadIdx.x == 0) {
+    // every block of the field sums the partials in the same order: identical results
+    const float* part = p.red_part + (size_t)gl * (p.nx / 16) * 2;
+    float dn_sum = 0.f, u_sum = 0.f;
+    for (int i = 0; i < p.nx / 16; i++) {
+      dn_sum += part[2 * i];
+      u_sum += part[2 * i + 1];
+    }
+    const float dn0 = dn_sum / u_sum;  // mult_dn_mean_buff, bpm_3d_kernels.cl:117
+    s_n = p.n00f + dn0;                // mult_propagator_buff, bpm_3d_kernels.cl:482
+    if (blockIdx.x == 0) p.dn0_field[gl] = dn0;
+  }
+  col_load<N, T>(tile, Wp, p.nx, x0);
+  __syncthreads();
+  float2 v[E];
+#pragma unroll
+  for (int m = 0; m < E; m++) v[m] = tile[tile_idx(t + 32 * m, warp)];
+  __syncthreads();
+  float2* buf = tile + warp * WarpFft<N>::BUF;
+  if (WHICH != 2) warp_fft<N, false>(v, buf, tw, t);
+  if (WHICH != 1) {
+    const float n_eff = WHICH == 2 ? s_n : (p.prop_mode == 1 ? p.slice_n[p.z + 1] : p.n00f);
+    const float nk = prop_nk(p, n_eff);
+    const float2 plain = (p.scat && x == 0) ? plain_wave(p) : make_float2(0.f, 0.f);
+    float S = 0.f, G = 0.f;
+#pragma unroll
+    for (int m = 0; m < E; m++) v[m] = prop_point(p, v[m], x, t + 32 * m, nk, plain, S, G);
+    if (p.scat) scat_partials_store<T>(p, S, G, gl, red);
+    warp_fft<N, true>(v, buf, tw, t);
+  }
+  __syncthreads();
+#pragma unroll
+  for (int m = 0; m < E; m++) tile[tile_idx(t + 32 * m, warp)] = v[m];
+  __syncthreads();
+  if (WHICH == 1) {
+    // weighted mode: sum |u_hat| and |u_hat|*dn over the tile while storing it, with the
+    // coalesced tile mapping (dn slice 0 read 16 columns at a time)
+    constexpr int PER = 16 * N / T;
+    float sdn = 0.f, su = 0.f;
+#pragma unroll 4
+    for (int i = 0; i < PER; i++) {
+      const int e = threadIdx.x + i * T;
+      const int n = e >> 4, c = e & 15;
+      const float2 u = tile[tile_idx(n, c)];
+      const size_t k = (size_t)n * p.nx + x0 + c;
+      Wp[k] = u;
+      const float a = __fsqrt_rn(cabs2(u));
+      su += a;
+      if (p.dn) sdn += a * load_dn_real(p.dn, p.dn_dtype, gl * p.dn_bstride + k);
+    }
+    block_sum2<T>(sdn, su, red);
+    if (threadIdx.x == 0) {
+      float* o = p.red_part + ((size_t)gl * (p.nx / 16) + blockIdx.x) * 2;
+      o[0] = sdn;
+      o[1] = su;
+    }
+  } else {
+    col_store<N, T>(tile, Wp, p.nx, x0);
+  }
+}
+
+// ---------------------------------------------------------------------------------------
 // dispatch over power-of-two sizes
 // ---------------------------------------------------------------------------------------
 template <template <int> class K>
@@ -540,22 +772,42 @@ struct SizeDispatch;
 
 template <int N>
 struct RowK {
+  static constexpr bool WARP = N >= 128 && N <= 512;
   static void prepare() {
     static bool attr = false;
     if (!attr) {
-      cudaFuncSetAttribute(row_pass_kernel<N, false>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                           (int)TileCfg<N>::SMEM);
-      cudaFuncSetAttribute(row_pass_kernel<N, true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                           (int)TileCfg<N>::SMEM);
+      if constexpr (WARP) {
+        cudaFuncSetAttribute(row_warp_kernel<N, false, 0>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                             (int)WarpCfg<N>::ROW_SMEM);
+        cudaFuncSetAttribute(row_warp_kernel<N, true, 0>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                             (int)WarpCfg<N>::ROW_SMEM);
+        cudaFuncSetAttribute(row_warp_kernel<N, false, 1>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                             (int)WarpCfg<N>::ROW_SMEM);
+        cudaFuncSetAttribute(row_warp_kernel<N, true, 1>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                             (int)WarpCfg<N>::ROW_SMEM);
+      } else {
+        cudaFuncSetAttribute(row_pass_kernel<N, false>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                             (int)TileCfg<N>::SMEM);
+        cudaFuncSetAttribute(row_pass_kernel<N, true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                             (int)TileCfg<N>::SMEM);
+      }
       attr = true;
     }
   }
+  // g.x counts 16-row tiles; the warp kernel covers kRowWarps rows per block
   static int launch(dim3 g, cudaStream_t s, const RowParams& p, bool adj) {
     prepare();
-    if (adj)
-      row_pass_kernel<N, true><<<g, TileCfg<N>::THREADS, TileCfg<N>::SMEM, s>>>(p);
-    else
-      row_pass_kernel<N, false><<<g, TileCfg<N>::THREADS, TileCfg<N>::SMEM, s>>>(p);
+    if constexpr (WARP) {
+      const dim3 gw(g.x * 16 / kRowWarps, g.y);
+      auto fn = adj ? (p.mask ? row_warp_kernel<N, true, 1> : row_warp_kernel<N, true, 0>)
+                    : (p.mask ? row_warp_kernel<N, false, 1> : row_warp_kernel<N, false, 0>);
+      fn<<<gw, kRowWarps * 32, WarpCfg<N>::ROW_SMEM, s>>>(p);
+    } else {
+      if (adj)
+        row_pass_kernel<N, true><<<g, TileCfg<N>::THREADS, TileCfg<N>::SMEM, s>>>(p);
+      else
+        row_pass_kernel<N, false><<<g, TileCfg<N>::THREADS, TileCfg<N>::SMEM, s>>>(p);
+    }
     BPM_LAUNCH_CHECK("row_pass_kernel");
     return BPM_OK;
   }
@@ -563,19 +815,23 @@ struct RowK {
 
 template <int N, int WHICH>
 struct ColK {
+  static constexpr bool WARP = N >= 128 && N <= 512;
   static void (*fn())(ColParams) {
+    if constexpr (WARP) return col_warp_kernel<N, WHICH>;
     return WHICH == 0 ? col_pass_kernel<N> : (WHICH == 1 ? col_fwd_reduce_kernel<N> : col_inv_kernel<N>);
   }
+  static constexpr int threads() { return WARP ? kColWarps * 32 : TileCfg<N>::THREADS; }
+  static constexpr size_t smem() { return WARP ? WarpCfg<N>::COL_SMEM : TileCfg<N>::SMEM; }
   static void prepare() {
     static bool attr = false;
     if (!attr) {
-      cudaFuncSetAttribute(fn(), cudaFuncAttributeMaxDynamicSharedMemorySize, (int)TileCfg<N>::SMEM);
+      cudaFuncSetAttribute(fn(), cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem());
       attr = true;
     }
   }
   static int launch(dim3 g, cudaStream_t s, const ColParams& p) {
     prepare();
-    fn()<<<g, TileCfg<N>::THREADS, TileCfg<N>::SMEM, s>>>(p);
+    fn()<<<g, threads(), smem(), s>>>(p);
     BPM_LAUNCH_CHECK("col_pass_kernel");
     return BPM_OK;
   }
@@ -635,12 +891,10 @@ void prepare_kernels(int nx, int ny) {
 }
 
 int default_group(const bpm_plan* pl, int batch) {
-  const int nx = pl->d.nx, ny = pl->d.ny;
-  const size_t plane_bytes = (size_t)nx * ny * 8;
-  // keep the group's planes well inside L2 (129 MB) and give each pass >= ~4 waves of blocks
-  int g_l2 = (int)std::max<size_t>(1, (48u << 20) / plane_bytes);
-  int g_fill = std::max(1, (152 * 4) / std::max(1, nx / 16));
-  int g = std::min(g_l2, g_fill);
+  const size_t plane_bytes = (size_t)pl->d.nx * pl->d.ny * 8;
+  // up to kMaxConcurrentGroups groups march at once: keep each group's planes near 16 MB so
+  // all of them stay resident in the 129 MB L2 next to the dn slices and output streams
+  const int g = (int)std::max<size_t>(1, (16u << 20) / plane_bytes);
   return std::max(1, std::min(g, batch));
 }
 
@@ -683,6 +937,10 @@ int check_request(const bpm_plan* pl, const bpm_request* r) {
   if (r->scatter_g && !r->scatter_p) { set_error("scatter_g needs scatter_p"); return BPM_ERR_ARG; }
   if (r->group < 0) { set_error("group must be >= 0"); return BPM_ERR_ARG; }
   if (r->ckpt && r->ckpt_every < 1) { set_error("ckpt_every must be >= 1 with ckpt"); return BPM_ERR_ARG; }
+  if (r->mask && (r->dn_dtype == BPM_DN_NONE || r->dn_batch_stride != 0 || ((uintptr_t)r->mask & 7))) {
+    set_error("mask needs one shared dn volume and 8-byte alignment");
+    return BPM_ERR_ARG;
+  }
   if (r->ckpt && ((uintptr_t)r->ckpt & 15)) { set_error("ckpt must be 16-byte aligned"); return BPM_ERR_ARG; }
   // 16-byte alignment of the vectorised accesses
   auto mis = [](const void* q) { return ((uintptr_t)q & 15) != 0; };
@@ -759,9 +1017,11 @@ MarchCtx make_ctx(const bpm_plan* pl, const bpm_request* r, void* ws, int b0, in
   rp.scat_g = r->scatter_g ? r->scatter_g + (size_t)b0 * nz : nullptr;
   rp.prefac_f = (float)(1. / nx / ny * d.dx * d.dy);
   rp.tw = pl->tw_x;
+  rp.wtw = pl->wtw_x;
   rp.src = W;
   rp.src_bstride = plane;
   rp.zout0 = 0;
+  rp.mask = static_cast<const float2*>(r->mask);
   if (r->ckpt) {
     rp.ckpt_every = r->ckpt_every;
     rp.n_ckpt = (nz - 1) / r->ckpt_every + 1;
@@ -793,6 +1053,7 @@ MarchCtx make_ctx(const bpm_plan* pl, const bpm_request* r, void* ws, int b0, in
   cp.plain_phase = pl->k0 * d.n0 * d.dz;
   cp.spi = r->scattering_plane_ind;
   cp.tw = pl->tw_y;
+  cp.wtw = pl->wtw_y;
 
   c.grow = dim3(ny / 16, Gc);
   c.gcol = dim3(nx / 16, Gc);
@@ -833,19 +1094,45 @@ int launch_row_z(const bpm_plan* pl, const bpm_request* r, MarchCtx& c, int z, c
   return launch_row(pl->d.nx, c.grow, s, rp);
 }
 
+// The march of one group of fields [b0, b0+Gc) on stream s with workspace slot ws.
+int enqueue_group(bpm_plan* pl, const bpm_request* r, void* ws, int b0, int Gc, cudaStream_t s) {
+  int rc;
+  MarchCtx c = make_ctx(pl, r, ws, b0, Gc);
+  if ((rc = launch_first_row(pl, r, c, b0, s))) return rc;
+  for (int i = 0; i + 1 < pl->d.nz; i++) {
+    if ((rc = launch_cols(pl, c, i, 0, s))) return rc;
+    if ((rc = launch_row_z(pl, r, c, i + 1, s))) return rc;
+  }
+  return BPM_OK;
+}
+
+// All groups of a request. With room for several workspace slots, groups march
+// concurrently on the plan's auxiliary streams (forked from and joined back to s through
+// events, which also captures into a CUDA graph as parallel branches), so one group's
+// kernels fill the device while another's run their tail waves; otherwise they march one
+// after the other on s.
 int enqueue_march(bpm_plan* pl, const bpm_request* r, void* ws, size_t ws_bytes, cudaStream_t s) {
   int rc = check_workspace(pl, r, ws, ws_bytes);
   if (rc) return rc;
   const int G = group_size(pl, r);
-  const int nz = pl->d.nz;
-  for (int b0 = 0; b0 < r->batch; b0 += G) {
-    const int Gc = std::min(G, r->batch - b0);
-    MarchCtx c = make_ctx(pl, r, ws, b0, Gc);
-    if ((rc = launch_first_row(pl, r, c, b0, s))) return rc;
-    for (int i = 0; i + 1 < nz; i++) {
-      if ((rc = launch_cols(pl, c, i, 0, s))) return rc;
-      if ((rc = launch_row_z(pl, r, c, i + 1, s))) return rc;
-    }
+  const int ngroups = (r->batch + G - 1) / G;
+  const size_t slot = ws_layout(pl, G).total;
+  const int conc = (int)std::min<size_t>({(size_t)ngroups, ws_bytes / slot, (size_t)kMaxConcurrentGroups});
+  if (conc <= 1) {
+    for (int b0 = 0; b0 < r->batch; b0 += G)
+      if ((rc = enqueue_group(pl, r, ws, b0, std::min(G, r->batch - b0), s))) return rc;
+    return BPM_OK;
+  }
+  BPM_CUDA_TRY(cudaEventRecord(pl->ev_fork, s));
+  for (int i = 0; i < conc; i++) BPM_CUDA_TRY(cudaStreamWaitEvent(pl->aux[i], pl->ev_fork, 0));
+  for (int g = 0; g < ngroups; g++) {
+    const int b0 = g * G;
+    char* wsg = static_cast<char*>(ws) + (size_t)(g % conc) * slot;
+    if ((rc = enqueue_group(pl, r, wsg, b0, std::min(G, r->batch - b0), pl->aux[g % conc]))) return rc;
+  }
+  for (int i = 0; i < conc; i++) {
+    BPM_CUDA_TRY(cudaEventRecord(pl->ev_join[i], pl->aux[i]));
+    BPM_CUDA_TRY(cudaStreamWaitEvent(s, pl->ev_join[i], 0));
   }
   return BPM_OK;
 }
@@ -1081,6 +1368,15 @@ extern "C" int bpm_plan_create(const bpm_grid_desc* d, bpm_plan** out) {
   if ((e = cudaMemcpy(pl->ky2, ky2.data(), ny * sizeof(float), cudaMemcpyHostToDevice))) return fail(e, "cudaMemcpy");
   if ((e = cudaMemcpy(pl->taper, taper.data(), taper.size() * sizeof(float), cudaMemcpyHostToDevice)))
     return fail(e, "cudaMemcpy");
+  for (int axis = 0; axis < 2; axis++) {
+    const int n = axis == 0 ? nx : ny;
+    if (n < 128 || n > 512) continue;
+    std::vector<float2> w = warp_twiddles(n);
+    float2** dst = axis == 0 ? &pl->wtw_x : &pl->wtw_y;
+    if ((e = cudaMalloc(dst, w.size() * sizeof(float2)))) return fail(e, "cudaMalloc");
+    if ((e = cudaMemcpy(*dst, w.data(), w.size() * sizeof(float2), cudaMemcpyHostToDevice)))
+      return fail(e, "cudaMemcpy");
+  }
   dim3 tb(128), tg((nx + 127) / 128, ny);
   build_tables_kernel<<<tg, tb>>>(nx, ny, d->dx, d->dy, d->dz, d->n0, pl->k0, pl->n0f, pl->k0f, d->prop_kind,
                                   d->use_fresnel_approx, pl->kx2, pl->ky2, pl->H, pl->sw, pl->gw);
@@ -1088,6 +1384,11 @@ extern "C" int bpm_plan_create(const bpm_grid_desc* d, bpm_plan** out) {
   count_launch();
   if ((e = cudaDeviceSynchronize())) return fail(e, "build_tables_kernel");
   prepare_kernels(nx, ny);
+  for (int i = 0; i < kMaxConcurrentGroups; i++) {
+    if ((e = cudaStreamCreateWithFlags(&pl->aux[i], cudaStreamNonBlocking))) return fail(e, "cudaStreamCreate");
+    if ((e = cudaEventCreateWithFlags(&pl->ev_join[i], cudaEventDisableTiming))) return fail(e, "cudaEventCreate");
+  }
+  if ((e = cudaEventCreateWithFlags(&pl->ev_fork, cudaEventDisableTiming))) return fail(e, "cudaEventCreate");
   *out = pl;
   return BPM_OK;
 }
@@ -1096,6 +1397,13 @@ extern "C" int bpm_plan_destroy(bpm_plan* pl) {
   if (!pl) return BPM_OK;
   cudaFree(pl->tw_x);
   cudaFree(pl->tw_y);
+  cudaFree(pl->wtw_x);
+  cudaFree(pl->wtw_y);
+  for (int i = 0; i < kMaxConcurrentGroups; i++) {
+    if (pl->aux[i]) cudaStreamDestroy(pl->aux[i]);
+    if (pl->ev_join[i]) cudaEventDestroy(pl->ev_join[i]);
+  }
+  if (pl->ev_fork) cudaEventDestroy(pl->ev_fork);
   cudaFree(pl->kx2);
   cudaFree(pl->ky2);
   cudaFree(pl->taper);
@@ -1106,10 +1414,16 @@ extern "C" int bpm_plan_destroy(bpm_plan* pl) {
   return BPM_OK;
 }
 
+extern "C" int bpm_group_size(const bpm_plan* pl, int batch, int group) {
+  if (!pl || batch < 1 || group < 0) return 0;
+  return group > 0 ? std::min(group, batch) : default_group(pl, batch);
+}
+
 extern "C" size_t bpm_workspace_bytes(const bpm_plan* pl, int batch, int group) {
   if (!pl || batch < 1) return 0;
   const int G = group > 0 ? std::min(group, batch) : default_group(pl, batch);
-  return ws_layout(pl, G).total;
+  const int ngroups = (batch + G - 1) / G;
+  return (size_t)std::min(ngroups, kMaxConcurrentGroups) * ws_layout(pl, G).total;
 }
 
 extern "C" int bpm_propagate(bpm_plan* pl, const bpm_request* r, void* ws, size_t ws_bytes, void* stream) {
@@ -1164,6 +1478,22 @@ extern "C" int bpm_backward(bpm_plan* pl, const bpm_request* r, const void* grad
   if ((rc = check_backward(pl, r, grad_last, grad_dn))) return rc;
   if (grad_u0 && ((uintptr_t)grad_u0 & 15)) { set_error("grad_u0 must be 16-byte aligned"); return BPM_ERR_ARG; }
   return enqueue_backward(pl, r, grad_last, grad_dn, grad_u0, ws, ws_bytes, static_cast<cudaStream_t>(stream));
+}
+
+extern "C" int bpm_mask_precompute(bpm_plan* pl, const void* dn, int dn_dtype, void* mask, void* stream) {
+  clear_error();
+  if (!pl || !dn || !mask) { set_error("plan, dn and mask must be given"); return BPM_ERR_ARG; }
+  if (dn_dtype != BPM_DN_F32 && dn_dtype != BPM_DN_F16 && dn_dtype != BPM_DN_C64) {
+    set_error("bad dn_dtype");
+    return BPM_ERR_ARG;
+  }
+  if (((uintptr_t)mask & 7) || ((uintptr_t)dn & 7)) { set_error("dn and mask must be 8-byte aligned"); return BPM_ERR_ARG; }
+  const bpm_grid_desc& d = pl->d;
+  dim3 g((d.nx + 127) / 128, d.ny, d.nz);
+  mask_precompute_kernel<<<g, 128, 0, static_cast<cudaStream_t>(stream)>>>(
+      dn, dn_dtype, pl->unit_k, d.nx, d.ny, d.absorbing_width, pl->taper, static_cast<float2*>(mask));
+  BPM_LAUNCH_CHECK("mask_precompute_kernel");
+  return BPM_OK;
 }
 
 extern "C" int bpm_exec_create(bpm_plan* pl, const bpm_request* r, void* ws, size_t ws_bytes, bpm_exec** out) {

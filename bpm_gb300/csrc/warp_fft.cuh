@@ -1,0 +1,121 @@
+// Warp-level FFT: one warp transforms one complex sequence of length N (64 <= N <= 512)
+// held in registers, 16 = N/32 values per lane for N = 512.
+//
+// Distribution. On entry and on exit lane t holds elements t + 32*m, m = 0 .. N/32-1, in
+// v[m]: natural order, consecutive elements on consecutive lanes. So a row of an image is
+// loaded and stored with fully coalesced accesses, and the output of an inverse transform
+// is already laid out as the input of the next forward transform (no exchange between
+// them).
+//
+// Algorithm. Stockham autosort (the same radix recurrence as fft_tile.cuh): stages of
+// radix RS <= N/32 with stride NS = 1, RS0, RS0*RS1, ...; butterfly j = 32*q + t of a
+// stage reads x[j + r*N/RS], applies W_N^{(j mod NS)*r*N/(NS*RS)}, runs a radix-RS DFT in
+// registers and writes (j/NS)*NS*RS + (j mod NS) + r*NS. The first stage reads its inputs
+// from the lane's own registers and the last stage writes its outputs back to them (both
+// fall on the lane's t + 32*m elements); the stages in between exchange through a
+// private per-warp shared-memory buffer synchronised with __syncwarp, with one pad
+// element every 16 (index p + p/16), which keeps every exchange at the minimum number of
+// shared-memory wavefronts for N = 256 and 512.
+#pragma once
+
+#include "fft_tile.cuh"
+
+namespace bpmgb {
+
+__device__ __forceinline__ int wpad(int p) { return p + (p >> 4); }
+
+// Twiddles are stored per stage, entry (r-1)*NS + jm of stage (RS, NS) holding
+// W_N^{jm*r*N/(NS*RS)} for r = 1..RS-1, jm = 0..NS-1, stages in march order, stages with
+// NS = 1 (no twiddles) skipped. A stage's lanes then read consecutive entries.
+__host__ __device__ constexpr int wtw_offset(int N, int ns_target) {
+  int off = 0, ns = 1;
+  const int E = N / 32;
+  while (ns < ns_target) {
+    const int rs = (N / ns) < E ? (N / ns) : E;
+    if (ns > 1) off += (rs - 1) * ns;
+    ns *= rs;
+  }
+  return off;
+}
+__host__ __device__ constexpr int wtw_size(int N) { return wtw_offset(N, N); }
+
+template <int N>
+struct WarpFft {
+  static constexpr int E = N / 32;          // values per lane
+  static constexpr int BUF = N + N / 16;    // padded per-warp exchange buffer (float2)
+  static constexpr int TW = wtw_size(N);    // stage-ordered twiddle entries
+};
+
+template <int N, int RS, int NS, bool INV, bool FIRST, bool LAST>
+__device__ __forceinline__ void warp_stage(float2 (&v)[N / 32], float2* buf, const float2* __restrict__ tw,
+                                           int t) {
+  constexpr int E = N / 32;
+  constexpr int Q = E / RS;                 // butterflies per lane
+  constexpr int STRIDE_IN = N / RS;
+  constexpr int TWOFF = wtw_offset(N, NS);  // this stage's twiddle block
+  float2 a[E];
+#pragma unroll
+  for (int q = 0; q < Q; q++) {
+#pragma unroll
+    for (int r = 0; r < RS; r++) {
+      if constexpr (FIRST)
+        a[q * RS + r] = v[q + r * Q];
+      else
+        a[q * RS + r] = buf[wpad(q * 32 + t + r * STRIDE_IN)];
+    }
+  }
+#pragma unroll
+  for (int q = 0; q < Q; q++) {
+    const int j = q * 32 + t;
+    if constexpr (NS > 1) {
+      const int jm = j & (NS - 1);
+#pragma unroll
+      for (int r = 1; r < RS; r++) {
+        float2 w = tw[TWOFF + (r - 1) * NS + jm];
+        if (INV) w.y = -w.y;
+        a[q * RS + r] = cmul(a[q * RS + r], w);
+      }
+    }
+    Dft<RS, INV>::run(&a[q * RS]);
+  }
+  if constexpr (LAST) {
+#pragma unroll
+    for (int q = 0; q < Q; q++)
+#pragma unroll
+      for (int r = 0; r < RS; r++) v[q + r * (NS / 32)] = a[q * RS + r];
+  } else {
+    __syncwarp();  // every lane is done reading the buffer (previous stage or transform)
+#pragma unroll
+    for (int q = 0; q < Q; q++) {
+      const int j = q * 32 + t;
+      const int jm = j & (NS - 1);
+      const int base = (j / NS) * NS * RS + jm;
+#pragma unroll
+      for (int r = 0; r < RS; r++) buf[wpad(base + r * NS)] = a[q * RS + r];
+    }
+    __syncwarp();
+  }
+}
+
+template <int N, int NS, bool INV>
+__device__ __forceinline__ void warp_fft_from(float2 (&v)[N / 32], float2* buf, const float2* __restrict__ tw,
+                                              int t) {
+  if constexpr (NS < N) {
+    constexpr int E = N / 32;
+    constexpr int REM = N / NS;
+    constexpr int RS = REM < E ? REM : E;
+    warp_stage<N, RS, NS, INV, NS == 1, NS * RS == N>(v, buf, tw, t);
+    warp_fft_from<N, NS * RS, INV>(v, buf, tw, t);
+  }
+}
+
+// In-place length-N FFT of the warp's sequence v (forward: exp(-i..), inverse: exp(+i..),
+// both unnormalised). buf: WarpFft<N>::BUF float2 of shared memory private to the warp;
+// tw: the stage-ordered twiddle table (WarpFft<N>::TW entries, see wtw_offset).
+template <int N, bool INV>
+__device__ __forceinline__ void warp_fft(float2 (&v)[N / 32], float2* buf, const float2* __restrict__ tw, int t) {
+  static_assert(N >= 64 && N <= 512, "warp FFT covers 64..512 points");
+  warp_fft_from<N, 1, INV>(v, buf, tw, t);
+}
+
+}  // namespace bpmgb

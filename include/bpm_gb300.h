@@ -100,6 +100,9 @@ typedef struct {
   void* ckpt;                    /* device (batch, (nz-1)/ckpt_every+1, ny, nx) complex64: the
                                     field at planes z = 0, k, 2k, ... (k = ckpt_every), or NULL  */
   int ckpt_every;                /* checkpoint spacing k (>= 1 when ckpt is set)                */
+  const void* mask;              /* device (nz, ny, nx) complex64 phase masks of the shared dn
+                                    from bpm_mask_precompute, or NULL to form them on the fly
+                                    (results are bit-identical either way)                     */
 } bpm_request;
 
 /* Library version (BPM_GB300_VERSION). */
@@ -124,7 +127,14 @@ int bpm_plan_create(const bpm_grid_desc* desc, bpm_plan** out);
 /* Release a plan and its device tables. */
 int bpm_plan_destroy(bpm_plan* plan);
 
-/* Bytes of scratch bpm_propagate needs for a request of `batch` fields (256-aligned). */
+/* Fields the march advances together per kernel launch for a request of `batch` fields
+ * (req->group if set, else the library default; 0 for invalid arguments). */
+int bpm_group_size(const bpm_plan* plan, int batch, int group);
+
+/* Bytes of scratch bpm_propagate needs for a request of `batch` fields (256-aligned): one
+ * slot per group of fields that may march at the same time (up to 4, each on its own
+ * stream forked from and joined back to the caller's stream). Any workspace of at least
+ * one slot works; smaller ones march the groups one after another. */
 size_t bpm_workspace_bytes(const bpm_plan* plan, int batch, int group);
 
 /* March every field of the request through all nz slices.
@@ -170,6 +180,13 @@ typedef enum {
  * counterpart: the reference's per-step launches are the kernels of bpm_3d_kernels.cl. */
 int bpm_launch_pass(bpm_plan* plan, const bpm_request* req, void* workspace, size_t workspace_bytes,
                     int pass, int z, void* stream);
+
+/* Phase masks of a dn volume shared by many fields: mask[z][y][x] = taper * exp(-i k0 dz dn)
+ * for real dn, exp(k0 dz Im dn) * exp(-i k0 dz Re dn) for complex dn (the factors of the
+ * reference's mult_dn* kernels, bpm/bpm/kernels/bpm_3d_kernels.cl:20-283, without the
+ * mean-index shift, which the march applies per field). Passing the result as req->mask
+ * saves every field of a batch from re-evaluating them; (nz, ny, nx) complex64 output. */
+int bpm_mask_precompute(bpm_plan* plan, const void* dn, int dn_dtype, void* mask, void* stream);
 
 /* Capture the launches of bpm_propagate for a fixed request and workspace into a CUDA
  * graph; bpm_exec_launch replays it on any stream. The buffers named by `req` and the
