@@ -312,6 +312,61 @@ def bench_ours(args, rank, world, local_rank):
     return res
 
 
+def psf_timing(reps=3):
+    """Config 2's vectorial Debye-Wolf PSF: 256^3, NA 1.1, n0 1.33, lambda 0.5, x-polarised,
+    512 quadrature steps (513 nodes), all four output volumes on the device. The
+    quadrature (debye_accum_kernel) executes 12 flops per octant voxel per node."""
+    import torch
+    import bpm_gb300
+    shape, units = (256, 256, 256), (.1, .1, .1)
+    args = (shape, units, .5, 1.1, 1.33, 512)
+    bpm_gb300.psf(*args, return_field=True, device=True)
+    torch.cuda.synchronize()
+    a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    a.record()
+    for _ in range(reps):
+        bpm_gb300.psf(*args, return_field=True, device=True)
+    b.record()
+    torch.cuda.synchronize()
+    t = a.elapsed_time(b) / reps
+    octant = 129 ** 3
+    flops = octant * 513 * 12
+    out_bytes = 256 ** 3 * 28
+    return {"workload": "vectorial PSF 256^3, NA 1.1, n0 1.33, 513 nodes, u+ex+ey+ez",
+            "ms": t, "voxels_per_s": 256 ** 3 / (t * 1e-3),
+            "quadrature_tflops": flops / (t * 1e-3) / 1e12, "quadrature_flops": flops,
+            "output_gbs": out_bytes / (t * 1e-3) / 1e9}
+
+
+def adjoint_timing():
+    """Config 4: d(loss)/d(dn) on 256x256x128 for 16 angles within NA 0.6, checkpoints
+    every 16 slices: forward march + hand-written adjoint (recompute + backward)."""
+    import torch
+    from bpm_gb300.adjoint import propagate_exit
+    size, units = (256, 256, 128), (.1, .1, .1)
+    u0 = torch.from_numpy(make_u0(16, 256, 256, SEED + 7)).cuda()
+    g = torch.Generator(device="cuda").manual_seed(3)
+    dn = (torch.rand((128, 256, 256), device="cuda", generator=g) * .04).requires_grad_(True)
+    target = torch.rand((16, 256, 256), device="cuda", generator=g)
+
+    def one():
+        dn.grad = None
+        out = propagate_exit(dn, u0, size, units, LAM, N0, ckpt_every=16)
+        ((out.abs() ** 2 - target) ** 2).sum().backward()
+    one()
+    torch.cuda.synchronize()
+    a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    a.record()
+    for _ in range(3):
+        one()
+    b.record()
+    torch.cuda.synchronize()
+    t = a.elapsed_time(b) / 3
+    vu = 16 * 256 * 256 * 127
+    return {"workload": "config 4: 256x256x128, 16 angles, ckpt 16, forward + adjoint", "ms": t,
+            "forward_voxel_updates_per_s_equiv": vu / (t * 1e-3)}
+
+
 def sphere_pool(side, nz, seed, n=50):
     """Complex random-sphere dn on the device: 50 spheres, radius U[3,15] px,
     Re dn U[0.01,0.05], Im dn U[0,1e-3] (input synthesis only)."""
@@ -494,6 +549,8 @@ def main():
     if rank == 0:
         if not args.no_serve:
             res["serve"] = serve_trace()
+        res["psf"] = psf_timing()
+        res["adjoint"] = adjoint_timing()
         if not args.no_cpu_baseline:
             v, t, sample = cpu_sample(4, NZ - 1)
             res["cpu_baseline"] = {"value": v, "unit": "voxel-updates/s", "cores": host_cores(), "kind": "port",

@@ -76,8 +76,17 @@ SIGNATURES = {
     "bpm_exec_create": (c_int, [c_vp, ctypes.POINTER(Request), c_vp, c_size, ctypes.POINTER(c_vp)]),
     "bpm_exec_launch": (c_int, [c_vp, c_vp]),
     "bpm_exec_destroy": (c_int, [c_vp]),
+    "bpm_spheres_fill": (c_int, [c_int, c_int, c_int, c_double, c_double, c_double, c_vp, c_int,
+                                 c_double, c_double, c_double, c_double, c_vp, c_vp]),
     "debye_workspace_bytes": (c_size, [ctypes.POINTER(DebyeDesc)]),
     "debye_focus_field": (c_int, [ctypes.POINTER(DebyeDesc), c_vp, c_vp, c_vp, c_vp, c_vp, c_size, c_vp]),
+    "debye_gauss_workspace_bytes": (c_size, [ctypes.POINTER(DebyeDesc)]),
+    "debye_focus_field_gauss": (c_int, [ctypes.POINTER(DebyeDesc), c_double, c_vp, c_vp, c_vp, c_vp, c_vp, c_size,
+                                        c_vp]),
+    "debye_points_workspace_bytes": (c_size, [ctypes.POINTER(DebyeDesc)]),
+    "debye_focus_field_plane": (c_int, [ctypes.POINTER(DebyeDesc), c_double, c_vp, c_vp, c_size, c_vp]),
+    "debye_focus_field_at": (c_int, [ctypes.POINTER(DebyeDesc), c_vp, c_vp, c_vp, ctypes.c_longlong, c_vp, c_vp, c_vp,
+                                     c_vp, c_vp, c_size, c_vp]),
 }
 
 _lib = None

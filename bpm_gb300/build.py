@@ -16,7 +16,7 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 CSRC = os.path.join(HERE, "csrc")
 LIB = os.path.join(HERE, "libbpm_gb300.so")
 BUILD = os.path.join(HERE, "_build")
-SOURCES = ["capi.cu", "bpm_march.cu", "debye.cu"]
+SOURCES = ["capi.cu", "bpm_march.cu", "debye.cu", "spheres.cu"]
 
 ARCH = "-gencode=arch=compute_103a,code=sm_103a"
 

@@ -31,22 +31,49 @@ namespace {
 
 constexpr int MAX_NA = 16;
 
+// Pupil weight of each quadrature node.
+//   W_STD:   psf_debye.cl:70-75, half weight at i = 0 and i = INT_STEPS, dt sqrt(cos t)
+//   W_SINE:  psf_debye.cl:155-159 / :240-244, half weight where the float32 angle equals an
+//            annulus limit, dt sqrt(cos t) sin t (debye_wolf_plane, debye_wolf_at)
+//   W_GAUSS: psf_debye.cl:336-339, W_SINE times exp(t^2 * gauss_prefac)
+enum WeightKind { W_STD = 0, W_SINE = 1, W_GAUSS = 2 };
+
 struct NodeArgs {
   float alpha[MAX_NA];
   int n_ann;
   int steps;
+  int kind;
+  double gauss_prefac;
 };
+
+// Octant (or plane) grid: x = x1 + i*(x2-x1)/(N-1.f) per axis
+struct OctGeom {
+  int nxo, nyo, nzo;
+  float x1, x2, y1, y2, z1, z2;
+};
+
+// Mirroring of the octant onto the full volume
+//   MIR_STD:   focus_field_debye (:116-144), full index m -> |m - N0/2|, conj for z <= Nz0/2
+//   MIR_GAUSS: focus_field_debye_gauss (:426-438), p -> p - (N0-N) for p >= N0-N else
+//              N-1-p, no conjugation
+enum MirrorKind { MIR_STD = 0, MIR_GAUSS = 1 };
 
 struct DebyeLayout {
   size_t si, ct, wf, kr, trig, J, E, I, total;
   int T, M, Zo, nxo, nyo, nzo;
 };
 
-DebyeLayout debye_layout(const debye_desc* d) {
+DebyeLayout debye_layout(const debye_desc* d, bool gauss = false) {
   DebyeLayout L;
-  L.nxo = d->nx / 2 + 1;
-  L.nyo = d->ny / 2 + 1;
-  L.nzo = d->nz / 2 + 1;
+  if (gauss) {
+    L.nxo = (d->nx + 1) / 2;
+    L.nyo = (d->ny + 1) / 2;
+    L.nzo = (d->nz + 1) / 2;
+  } else {
+    L.nxo = d->nx / 2 + 1;
+    L.nyo = d->ny / 2 + 1;
+    L.nzo = d->nz / 2 + 1;
+  }
   L.T = (d->n_na / 2) * (d->n_integration_steps + 1);
   L.M = L.nxo * L.nyo;
   L.Zo = L.nzo;
@@ -63,9 +90,9 @@ DebyeLayout debye_layout(const debye_desc* d) {
   return L;
 }
 
-// x = x1 + i*(x2-x1)/(N-1.f) with x1 = 0, FP32 as the kernel evaluates it (psf_debye.cl:46-48)
-__device__ __forceinline__ float coord_f32(int i, float x2, int N) {
-  return 0.f + __fdiv_rn(__fmul_rn((float)i, x2 - 0.f), (float)N - 1.f);
+// x = x1 + i*(x2-x1)/(N-1.f), FP32 as the kernels evaluate it (psf_debye.cl:46-48)
+__device__ __forceinline__ float coord_f32(int i, float x1, float x2, int N) {
+  return __fadd_rn(x1, __fdiv_rn(__fmul_rn((float)i, __fsub_rn(x2, x1)), __fsub_rn((float)N, 1.f)));
 }
 
 // trapezoid nodes and weights per annulus (psf_debye.cl:62-78), FP64
@@ -79,7 +106,17 @@ __global__ void debye_nodes_kernel(NodeArgs a, double* si, double* ct, float* wf
   const double t = a1 + i * dt;
   double s, c;
   sincos(t, &s, &c);
-  const double w = ((i == 0 || i == a.steps) ? .5 : 1.) * dt * sqrt(c);
+  double w;
+  if (a.kind == W_STD) {
+    w = ((i == 0 || i == a.steps) ? .5 : 1.) * dt * sqrt(c);
+  } else {
+    // the end test runs on the float32 angle, each operation rounded on its own
+    const float a1f = a.alpha[2 * ann], a2f = a.alpha[2 * ann + 1];
+    const float dtf = __fdiv_rn(__fsub_rn(a2f, a1f), __fsub_rn((float)a.steps, 1.f));
+    const float tf = __fadd_rn(a1f, __fmul_rn((float)i, dtf));
+    w = ((tf == a1f || tf == a2f) ? .5 : 1.) * dt * sqrt(c) * s;
+    if (a.kind == W_GAUSS) w *= exp(t * t * a.gauss_prefac);
+  }
   si[idx] = s;
   ct[idx] = c;
   wf[idx] = (float)(w * (c + 1.));
@@ -88,11 +125,11 @@ __global__ void debye_nodes_kernel(NodeArgs a, double* si, double* ct, float* wf
 }
 
 // radius and azimuth per octant column (ix, jy)
-__global__ void debye_radii_kernel(int nxo, int nyo, float x2, float y2, double k, double* kr, float* trig, int M) {
+__global__ void debye_radii_kernel(OctGeom g, double k, double* kr, float* trig, int M) {
   int m = blockIdx.x * blockDim.x + threadIdx.x;
   if (m >= M) return;
-  const int jy = m / nxo, ix = m - jy * nxo;
-  const double x = coord_f32(ix, x2, nxo), y = coord_f32(jy, y2, nyo);
+  const int jy = m / g.nxo, ix = m - jy * g.nxo;
+  const double x = coord_f32(ix, g.x1, g.x2, g.nxo), y = coord_f32(jy, g.y1, g.y2, g.nyo);
   kr[m] = k * sqrt(x * x + y * y);
   const double phi = atan2(y, x);
   double s1, c1, s2, c2;
@@ -105,11 +142,11 @@ __global__ void debye_radii_kernel(int nxo, int nyo, float x2, float y2, double 
 }
 
 // E(t, z) = exp(i kz cos t), phase formed and reduced in FP64
-__global__ void debye_phase_kernel(int Zo, float z2, double k, const double* ct, float2* E, int T) {
+__global__ void debye_phase_kernel(int Zo, float z1, float z2, double k, const double* ct, float2* E, int T) {
   int idx = blockIdx.x * blockDim.x + threadIdx.x;
   if (idx >= T * Zo) return;
   const int t = idx / Zo, z = idx - t * Zo;
-  const double kz = k * (double)coord_f32(z, z2, Zo);
+  const double kz = k * (double)(Zo == 1 ? z1 : coord_f32(z, z1, z2, Zo));
   double s, c;
   sincos(kz * ct[t], &s, &c);
   E[idx] = make_float2((float)c, (float)s);
@@ -214,17 +251,29 @@ __global__ void __launch_bounds__(256) debye_accum_kernel(int T, int M, int Zo, 
     }
 }
 
+__device__ __forceinline__ int mirror_gauss(int p, int N0, int N) {
+  return p >= N0 - N ? p - (N0 - N) : N - 1 - p;
+}
+
 // full-volume assembly fused with the octant mirroring
-__global__ void debye_assemble_kernel(int nx, int ny, int nz, int nxo, int M, int Zo, float ex0, float ey0,
+template <int MIR>
+__global__ void debye_assemble_kernel(int nx, int ny, int nz, OctGeom g, int M, int Zo, float ex0, float ey0,
                                       const float2* __restrict__ I, const float* __restrict__ trig,
                                       float* __restrict__ u, float2* __restrict__ ex, float2* __restrict__ ey,
                                       float2* __restrict__ ez) {
   const int x = blockIdx.x * blockDim.x + threadIdx.x;
   const int y = blockIdx.y, z = blockIdx.z;
   if (x >= nx) return;
-  const int ix = abs(x - nx / 2), jy = abs(y - ny / 2), kz = abs(z - nz / 2);
-  const bool conj = z <= nz / 2;
-  const int m = jy * nxo + ix;
+  int ix, jy, kz;
+  bool conj;
+  if (MIR == MIR_STD) {
+    ix = abs(x - nx / 2), jy = abs(y - ny / 2), kz = abs(z - nz / 2);
+    conj = z <= nz / 2;
+  } else {
+    ix = mirror_gauss(x, nx, g.nxo), jy = mirror_gauss(y, ny, g.nyo), kz = mirror_gauss(z, nz, g.nzo);
+    conj = false;
+  }
+  const int m = jy * g.nxo + ix;
   const size_t ZM = (size_t)Zo * M, o = (size_t)kz * M + m;
   const float2 I0 = __ldg(I + o), I1 = __ldg(I + ZM + o), I2 = __ldg(I + 2 * ZM + o);
   const float c1 = __ldg(trig + m), s1 = __ldg(trig + M + m);
@@ -246,22 +295,286 @@ __global__ void debye_assemble_kernel(int nx, int ny, int nz, int nxo, int M, in
   if (ez) __stcs(ez + v, vz);
 }
 
-int check_desc(const debye_desc* d) {
-  if (!d) { set_error("description is NULL"); return BPM_ERR_ARG; }
-  if (d->nx < 2 || d->ny < 2 || d->nz < 2) { set_error("shape must be >= 2 in every axis"); return BPM_ERR_SHAPE; }
-  if (d->nx % 2 + d->ny % 2 + d->nz % 2 != 0) {
-    set_error("odd shapes not supported yet");  // _focus_fields_debye.py:81-82
-    return BPM_ERR_SHAPE;
+// Fields at arbitrary points (debye_wolf_at, psf_debye.cl:187-269) or on one z plane
+// (debye_wolf_plane, :117-183). Without a grid in z the quadrature does not factorise into
+// a matrix product, so each thread sums its point's integrand over the nodes, as the
+// reference does, with the node tables staged through shared memory. On the plane the
+// phase e^{i kz cos t} is one table over the nodes; at free points the argument kz cos t
+// is formed and reduced modulo 2 pi in FP64 and the reduced angle goes through sincosf.
+struct PointArgs {
+  long long n;
+  int nx, ny;  // plane grid (GRID only)
+  float x1, x2, y1, y2;
+  double k;
+  float ex0, ey0;
+  int T;
+};
+
+constexpr int PT_THREADS = 128, PT_CHUNK = 256;
+constexpr double kTwoPi = 6.283185307179586, kInvTwoPi = 0.15915494309189535;
+
+template <bool GRID>
+__global__ void __launch_bounds__(PT_THREADS) debye_points_kernel(
+    PointArgs a, const float* __restrict__ xs, const float* __restrict__ ys, const float* __restrict__ zs,
+    const double* __restrict__ si, const double* __restrict__ ct, const float* __restrict__ wf,
+    const float2* __restrict__ Et, float* __restrict__ u, float2* __restrict__ ex, float2* __restrict__ ey,
+    float2* __restrict__ ez) {
+  __shared__ float s_si[PT_CHUNK];
+  __shared__ float s_w[3][PT_CHUNK];
+  __shared__ double s_ct[GRID ? 1 : PT_CHUNK];
+  __shared__ float2 s_E[GRID ? PT_CHUNK : 1];
+  const long long p = (long long)blockIdx.x * PT_THREADS + threadIdx.x;
+  const bool active = p < a.n;
+  float x = 0.f, y = 0.f, z = 0.f;
+  if (active) {
+    if (GRID) {
+      const int j = (int)(p / a.nx), i = (int)(p - (long long)j * a.nx);
+      x = coord_f32(i, a.x1, a.x2, a.nx);
+      y = coord_f32(j, a.y1, a.y2, a.ny);
+    } else {
+      x = xs[p];
+      y = ys[p];
+      z = zs[p];
+    }
   }
+  const double xd = x, yd = y;
+  const float kr = (float)(a.k * sqrt(xd * xd + yd * yd));
+  const double kz = a.k * (double)z;
+  float2 I0 = make_float2(0.f, 0.f), I1 = I0, I2 = I0;
+  for (int t0 = 0; t0 < a.T; t0 += PT_CHUNK) {
+    const int nt = min(PT_CHUNK, a.T - t0);
+    __syncthreads();
+    for (int e = threadIdx.x; e < nt; e += PT_THREADS) {
+      s_si[e] = (float)si[t0 + e];
+      s_w[0][e] = wf[t0 + e];
+      s_w[1][e] = wf[a.T + t0 + e];
+      s_w[2][e] = wf[2 * a.T + t0 + e];
+      if (GRID)
+        s_E[e] = Et[t0 + e];
+      else
+        s_ct[e] = ct[t0 + e];
+    }
+    __syncthreads();
+    if (!active) continue;
+    for (int tt = 0; tt < nt; tt++) {
+      const float xb = kr * s_si[tt];
+      const float j0 = j0f(xb), j1 = j1f(xb);
+      const float j2 = bessel_j2(xb, j0, j1);
+      float2 e;
+      if (GRID) {
+        e = s_E[tt];
+      } else {
+        const double arg = kz * s_ct[tt];
+        const double q = rint(arg * kInvTwoPi);
+        sincosf((float)fma(-q, kTwoPi, arg), &e.y, &e.x);
+      }
+      const float a0 = s_w[0][tt] * j0, a1 = s_w[1][tt] * j1, a2 = s_w[2][tt] * j2;
+      I0.x = fmaf(a0, e.x, I0.x);
+      I0.y = fmaf(a0, e.y, I0.y);
+      I1.x = fmaf(a1, e.x, I1.x);
+      I1.y = fmaf(a1, e.y, I1.y);
+      I2.x = fmaf(a2, e.x, I2.x);
+      I2.y = fmaf(a2, e.y, I2.y);
+    }
+  }
+  if (!active) return;
+  const double phi = atan2(yd, xd);
+  double s1d, c1d, s2d, c2d;
+  sincos(phi, &s1d, &c1d);
+  sincos(2. * phi, &s2d, &c2d);
+  const float c1 = (float)c1d, s1 = (float)s1d, c2 = (float)c2d, s2 = (float)s2d;
+  const float ex0 = a.ex0, ey0 = a.ey0;
+  // psf_debye.cl:254-263
+  const float2 vx = make_float2(ex0 * (I0.x + I2.x * c2) + (ey0 * s2) * I2.x,
+                                ex0 * (I0.y + I2.y * c2) + (ey0 * s2) * I2.y);
+  if (ex) ex[p] = vx;
+  if (u) u[p] = cabs2(vx);  // the reference kernel stores |ex|^2 (psf_debye.cl:267)
+  if (ey) ey[p] = make_float2(ey0 * (I0.x - I2.x * c2) + (ex0 * s2) * I2.x, ey0 * (I0.y - I2.y * c2) + (ex0 * s2) * I2.y);
+  const float pz = ex0 * c1 + ey0 * s1;
+  if (ez) ez[p] = make_float2(2.f * I1.y * pz, -2.f * I1.x * pz);
+}
+
+enum Variant { V_STD = 0, V_GAUSS = 1, V_PLANE = 2, V_AT = 3 };
+
+int check_desc(const debye_desc* d, Variant v = V_STD) {
+  if (!d) { set_error("description is NULL"); return BPM_ERR_ARG; }
+  if (v == V_STD) {
+    if (d->nx < 2 || d->ny < 2 || d->nz < 2) { set_error("shape must be >= 2 in every axis"); return BPM_ERR_SHAPE; }
+    if (d->nx % 2 + d->ny % 2 + d->nz % 2 != 0) {
+      set_error("odd shapes not supported yet");  // _focus_fields_debye.py:81-82
+      return BPM_ERR_SHAPE;
+    }
+  } else if (v == V_GAUSS) {
+    // octant (N0+1)/2 >= 2 per axis: the grid divides by (N-1)
+    if (d->nx < 3 || d->ny < 3 || d->nz < 3) { set_error("shape must be >= 3 in every axis"); return BPM_ERR_SHAPE; }
+  } else if (v == V_PLANE) {
+    if (d->nx < 2 || d->ny < 2) { set_error("plane shape must be >= 2 in both axes"); return BPM_ERR_SHAPE; }
+  }
+  if (d->ny > 65535 || d->nz > 65535) { set_error("ny and nz must be <= 65535"); return BPM_ERR_SHAPE; }
   if (!d->na || d->n_na < 2 || d->n_na % 2 || d->n_na > MAX_NA) {
     set_error("NA must be a scalar or an even-length list of at most 16 values");
     return BPM_ERR_ARG;
   }
   if (d->n_integration_steps < 2) { set_error("n_integration_steps must be >= 2"); return BPM_ERR_ARG; }
-  if (!(d->lam > 0) || !(d->n0 > 0) || !(d->dx > 0) || !(d->dy > 0) || !(d->dz >= 0)) {
-    set_error("lam, n0, dx, dy must be positive and dz >= 0");
+  if ((long long)(d->n_na / 2) * (d->n_integration_steps + 1) > 65535) {
+    set_error("too many quadrature nodes: (len(NA)/2) * (n_integration_steps+1) must be <= 65535");
     return BPM_ERR_ARG;
   }
+  if (!(d->lam > 0) || !(d->n0 > 0)) { set_error("lam and n0 must be positive"); return BPM_ERR_ARG; }
+  if ((v == V_STD || v == V_GAUSS || v == V_PLANE) && (!(d->dx > 0) || !(d->dy > 0))) {
+    set_error("dx and dy must be positive");
+    return BPM_ERR_ARG;
+  }
+  if ((v == V_STD || v == V_GAUSS) && !(d->dz >= 0)) { set_error("dz must be >= 0"); return BPM_ERR_ARG; }
+  return BPM_OK;
+}
+
+NodeArgs node_args(const debye_desc* d, int kind) {
+  NodeArgs na;
+  memset(&na, 0, sizeof(na));
+  na.n_ann = d->n_na / 2;
+  na.steps = d->n_integration_steps;
+  na.kind = kind;
+  // alphas = arcsin(NA/n0) cast to float32 (_focus_fields_debye.py:76, :108)
+  for (int i = 0; i < d->n_na; i++) na.alpha[i] = (float)asin(d->na[i] / d->n0);
+  return na;
+}
+
+// lam/n0 as the float32 kernel argument, and 2 pi / lam from it
+double wave_number(const debye_desc* d) {
+  const float lamf = (float)(1. * d->lam / d->n0);
+  return 2. * M_PI / (double)lamf;
+}
+
+// the octant pipeline shared by focus_field_debye and focus_field_debye_gauss
+int run_octant(const debye_desc* d, bool gauss, double sig, float* u, void* ex, void* ey, void* ez, void* ws,
+               size_t ws_bytes, cudaStream_t s) {
+  DebyeLayout L = debye_layout(d, gauss);
+  if (!ws || ws_bytes < L.total) {
+    set_error("workspace too small: need " + std::to_string(L.total) + " bytes");
+    return BPM_ERR_OOM;
+  }
+  char* w = static_cast<char*>(ws);
+  double* si = reinterpret_cast<double*>(w + L.si);
+  double* ct = reinterpret_cast<double*>(w + L.ct);
+  float* wf = reinterpret_cast<float*>(w + L.wf);
+  double* kr = reinterpret_cast<double*>(w + L.kr);
+  float* trig = reinterpret_cast<float*>(w + L.trig);
+  float* J = reinterpret_cast<float*>(w + L.J);
+  float2* E = reinterpret_cast<float2*>(w + L.E);
+  float2* I = reinterpret_cast<float2*>(w + L.I);
+
+  NodeArgs na = node_args(d, gauss ? W_GAUSS : W_STD);
+  OctGeom g;
+  g.nxo = L.nxo;
+  g.nyo = L.nyo;
+  g.nzo = L.nzo;
+  g.x1 = g.y1 = g.z1 = 0.f;
+  if (gauss) {
+    // _focus_fields_debye.py:404-412: x2 = dx*Nx with Nx the octant size
+    g.x2 = (float)(d->dx * L.nxo);
+    g.y2 = (float)(d->dy * L.nyo);
+    g.z2 = (float)(d->dz * L.nzo);
+    // psf_debye.cl:310-311: exp_prefac = -.5/alpha_max^2/sig^2, from the float32 arguments
+    const double amax = na.alpha[d->n_na - 1], sg = (float)sig;
+    na.gauss_prefac = -.5 / amax / amax / sg / sg;
+  } else {
+    // _focus_fields_debye.py:102-109
+    g.x2 = (float)(d->dx * (L.nxo - 1.));
+    g.y2 = (float)(d->dy * (L.nyo - 1.));
+    g.z2 = (float)(d->dz * (L.nzo - 1.));
+  }
+  const double k = wave_number(d);
+
+  debye_nodes_kernel<<<(L.T + 127) / 128, 128, 0, s>>>(na, si, ct, wf, L.T);
+  BPM_LAUNCH_CHECK("debye_nodes_kernel");
+  debye_radii_kernel<<<(L.M + 127) / 128, 128, 0, s>>>(g, k, kr, trig, L.M);
+  BPM_LAUNCH_CHECK("debye_radii_kernel");
+  debye_phase_kernel<<<(L.T * L.Zo + 127) / 128, 128, 0, s>>>(L.Zo, g.z1, g.z2, k, ct, E, L.T);
+  BPM_LAUNCH_CHECK("debye_phase_kernel");
+  debye_bessel_kernel<<<dim3((L.M + 127) / 128, L.T), 128, 0, s>>>(L.T, L.M, si, kr, wf, J);
+  BPM_LAUNCH_CHECK("debye_bessel_kernel");
+  debye_accum_kernel<<<dim3((L.M + AM - 1) / AM, (L.Zo + AZ - 1) / AZ), 256, 0, s>>>(L.T, L.M, L.Zo, J, E, I);
+  BPM_LAUNCH_CHECK("debye_accum_kernel");
+  if (u || ex || ey || ez) {
+    const dim3 grid((d->nx + 127) / 128, d->ny, d->nz);
+    float2 *pex = static_cast<float2*>(ex), *pey = static_cast<float2*>(ey), *pez = static_cast<float2*>(ez);
+    if (gauss)
+      debye_assemble_kernel<MIR_GAUSS><<<grid, 128, 0, s>>>(d->nx, d->ny, d->nz, g, L.M, L.Zo, (float)d->ex0,
+                                                            (float)d->ey0, I, trig, u, pex, pey, pez);
+    else
+      debye_assemble_kernel<MIR_STD><<<grid, 128, 0, s>>>(d->nx, d->ny, d->nz, g, L.M, L.Zo, (float)d->ex0,
+                                                          (float)d->ey0, I, trig, u, pex, pey, pez);
+    BPM_LAUNCH_CHECK("debye_assemble_kernel");
+  }
+  return BPM_OK;
+}
+
+struct PointsLayout {
+  size_t si, ct, wf, E, total;
+  int T;
+};
+
+PointsLayout points_layout(const debye_desc* d) {
+  PointsLayout L;
+  L.T = (d->n_na / 2) * (d->n_integration_steps + 1);
+  size_t off = 0;
+  L.si = off; off += align256(sizeof(double) * L.T);
+  L.ct = off; off += align256(sizeof(double) * L.T);
+  L.wf = off; off += align256(sizeof(float) * 3 * L.T);
+  L.E = off; off += align256(sizeof(float2) * L.T);
+  L.total = off;
+  return L;
+}
+
+// shared by focus_field_debye_plane (GRID) and focus_field_debye_at
+int run_points(const debye_desc* d, bool grid, double zplane, const float* xs, const float* ys, const float* zs,
+               long long n, float* u, void* ex, void* ey, void* ez, void* ws, size_t ws_bytes, cudaStream_t s) {
+  PointsLayout L = points_layout(d);
+  if (!ws || ws_bytes < L.total) {
+    set_error("workspace too small: need " + std::to_string(L.total) + " bytes");
+    return BPM_ERR_OOM;
+  }
+  char* w = static_cast<char*>(ws);
+  double* si = reinterpret_cast<double*>(w + L.si);
+  double* ct = reinterpret_cast<double*>(w + L.ct);
+  float* wf = reinterpret_cast<float*>(w + L.wf);
+  float2* E = reinterpret_cast<float2*>(w + L.E);
+  NodeArgs na = node_args(d, W_SINE);
+  const double k = wave_number(d);
+  debye_nodes_kernel<<<(L.T + 127) / 128, 128, 0, s>>>(na, si, ct, wf, L.T);
+  BPM_LAUNCH_CHECK("debye_nodes_kernel");
+  PointArgs a;
+  memset(&a, 0, sizeof(a));
+  a.n = n;
+  a.k = k;
+  a.ex0 = (float)d->ex0;
+  a.ey0 = (float)d->ey0;
+  a.T = L.T;
+  if (n == 0) return BPM_OK;
+  const long long blocks = (n + PT_THREADS - 1) / PT_THREADS;
+  if (blocks > 0x7fffffffLL) { set_error("too many points"); return BPM_ERR_SHAPE; }
+  if (grid) {
+    // _focus_fields_debye.py:201-209: x in [-(Nx//2) dx, (Nx - Nx//2) dx], float32
+    a.nx = d->nx;
+    a.ny = d->ny;
+    a.x1 = (float)(-(double)(d->nx / 2) * d->dx);
+    a.x2 = (float)((double)(d->nx - d->nx / 2) * d->dx);
+    a.y1 = (float)(-(double)(d->ny / 2) * d->dy);
+    a.y2 = (float)((double)(d->ny - d->ny / 2) * d->dy);
+    debye_phase_kernel<<<(L.T + 127) / 128, 128, 0, s>>>(1, (float)zplane, 0.f, k, ct, E, L.T);
+    BPM_LAUNCH_CHECK("debye_phase_kernel");
+    debye_points_kernel<true><<<(unsigned)blocks, PT_THREADS, 0, s>>>(a, nullptr, nullptr, nullptr, si, ct, wf, E,
+                                                                      u, static_cast<float2*>(ex),
+                                                                      static_cast<float2*>(ey),
+                                                                      static_cast<float2*>(ez));
+  } else {
+    debye_points_kernel<false><<<(unsigned)blocks, PT_THREADS, 0, s>>>(a, xs, ys, zs, si, ct, wf, E, u,
+                                                                       static_cast<float2*>(ex),
+                                                                       static_cast<float2*>(ey),
+                                                                       static_cast<float2*>(ez));
+  }
+  BPM_LAUNCH_CHECK("debye_points_kernel");
   return BPM_OK;
 }
 
@@ -277,48 +590,45 @@ extern "C" int debye_focus_field(const debye_desc* d, float* u, void* ex, void* 
   clear_error();
   int rc = check_desc(d);
   if (rc) return rc;
-  DebyeLayout L = debye_layout(d);
-  if (!ws || ws_bytes < L.total) {
-    set_error("workspace too small: need " + std::to_string(L.total) + " bytes");
-    return BPM_ERR_OOM;
-  }
-  cudaStream_t s = static_cast<cudaStream_t>(stream);
-  char* w = static_cast<char*>(ws);
-  double* si = reinterpret_cast<double*>(w + L.si);
-  double* ct = reinterpret_cast<double*>(w + L.ct);
-  float* wf = reinterpret_cast<float*>(w + L.wf);
-  double* kr = reinterpret_cast<double*>(w + L.kr);
-  float* trig = reinterpret_cast<float*>(w + L.trig);
-  float* J = reinterpret_cast<float*>(w + L.J);
-  float2* E = reinterpret_cast<float2*>(w + L.E);
-  float2* I = reinterpret_cast<float2*>(w + L.I);
+  return run_octant(d, false, 0., u, ex, ey, ez, ws, ws_bytes, static_cast<cudaStream_t>(stream));
+}
 
-  // the float32 launch arguments of _focus_fields_debye.py:102-109
-  NodeArgs na;
-  memset(&na, 0, sizeof(na));
-  na.n_ann = d->n_na / 2;
-  na.steps = d->n_integration_steps;
-  for (int i = 0; i < d->n_na; i++) na.alpha[i] = (float)asin(d->na[i] / d->n0);
-  const float x2 = (float)(d->dx * (L.nxo - 1.)), y2 = (float)(d->dy * (L.nyo - 1.)),
-              z2 = (float)(d->dz * (L.nzo - 1.));
-  const float lamf = (float)(1. * d->lam / d->n0);
-  const double k = 2. * M_PI / (double)lamf;
+extern "C" size_t debye_gauss_workspace_bytes(const debye_desc* d) {
+  if (check_desc(d, V_GAUSS)) return 0;
+  return debye_layout(d, true).total;
+}
 
-  debye_nodes_kernel<<<(L.T + 127) / 128, 128, 0, s>>>(na, si, ct, wf, L.T);
-  BPM_LAUNCH_CHECK("debye_nodes_kernel");
-  debye_radii_kernel<<<(L.M + 127) / 128, 128, 0, s>>>(L.nxo, L.nyo, x2, y2, k, kr, trig, L.M);
-  BPM_LAUNCH_CHECK("debye_radii_kernel");
-  debye_phase_kernel<<<(L.T * L.Zo + 127) / 128, 128, 0, s>>>(L.Zo, z2, k, ct, E, L.T);
-  BPM_LAUNCH_CHECK("debye_phase_kernel");
-  debye_bessel_kernel<<<dim3((L.M + 127) / 128, L.T), 128, 0, s>>>(L.T, L.M, si, kr, wf, J);
-  BPM_LAUNCH_CHECK("debye_bessel_kernel");
-  debye_accum_kernel<<<dim3((L.M + AM - 1) / AM, (L.Zo + AZ - 1) / AZ), 256, 0, s>>>(L.T, L.M, L.Zo, J, E, I);
-  BPM_LAUNCH_CHECK("debye_accum_kernel");
-  if (u || ex || ey || ez) {
-    debye_assemble_kernel<<<dim3((d->nx + 127) / 128, d->ny, d->nz), 128, 0, s>>>(
-        d->nx, d->ny, d->nz, L.nxo, L.M, L.Zo, (float)d->ex0, (float)d->ey0, I, trig, u,
-        static_cast<float2*>(ex), static_cast<float2*>(ey), static_cast<float2*>(ez));
-    BPM_LAUNCH_CHECK("debye_assemble_kernel");
-  }
-  return BPM_OK;
+extern "C" int debye_focus_field_gauss(const debye_desc* d, double sig, float* u, void* ex, void* ey, void* ez,
+                                       void* ws, size_t ws_bytes, void* stream) {
+  clear_error();
+  int rc = check_desc(d, V_GAUSS);
+  if (rc) return rc;
+  if (!(sig > 0)) { set_error("sig must be > 0"); return BPM_ERR_ARG; }  // _focus_fields_debye.py:387
+  return run_octant(d, true, sig, u, ex, ey, ez, ws, ws_bytes, static_cast<cudaStream_t>(stream));
+}
+
+extern "C" size_t debye_points_workspace_bytes(const debye_desc* d) {
+  if (check_desc(d, V_AT)) return 0;
+  return points_layout(d).total;
+}
+
+extern "C" int debye_focus_field_plane(const debye_desc* d, double z, void* ex, void* ws, size_t ws_bytes,
+                                       void* stream) {
+  clear_error();
+  int rc = check_desc(d, V_PLANE);
+  if (rc) return rc;
+  if (!ex) { set_error("ex is NULL"); return BPM_ERR_ARG; }
+  return run_points(d, true, z, nullptr, nullptr, nullptr, (long long)d->nx * d->ny, nullptr, ex, nullptr,
+                    nullptr, ws, ws_bytes, static_cast<cudaStream_t>(stream));
+}
+
+extern "C" int debye_focus_field_at(const debye_desc* d, const float* x, const float* y, const float* z,
+                                    long long n, float* u, void* ex, void* ey, void* ez, void* ws,
+                                    size_t ws_bytes, void* stream) {
+  clear_error();
+  int rc = check_desc(d, V_AT);
+  if (rc) return rc;
+  if (n < 0) { set_error("n must be >= 0"); return BPM_ERR_ARG; }
+  if (n > 0 && (!x || !y || !z)) { set_error("coordinate arrays are NULL"); return BPM_ERR_ARG; }
+  return run_points(d, false, 0., x, y, z, n, u, ex, ey, ez, ws, ws_bytes, static_cast<cudaStream_t>(stream));
 }

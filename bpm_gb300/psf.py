@@ -14,29 +14,42 @@ import torch
 from . import _native as N
 from .bpm3d import _device, _d2h, _ptr, _stream_ptr
 
-__all__ = ["focus_field_debye", "psf", "psf_u0", "psf_lightsheet"]
+__all__ = ["focus_field_debye", "focus_field_debye_gauss", "focus_field_debye_plane", "focus_field_debye_at",
+           "psf", "psf_u0", "psf_lightsheet"]
+
+
+def _desc(shape3, units3, lam, NA, n0, n_integration_steps, ex0=1., ey0=0.):
+    """debye_desc for the C ABI; returns (desc, keep-alive NA array)."""
+    if np.isscalar(NA):
+        NA = [0., NA]
+    NA = [float(a) for a in np.asarray(NA, np.float64).ravel()]
+    assert len(NA) % 2 == 0
+    na = (ctypes.c_double * len(NA))(*NA)
+    desc = N.DebyeDesc(int(shape3[0]), int(shape3[1]), int(shape3[2]), float(units3[0]), float(units3[1]),
+                       float(units3[2]), float(lam), float(n0), ctypes.cast(na, ctypes.POINTER(ctypes.c_double)),
+                       len(NA), int(n_integration_steps), float(ex0), float(ey0))
+    return desc, na
+
+
+def _workspace(size_fn, run_fn, desc, what):
+    """Workspace tensor for `desc`; a size of 0 means the description is invalid, and the
+    entry point itself then reports why."""
+    wsb = int(size_fn(ctypes.byref(desc)))
+    if wsb == 0:
+        N.check(run_fn(), what)
+    return torch.empty(wsb, dtype=torch.uint8, device=_device()), wsb
 
 
 def _debye(shape, units, lam, NA, n0, n_integration_steps, want_u, want_field, ex0=1., ey0=0.):
-    if np.isscalar(NA):
-        NA = [0., NA]
-    NA = [float(a) for a in NA]
     Nx0, Ny0, Nz0 = (int(s) for s in shape)
-    dx, dy, dz = (float(u) for u in units)
     if not Nx0 % 2 + Ny0 % 2 + Nz0 % 2 == 0:
         raise NotImplementedError("odd shapes not supported yet")
-    assert len(NA) % 2 == 0
-    na = (ctypes.c_double * len(NA))(*NA)
-    desc = N.DebyeDesc(Nx0, Ny0, Nz0, dx, dy, dz, float(lam), float(n0),
-                       ctypes.cast(na, ctypes.POINTER(ctypes.c_double)), len(NA),
-                       int(n_integration_steps), float(ex0), float(ey0))
+    desc, _na = _desc(shape, units, lam, NA, n0, n_integration_steps, ex0, ey0)
     L = N.lib()
-    wsb = int(L.debye_workspace_bytes(ctypes.byref(desc)))
-    if wsb == 0:
-        rc = L.debye_focus_field(ctypes.byref(desc), None, None, None, None, None, 0, None)
-        N.check(rc, "debye_focus_field")
+    ws, wsb = _workspace(L.debye_workspace_bytes,
+                         lambda: L.debye_focus_field(ctypes.byref(desc), None, None, None, None, None, 0, None),
+                         desc, "debye_focus_field")
     dev = _device()
-    ws = torch.empty(wsb, dtype=torch.uint8, device=dev)
     u = torch.empty((Nz0, Ny0, Nx0), dtype=torch.float32, device=dev) if want_u else None
     ex = ey = ez = None
     if want_field:
@@ -57,6 +70,90 @@ def focus_field_debye(shape, units, lam, NA, n0=1., n_integration_steps=200, dev
     if device:
         return u, ex, ey, ez
     return _d2h(u), _d2h(ex), _d2h(ey), _d2h(ez)
+
+
+def focus_field_debye_gauss(shape, units, lam, NAs, sig=1. / np.sqrt(2), n_integration_steps=200, device=False):
+    """Detection PSF of a pupil under a Gaussian envelope exp(-r^2/2/sig^2), r = 1 at the
+    aperture edge (bpm/psf/_focus_fields_debye.py:361). NAs is an increasing even-length
+    list of annulus limits (no n0: the angles are arcsin(NAs)). Returns u, ex, ey, ez on
+    (Nz, Ny, Nx); any shape >= 3 per axis."""
+    assert sig > 0
+    NAs = list(np.asarray(NAs, np.float64).ravel())
+    shape = tuple(int(s) for s in shape)
+    desc, _na = _desc(shape, units, lam, NAs, 1., n_integration_steps)
+    L = N.lib()
+    ws, wsb = _workspace(L.debye_gauss_workspace_bytes,
+                         lambda: L.debye_focus_field_gauss(ctypes.byref(desc), float(sig), None, None, None, None,
+                                                           None, 0, None),
+                         desc, "debye_focus_field_gauss")
+    dev = _device()
+    Nx0, Ny0, Nz0 = shape
+    u = torch.empty((Nz0, Ny0, Nx0), dtype=torch.float32, device=dev)
+    ex = torch.empty((Nz0, Ny0, Nx0), dtype=torch.complex64, device=dev)
+    ey = torch.empty_like(ex)
+    ez = torch.empty_like(ex)
+    N.check(L.debye_focus_field_gauss(ctypes.byref(desc), float(sig), _ptr(u), _ptr(ex), _ptr(ey), _ptr(ez),
+                                      _ptr(ws), wsb, _stream_ptr()), "debye_focus_field_gauss")
+    if device:
+        return u, ex, ey, ez
+    return _d2h(u), _d2h(ex), _d2h(ey), _d2h(ez)
+
+
+def focus_field_debye_plane(shape=(128, 128), units=(.1, .1), z=0., lam=.5, NA=.6, n0=1., ex_g=None,
+                            n_integration_steps=200, device=False):
+    """x component of the focus field on the plane at height z (bpm/psf/_focus_fields_debye.py:149),
+    on (Ny, Nx) for shape = (Nx, Ny), x spanning [-(Nx//2)*dx, (Nx - Nx//2)*dx]. If ex_g (a
+    CUDA complex64 tensor of shape (Ny, Nx)) is given it is filled and None is returned."""
+    Nx, Ny = (int(s) for s in shape)
+    dx, dy = units
+    use_buffer = ex_g is not None
+    if use_buffer:
+        assert tuple(ex_g.shape)[::-1] == (Nx, Ny)
+        if not (isinstance(ex_g, torch.Tensor) and ex_g.is_cuda and ex_g.dtype == torch.complex64
+                and ex_g.is_contiguous()):
+            raise TypeError("ex_g must be a contiguous complex64 CUDA tensor")
+    desc, _na = _desc((Nx, Ny, 1), (dx, dy, 0.), lam, NA, n0, n_integration_steps)
+    L = N.lib()
+    ws, wsb = _workspace(L.debye_points_workspace_bytes,
+                         lambda: L.debye_focus_field_plane(ctypes.byref(desc), float(z), None, None, 0, None),
+                         desc, "debye_focus_field_plane")
+    ex = ex_g if use_buffer else torch.empty((Ny, Nx), dtype=torch.complex64, device=_device())
+    N.check(L.debye_focus_field_plane(ctypes.byref(desc), float(z), _ptr(ex), _ptr(ws), wsb, _stream_ptr()),
+            "debye_focus_field_plane")
+    if use_buffer:
+        return None
+    return ex if device else _d2h(ex)
+
+
+def focus_field_debye_at(x, y, z, lam, NA, n0=1., n_integration_steps=200, device=False):
+    """focus_field_debye at the points (x, y, z) (arrays of one shape; numpy or CUDA
+    tensors) instead of a grid (bpm/psf/_focus_fields_debye.py:315). Returns u, ex, ey, ez
+    of that shape, u being |ex|^2 as the reference kernel writes it."""
+    dev = _device()
+
+    def flat(a):
+        t = a if isinstance(a, torch.Tensor) else torch.from_numpy(np.ascontiguousarray(np.asarray(a, np.float32)))
+        return t.to(device=dev, dtype=torch.float32).reshape(-1).contiguous()
+    shp = tuple(x.shape)
+    assert shp == tuple(y.shape) == tuple(z.shape)
+    xs, ys, zs = flat(x), flat(y), flat(z)
+    n = xs.numel()
+    desc, _na = _desc((0, 0, 0), (0., 0., 0.), lam, NA, n0, n_integration_steps)
+    L = N.lib()
+    ws, wsb = _workspace(L.debye_points_workspace_bytes,
+                         lambda: L.debye_focus_field_at(ctypes.byref(desc), None, None, None, 0, None, None, None,
+                                                        None, None, 0, None),
+                         desc, "debye_focus_field_at")
+    u = torch.empty(n, dtype=torch.float32, device=dev)
+    ex = torch.empty(n, dtype=torch.complex64, device=dev)
+    ey = torch.empty_like(ex)
+    ez = torch.empty_like(ex)
+    N.check(L.debye_focus_field_at(ctypes.byref(desc), _ptr(xs), _ptr(ys), _ptr(zs), n, _ptr(u), _ptr(ex), _ptr(ey),
+                                   _ptr(ez), _ptr(ws), wsb, _stream_ptr()), "debye_focus_field_at")
+    res = tuple(a.reshape(shp) for a in (u, ex, ey, ez))
+    if device:
+        return res
+    return tuple(_d2h(a) for a in res)
 
 
 def psf(shape, units, lam, NA, n0=1., n_integration_steps=200, return_field=False, device=False):

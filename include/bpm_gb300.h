@@ -216,6 +216,19 @@ int bpm_backward(bpm_plan* plan, const bpm_request* req, const void* grad_last, 
                  void* grad_u0, void* workspace, size_t workspace_bytes, void* stream);
 
 /* ---------------------------------------------------------------------------------- */
+/* Coated-sphere refractive-index volumes                                              */
+/* ---------------------------------------------------------------------------------- */
+
+/* Fill dn (nz, ny, nx) float32 on the device with coated spheres: a voxel at
+ * (dx*i, dy*j, dz*k) whose nearest centre lies within rad_inner gets dn_inner, within
+ * rad_outer dn_outer, else 0. points: device (np, 3) float32 centres (x, y, z) in microns,
+ * sorted by ascending z. Replaces bpm/bpm/bpm_3d_spheres.py:create_dn_buffer (:11-38) and
+ * its kernel bpm/bpm/kernels/bpm_3d_spheres.cl:fill_dn (:31-74); bit-identical volume. */
+int bpm_spheres_fill(int nx, int ny, int nz, double dx, double dy, double dz, const float* points, int np,
+                     double dn_inner, double rad_inner, double dn_outer, double rad_outer, float* dn,
+                     void* stream);
+
+/* ---------------------------------------------------------------------------------- */
 /* Vectorial Debye-Wolf focus field                                                    */
 /* ---------------------------------------------------------------------------------- */
 
@@ -240,6 +253,37 @@ size_t debye_workspace_bytes(const debye_desc* desc);
  * u: float32 |E|^2 (may be NULL); ex, ey, ez: complex64 (each may be NULL). */
 int debye_focus_field(const debye_desc* desc, float* u, void* ex, void* ey, void* ez,
                       void* workspace, size_t workspace_bytes, void* stream);
+
+/* Bytes of scratch debye_focus_field_gauss needs (256-aligned); 0 for an invalid desc. */
+size_t debye_gauss_workspace_bytes(const debye_desc* desc);
+
+/* Focus field of a Gaussian-illuminated pupil, amplitude exp(-t^2/(2 alpha_max^2 sig^2)).
+ * Replaces bpm/psf/_focus_fields_debye.py:focus_field_debye_gauss (:361-441) with the
+ * kernel bpm/psf/kernels/psf_debye.cl:debye_wolf_gauss (:273-362), including its octant of
+ * (N0+1)/2 samples per axis on [0, d*N] and its spreading without conjugation (:426-438).
+ * Any shape >= 3 per axis. The reference's function has no n0 argument: pass n0 = 1 for
+ * its behaviour (alphas = asin(na), wavelength lam). sig > 0. Outputs as debye_focus_field. */
+int debye_focus_field_gauss(const debye_desc* desc, double sig, float* u, void* ex, void* ey,
+                            void* ez, void* workspace, size_t workspace_bytes, void* stream);
+
+/* Bytes of scratch debye_focus_field_plane / debye_focus_field_at need (256-aligned). */
+size_t debye_points_workspace_bytes(const debye_desc* desc);
+
+/* Ex on one plane at height z: (ny, nx) complex64 over x in [-(nx/2) dx, (nx - nx/2) dx]
+ * (likewise y). Replaces bpm/psf/_focus_fields_debye.py:focus_field_debye_plane
+ * (:149-214) with bpm/psf/kernels/psf_debye.cl:debye_wolf_plane (:117-183). nz and dz are
+ * not used; nx, ny >= 2. */
+int debye_focus_field_plane(const debye_desc* desc, double z, void* ex, void* workspace,
+                            size_t workspace_bytes, void* stream);
+
+/* Fields at n arbitrary points (device float32 arrays x, y, z, microns). u receives
+ * |ex|^2, as the reference kernel writes it (psf_debye.cl:267); u, ex, ey, ez (complex64)
+ * may each be NULL. Replaces bpm/psf/_focus_fields_debye.py:focus_field_debye_at
+ * (:315-358) with bpm/psf/kernels/psf_debye.cl:debye_wolf_at (:187-269). Only the optical
+ * fields of desc (lam, n0, na, n_integration_steps, ex0, ey0) are used. */
+int debye_focus_field_at(const debye_desc* desc, const float* x, const float* y, const float* z,
+                         long long n, float* u, void* ex, void* ey, void* ez, void* workspace,
+                         size_t workspace_bytes, void* stream);
 
 #ifdef __cplusplus
 }

@@ -58,12 +58,29 @@ static inline float shim_half_to_float(uint16_t h) {
 }
 static inline float vload_half(size_t off, const half* p) { return shim_half_to_float(p[off]); }
 
-/* image / vector types used only by kernels the oracle never calls */
+/* vector types: float4 arithmetic as OpenCL defines it for the kernels the oracle runs
+ * (bpm_3d_spheres.cl:fill_dn uses r - r2 and length()); the OpenCL vector literal
+ * (float4)(a, b, c, d) is rewritten to make_float4(a, b, c, d) by the build recipe. The
+ * scalar-broadcast constructor serves image kernels the oracle never calls. */
 struct float2 { float x, y; float2() : x(0), y(0) {} };
 struct float4 {
   float x, y, z, w; float2 xy;
+  float4() : x(0), y(0), z(0), w(0) {}
   template <typename T> float4(T) : x(0), y(0), z(0), w(0) {}
 };
+static inline float4 make_float4(float a, float b, float c, float d) {
+  float4 r; r.x = a; r.y = b; r.z = c; r.w = d; return r;
+}
+static inline float4 operator-(const float4& a, const float4& b) {
+  return make_float4(a.x - b.x, a.y - b.y, a.z - b.z, a.w - b.w);
+}
+static inline float length(const float4& a) {
+  float s = a.x * a.x;
+  s = s + a.y * a.y;
+  s = s + a.z * a.z;
+  s = s + a.w * a.w;
+  return std::sqrt(s);
+}
 typedef int sampler_t;
 struct image3d_t { int unused; };
 #define CLK_NORMALIZED_COORDS_FALSE 0

@@ -35,6 +35,9 @@ def load():
     F = ctypes.c_float
     I = ctypes.c_int
     lib.ref_debye_wolf.argtypes = [P, P, P, P, F, F, F, F, F, F, F, F, F, P, I, I, I, I, I]
+    lib.ref_debye_wolf_plane.argtypes = [P, F, F, F, F, F, F, F, F, P, I, I, I, I]
+    lib.ref_debye_wolf_at.argtypes = [P, P, P, P, P, P, P, F, F, F, P, I, ctypes.c_long, I]
+    lib.ref_debye_wolf_gauss.argtypes = [P, P, P, P, F, F, F, F, F, F, F, F, F, F, P, I, I, I, I, I]
     lib.ref_bessel_jn.argtypes = [I, P, P, ctypes.c_long]
     lib.ref_compute_propagator.argtypes = [P, F, F, F, F, F, I, I]
     lib.ref_mult_propagator.argtypes = [P, F, F, F, F, F, I, I]
@@ -49,6 +52,7 @@ def load():
     lib.ref_mult_dn_mean_buff.argtypes = [P, P, P, P, F, I, I, I, I]
     lib.ref_mult_dn_mean_half_buff.argtypes = [P, P, P, P, F, I, I, I, I]
     lib.ref_copy_intens.argtypes = [P, P, I, I]
+    lib.ref_fill_dn.argtypes = [P, P, I, F, F, F, F, F, F, F, I, I, I]
     _lib = lib
     return lib
 

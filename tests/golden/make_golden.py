@@ -12,6 +12,9 @@ Golden outputs come from the reference's OpenCL kernel sources compiled as host 
     bpm/bpmclass/_bpm3d_ocl.py:_propagate_single (:100-126), each elementwise kernel the
     reference's own, with a single-precision scipy FFT standing in for the third-party
     gputools FFT (forward unnormalised, inverse 1/(Nx*Ny)).
+  * Debye-Wolf variants: debye_wolf_gauss / _plane / _at (psf_debye.cl:273-362, :117-183,
+    :187-269) with the launch arguments of _focus_fields_debye.py:404-412, :201-209, :346-352.
+  * Coated spheres: fill_dn (bpm/bpm/kernels/bpm_3d_spheres.cl:31-74) on z-sorted centres.
   * Masks: compute_propagator's evanescent mask and the mult_dn taper, straight from the
     kernels, for bit-exact comparisons.
 Inputs are seeded and stored next to the outputs, so the fixtures are self-contained.
@@ -218,6 +221,67 @@ def main():
         out[name + "_ez"] = ez
         out[name + "_args"] = np.array(list(shape) + list(units) + [lam, n0, steps], np.float64)
         out[name + "_NA"] = np.atleast_1d(np.array(NA, np.float64))
+
+    # --- coated spheres (bpm_3d_spheres.cl:fill_dn) --------------------------------------
+    for name, size, units, n, radii in [("spheres_a", (48, 40, 36), (.1, .12, .15), 15, (.03, .3, .06, .7)),
+                                        ("spheres_b", (32, 32, 24), (.1, .1, .1), 40, (0., 0., .05, .45))]:
+        Nx, Ny, Nz = size
+        pts = rng.uniform(-.2, 1.2, (n, 3)) * np.array([Nx * units[0], Ny * units[1], Nz * units[2]])
+        pts[5:8, 2] = pts[4, 2]                                  # equal z values
+        ps = pts[np.argsort(pts[:, 2], kind="stable")].astype(np.float32)
+        dn = np.zeros((Nz, Ny, Nx), np.float32)
+        lib.ref_fill_dn(ptr(dn), ptr(np.ascontiguousarray(ps.ravel())), n, f32(units[0]), f32(units[1]),
+                        f32(units[2]), f32(radii[0]), f32(radii[1]), f32(radii[2]), f32(radii[3]), Nx, Ny, Nz)
+        out[name + "_out"] = dn
+        out[name + "_pts"] = pts
+        out[name + "_args"] = np.array(list(size) + list(units) + list(radii), np.float64)
+
+    # --- Debye-Wolf variants (psf_debye.cl: debye_wolf_gauss / _plane / _at) -------------
+    for name, shape, units, lam, NAs, sig, steps in [
+            ("gauss_a", (16, 14, 10), (.1, .12, .15), .5, [0., .8], .7, 60),
+            ("gauss_b", (15, 17, 9), (.1, .1, .1), .6, [.2, .4, .6, .9], 1.2, 41)]:
+        Nx0, Ny0, Nz0 = shape
+        Nx, Ny, Nz = (Nx0 + 1) // 2, (Ny0 + 1) // 2, (Nz0 + 1) // 2
+        al = np.arcsin(np.array(NAs)).astype(np.float32)
+        u = np.zeros((Nz, Ny, Nx), np.float32)
+        ex = np.zeros((Nz, Ny, Nx), np.complex64)
+        ey = np.zeros_like(ex)
+        ez = np.zeros_like(ex)
+        lib.ref_debye_wolf_gauss(ptr(ex), ptr(ey), ptr(ez), ptr(u), f32(1.), f32(0.), f32(0.),
+                                 f32(units[0] * Nx), f32(0.), f32(units[1] * Ny), f32(0.), f32(units[2] * Nz),
+                                 f32(lam), f32(sig), ptr(al), len(al), Nx, Ny, Nz, steps)
+        for k, v in zip(("u", "ex", "ey", "ez"), debye_ref.mirror_octant_gauss(shape, u, ex, ey, ez)):
+            out["%s_%s" % (name, k)] = v
+        out[name + "_args"] = np.array(list(shape) + list(units) + [lam, sig, steps], np.float64)
+        out[name + "_NA"] = np.array(NAs, np.float64)
+    for name, shape, units, z, lam, NA, n0, steps in [("plane_a", (32, 24), (.1, .1), 0., .5, .8, 1., 80),
+                                                      ("plane_b", (31, 20), (.07, .1), 1.3, .5, 1.1, 1.33, 100)]:
+        Nx, Ny = shape
+        dx, dy = units
+        al = np.arcsin(np.array([0., NA]) / n0).astype(np.float32)
+        ex = np.zeros((Ny, Nx), np.complex64)
+        lib.ref_debye_wolf_plane(ptr(ex), f32(1.), f32(0.), f32(-(Nx // 2) * dx), f32((Nx - Nx // 2) * dx),
+                                 f32(-(Ny // 2) * dy), f32((Ny - Ny // 2) * dy), f32(z), f32(lam / n0), ptr(al),
+                                 len(al), Nx, Ny, steps)
+        out[name + "_ex"] = ex
+        out[name + "_args"] = np.array([Nx, Ny, dx, dy, z, lam, NA, n0, steps], np.float64)
+    pts = rng.uniform(-2, 2, (3, 7, 9)).astype(np.float32)
+    pts[2] *= 1.5
+    pts[:, 0, 0] = 0.                                             # the optical axis at the focus
+    al = np.arcsin(np.array([.1, .5, .7, 1.0]) / 1.33).astype(np.float32)
+    n = pts[0].size
+    u = np.zeros(n, np.float32)
+    ex = np.zeros(n, np.complex64)
+    ey = np.zeros_like(ex)
+    ez = np.zeros_like(ex)
+    lib.ref_debye_wolf_at(ptr(np.ascontiguousarray(pts[0].ravel())), ptr(np.ascontiguousarray(pts[1].ravel())),
+                          ptr(np.ascontiguousarray(pts[2].ravel())), ptr(ex), ptr(ey), ptr(ez), ptr(u), f32(1.),
+                          f32(0.), f32(.5 / 1.33), ptr(al), len(al), n, 120)
+    for k, v in zip(("u", "ex", "ey", "ez"), (u, ex, ey, ez)):
+        out["at_a_" + k] = v.reshape(pts[0].shape)
+    out["at_a_pts"] = pts
+    out["at_a_args"] = np.array([.5, 1.33, 120], np.float64)
+    out["at_a_NA"] = np.array([.1, .5, .7, 1.0], np.float64)
 
     xs = np.linspace(0, 30, 301).astype(np.float32)
     for n in (0, 1, 2):

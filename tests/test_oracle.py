@@ -97,3 +97,71 @@ def test_reflib_optional():
     if lib is None:
         pytest.skip("oracle/_ref/libref_cl.so not built here")
     assert hasattr(lib, "ref_debye_wolf")
+
+
+@pytest.mark.parametrize("name", ["spheres_a", "spheres_b"])
+def test_spheres_oracle_bit_exact(golden, name):
+    """bpm_3d_spheres.cl:fill_dn (reference kernel) against the numpy restatement."""
+    from oracle import spheres_ref
+    a = golden[name + "_args"]
+    size = tuple(int(v) for v in a[:3])
+    r = a[6:10]
+    dn = spheres_ref.create_dn_buffer(size, tuple(a[3:6]), golden[name + "_pts"], r[0], r[1], r[2], r[3])
+    assert np.array_equal(dn, golden[name + "_out"])
+
+
+@pytest.mark.parametrize("name", ["gauss_a", "gauss_b"])
+def test_debye_gauss_oracle_vs_reference_kernel(golden, name):
+    """debye_wolf_gauss (reference kernel) + the gauss spreading loop against the restatement;
+    gauss_b has odd shapes and two annuli."""
+    a = golden[name + "_args"]
+    shape = tuple(int(v) for v in a[:3])
+    o = debye_ref.focus_field_debye_gauss(shape, tuple(a[3:6]), a[6], list(golden[name + "_NA"]), a[7], int(a[8]))
+    for v, k in zip(o, ("u", "ex", "ey", "ez")):
+        assert v.shape == shape[::-1]
+        assert rel_l2(v, golden["%s_%s" % (name, k)]) < 5e-6, k
+
+
+@pytest.mark.parametrize("name", ["plane_a", "plane_b"])
+def test_debye_plane_oracle_vs_reference_kernel(golden, name):
+    Nx, Ny, dx, dy, z, lam, NA, n0, steps = golden[name + "_args"]
+    o = debye_ref.focus_field_debye_plane((int(Nx), int(Ny)), (dx, dy), z, lam, NA, n0, int(steps))
+    assert o.shape == (int(Ny), int(Nx))
+    assert rel_l2(o, golden[name + "_ex"]) < 5e-6
+
+
+def test_debye_at_oracle_vs_reference_kernel(golden):
+    p = golden["at_a_pts"]
+    lam, n0, steps = golden["at_a_args"]
+    o = debye_ref.focus_field_debye_at(p[0], p[1], p[2], lam, list(golden["at_a_NA"]), n0, int(steps))
+    for v, k in zip(o, ("u", "ex", "ey", "ez")):
+        assert rel_l2(v, golden["at_a_" + k]) < 5e-6, k
+
+
+def test_sine_rule_end_weights():
+    """psf_debye.cl:155: the half weight follows the float32 test t == a2, so node
+    INT_STEPS-1 gets it only when a1 + (INT_STEPS-1)*dt rounds exactly onto a2."""
+    hits = []
+    for NA in (.3, .5, .8, 1.0):
+        a = np.arcsin(np.array([0., NA])).astype(np.float32)
+        t, w = debye_ref.quadrature_nodes_f32_ends(a, 200)
+        dt = w[1]
+        assert w[0] == .5 * dt and w[-1] == dt
+        f = np.float32
+        t32 = f(a[0]) + f(199) * ((a[1] - a[0]) / f(199.))
+        hits.append(w[-2] == .5 * dt)
+        assert hits[-1] == (t32 == a[1])
+    assert any(hits) and not all(hits)
+
+
+@pytest.mark.parametrize("N0", [5, 6, 9, 16])
+def test_gauss_mirror_index_form_equals_slice_loop(N0):
+    rng = np.random.default_rng(N0)
+    shape = (N0, N0 + 1, 3)
+    No = [(s + 1) // 2 for s in shape]
+    u = rng.normal(size=(No[2], No[1], No[0])).astype(np.float32)
+    e = (rng.normal(size=u.shape) + 1j * rng.normal(size=u.shape)).astype(np.complex64)
+    U, E, _, _ = debye_ref.mirror_octant_gauss(shape, u, e, e, e)
+    ix, iy, iz = (debye_ref.mirror_index_gauss(s) for s in shape)
+    assert np.array_equal(U, u[iz][:, iy][:, :, ix])
+    assert np.array_equal(E, e[iz][:, iy][:, :, ix])

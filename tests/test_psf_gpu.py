@@ -77,3 +77,89 @@ def test_psf_errors(bpm):
         bpm.psf((16, 16, 15), (.1, .1, .1), .5, .8)
     with pytest.raises(AssertionError):
         bpm.psf((16, 16, 16), (.1, .1, .1), .5, [.1, .2, .3])
+
+
+# --- variants: Gaussian pupil, single plane, arbitrary points ---------------------------
+
+@pytest.mark.parametrize("name", ["gauss_a", "gauss_b"])
+def test_gauss_golden_reference_kernel(bpm, golden, name):
+    a = golden[name + "_args"]
+    shape = tuple(int(v) for v in a[:3])
+    res = bpm.focus_field_debye_gauss(shape, tuple(a[3:6]), a[6], list(golden[name + "_NA"]), a[7], int(a[8]))
+    for v, k in zip(res, ("u", "ex", "ey", "ez")):
+        assert v.shape == shape[::-1]
+        assert rel_l2(v, golden["%s_%s" % (name, k)]) < TOL, k
+
+
+@pytest.mark.parametrize("shape,units,lam,NAs,sig,steps", [
+    ((64, 48, 33), (.1, .1, .1), .5, [0., .9], 1. / np.sqrt(2), 200),
+    ((101, 64, 40), (.08, .1, .15), .488, [.3, .5, .7, .95], .5, 128),
+])
+def test_gauss_oracle_parity(bpm, shape, units, lam, NAs, sig, steps):
+    res = bpm.focus_field_debye_gauss(shape, units, lam, NAs, sig, steps)
+    o = debye_ref.focus_field_debye_gauss(shape, units, lam, NAs, sig, steps)
+    for v, b, k in zip(res, o, ("u", "ex", "ey", "ez")):
+        assert rel_l2(v, b) < TOL, k
+
+
+@pytest.mark.parametrize("name", ["plane_a", "plane_b"])
+def test_plane_golden_reference_kernel(bpm, golden, name):
+    Nx, Ny, dx, dy, z, lam, NA, n0, steps = golden[name + "_args"]
+    ex = bpm.focus_field_debye_plane((int(Nx), int(Ny)), (dx, dy), z, lam, NA, n0, n_integration_steps=int(steps))
+    assert ex.shape == (int(Ny), int(Nx)) and ex.dtype == np.complex64
+    assert rel_l2(ex, golden[name + "_ex"]) < TOL
+
+
+@pytest.mark.parametrize("shape,z,NA,n0", [((256, 256), 0., 1.1, 1.33), ((200, 120), 3.7, .8, 1.),
+                                           ((64, 64), -2.5, [.2, .4, .6, .8], 1.)])
+def test_plane_oracle_parity(bpm, shape, z, NA, n0):
+    ex = bpm.focus_field_debye_plane(shape, (.1, .1), z, .5, NA, n0, n_integration_steps=150)
+    o = debye_ref.focus_field_debye_plane(shape, (.1, .1), z, .5, NA, n0, 150)
+    assert rel_l2(ex, o) < TOL
+
+
+def test_plane_fills_buffer(bpm):
+    import torch
+    buf = torch.zeros((24, 32), dtype=torch.complex64, device="cuda")
+    assert bpm.focus_field_debye_plane((32, 24), (.1, .1), 1., .5, .8, ex_g=buf) is None
+    ref = bpm.focus_field_debye_plane((32, 24), (.1, .1), 1., .5, .8)
+    assert np.array_equal(buf.cpu().numpy(), ref)
+
+
+def test_at_golden_reference_kernel(bpm, golden):
+    p = golden["at_a_pts"]
+    lam, n0, steps = golden["at_a_args"]
+    res = bpm.focus_field_debye_at(p[0], p[1], p[2], lam, list(golden["at_a_NA"]), n0, int(steps))
+    for v, k in zip(res, ("u", "ex", "ey", "ez")):
+        assert v.shape == p[0].shape
+        assert rel_l2(v, golden["at_a_" + k]) < TOL, k
+
+
+def test_at_oracle_parity_and_grid_consistency(bpm):
+    """Random points, including far from focus (large kz cos t phases), against the FP64
+    oracle; and the grid samples of focus_field_debye re-evaluated as free points."""
+    import torch
+    rng = np.random.default_rng(7)
+    x, y = rng.uniform(-3, 3, (2, 4000)).astype(np.float32)
+    z = rng.uniform(-40, 40, 4000).astype(np.float32)
+    res = bpm.focus_field_debye_at(x, y, z, .5, 1.1, 1.33, 200)
+    o = debye_ref.focus_field_debye_at(x, y, z, .5, 1.1, 1.33, 200)
+    for v, b, k in zip(res, o, ("u", "ex", "ey", "ez")):
+        assert rel_l2(v, b) < TOL, k
+    # torch inputs on the device, device outputs
+    t = [torch.from_numpy(a).cuda() for a in (x, y, z)]
+    res_d = bpm.focus_field_debye_at(*t, .5, 1.1, 1.33, 200, device=True)
+    assert res_d[1].is_cuda and np.array_equal(res_d[1].cpu().numpy(), res[1])
+
+
+def test_variant_errors(bpm):
+    with pytest.raises(NotImplementedError):
+        bpm.focus_field_debye_gauss((2, 16, 16), (.1, .1, .1), .5, [0., .8])
+    with pytest.raises(AssertionError):
+        bpm.focus_field_debye_gauss((16, 16, 16), (.1, .1, .1), .5, [0., .8], sig=0.)
+    with pytest.raises(NotImplementedError):
+        bpm.focus_field_debye_plane((1, 16), (.1, .1), 0., .5, .8)
+    with pytest.raises(AssertionError):
+        bpm.focus_field_debye_at(np.zeros(3), np.zeros(3), np.zeros(4), .5, .8)
+    u, ex, ey, ez = bpm.focus_field_debye_at(np.zeros(0), np.zeros(0), np.zeros(0), .5, .8)
+    assert u.shape == (0,)
