@@ -258,15 +258,25 @@ def bench_ours(args, rank, world, local_rank):
     out_h = torch.empty((BATCH, NZ, NY, NX), dtype=torch.float32, pin_memory=True)
     del march
     torch.cuda.empty_cache()
-    e2e_steps = max(1, min(args.steps, 3))
+    # each step is one public-API call: H2D of u0 and dn from pinned memory, the march, and
+    # the D2H of the |u|^2 volume into pinned memory (the call returns once it has landed)
+    e2e_steps = max(3, min(args.steps, 8))
     for _ in range(1):
         bpm_gb300.bpm_3d_batched((NX, NY, NZ), UNITS, lam=LAM, u0=u0_h, dn=dn_h, n0=N0, return_field=False,
                                  mean_mode=MODE, group=grp, out=out_h)
     barrier()
+    step_ms, step_gpu_ms = [], []
     t0 = time.perf_counter()
     for _ in range(e2e_steps):
+        ts = time.perf_counter()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record()
         bpm_gb300.bpm_3d_batched((NX, NY, NZ), UNITS, lam=LAM, u0=u0_h, dn=dn_h, n0=N0, return_field=False,
                                  mean_mode=MODE, group=grp, out=out_h)
+        e1.record()
+        step_ms.append((time.perf_counter() - ts) * 1e3)
+        e1.synchronize()
+        step_gpu_ms.append(e0.elapsed_time(e1))
     barrier()
     t_e2e = (time.perf_counter() - t0) / e2e_steps
     if world > 1:
@@ -276,6 +286,8 @@ def bench_ours(args, rank, world, local_rank):
     e2e = {"value": world * units_per_step / t_e2e, "unit": "voxel-updates/s",
            "h2d_bytes_per_step": int(u0_h.numel() * 8 + dn_h.numel() * 4),
            "d2h_bytes_per_step": int(out_h.numel() * 4), "ms_per_step": t_e2e * 1e3,
+           "steps": e2e_steps, "step_ms": [round(v, 2) for v in step_ms],
+           "step_gpu_ms": [round(v, 2) for v in step_gpu_ms],
            "api": "bpm_gb300.bpm_3d_batched (pinned host u0/dn/out)"}
 
     res = {

@@ -70,6 +70,7 @@ SIGNATURES = {
     "bpm_propagate": (c_int, [c_vp, ctypes.POINTER(Request), c_vp, c_size, c_vp]),
     "bpm_mask_precompute": (c_int, [c_vp, c_vp, c_int, c_vp, c_vp]),
     "bpm_propagate_noalloc": (c_int, [c_vp, ctypes.POINTER(Request), c_vp]),
+    "bpm_propagate_to_host": (c_int, [c_vp, ctypes.POINTER(Request), c_vp, c_int, c_vp, c_size, c_vp]),
     "bpm_launch_pass": (c_int, [c_vp, ctypes.POINTER(Request), c_vp, c_size, c_int, c_int, c_vp]),
     "bpm_backward_workspace_bytes": (c_size, [c_vp, c_int, c_int, c_int]),
     "bpm_backward": (c_int, [c_vp, ctypes.POINTER(Request), c_vp, c_vp, c_vp, c_vp, c_size, c_vp]),
@@ -78,6 +79,7 @@ SIGNATURES = {
     "bpm_exec_destroy": (c_int, [c_vp]),
     "bpm_spheres_fill": (c_int, [c_int, c_int, c_int, c_double, c_double, c_double, c_vp, c_int,
                                  c_double, c_double, c_double, c_double, c_vp, c_vp]),
+    "bpm_host_ptr_mapped": (c_int, [c_vp]),
     "debye_workspace_bytes": (c_size, [ctypes.POINTER(DebyeDesc)]),
     "debye_focus_field": (c_int, [ctypes.POINTER(DebyeDesc), c_vp, c_vp, c_vp, c_vp, c_vp, c_size, c_vp]),
     "debye_gauss_workspace_bytes": (c_size, [ctypes.POINTER(DebyeDesc)]),

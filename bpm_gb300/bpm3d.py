@@ -405,7 +405,10 @@ def bpm_3d_batched(size, units, lam=.5, u0=None, dn=None, n0=1., return_full=Tru
         vdt = torch.complex64 if return_field else torch.float32
         if tuple(host.shape) != (B, Nz, Ny, Nx) or host.dtype != vdt:
             raise ValueError("out must have shape %s and dtype %s" % ((B, Nz, Ny, Nx), vdt))
-        _run_to_host(plan, u0_t, dn_t, kind, bstride, out_kind, tabs, group, mask, host)
+        if host.is_contiguous() and host.is_pinned():
+            _run_streamed_to_host(plan, u0_t, dn_t, kind, bstride, out_kind, tabs, group, mask, host)
+        else:
+            _run_to_host(plan, u0_t, dn_t, kind, bstride, out_kind, tabs, group, mask, host)
         return out
     vol, last, _, _ = _run(plan, u0_t, dn_t, kind, bstride, out_kind, True, slice_tabs=tabs, group=group,
                            mask=mask)
@@ -418,6 +421,26 @@ def bpm_3d_batched(size, units, lam=.5, u0=None, dn=None, n0=1., return_full=Tru
         torch.cuda.current_stream().synchronize()
         return out
     return res if as_tensor else _d2h(res)
+
+
+def _run_streamed_to_host(plan, u0_t, dn_t, kind, bstride, out_kind, tabs, group, mask, host, chunk_planes=16):
+    """March the whole batch into a device volume while the library's copy stream moves
+    each finished run of `chunk_planes` planes into the page-locked host buffer
+    (bpm_propagate_to_host), so the device->host copy runs alongside the march."""
+    Nx, Ny, Nz = plan.size
+    B = u0_t.shape[0]
+    dev = u0_t.device
+    vdt = torch.complex64 if out_kind == N.OUT_FIELD else torch.float32
+    vol = torch.empty((B, Nz, Ny, Nx), dtype=vdt, device=dev)
+    last = torch.empty((B, Ny, Nx), dtype=torch.complex64, device=dev)
+    wsb = plan.workspace_bytes(B, group)
+    ws = torch.empty(wsb, dtype=torch.uint8, device=dev)
+    req = N.Request(B, _ptr(u0_t), _ptr(dn_t), kind, int(bstride), _ptr(tabs[0]), _ptr(tabs[1]), _ptr(vol),
+                    out_kind, Nz * Ny * Nx, _ptr(last), None, None, 0, int(group), None, 0, _ptr(mask))
+    N.check(N.lib().bpm_propagate_to_host(plan.handle, ctypes.byref(req), ctypes.c_void_p(host.data_ptr()),
+                                          int(chunk_planes), _ptr(ws), wsb, _stream_ptr()),
+            "bpm_propagate_to_host")
+    torch.cuda.current_stream().synchronize()
 
 
 def _run_to_host(plan, u0_t, dn_t, kind, bstride, out_kind, tabs, group, mask, host):

@@ -46,6 +46,7 @@ struct bpm_plan {
   float* kx2;       // (2.f*M_PI*FFTFREQ(i,nx,dx))^2, FP32 recipe
   float* ky2;
   float2* H;        // unnormalised propagator table (IGNORE mean mode), (ny, nx)
+  float2* Ht;       // the same table transposed, (nx, ny): a column's entries are contiguous
   float* taper;     // taper value per distance < absorbing_width
   float* sw;        // scattering weights cos(theta), (ny, nx)
   float* gw;        // g-factor weights cos(theta)^2
@@ -54,6 +55,11 @@ struct bpm_plan {
   // streams on which groups of fields march concurrently, with their fork/join events
   cudaStream_t aux[4];
   cudaEvent_t ev_fork, ev_join[4];
+  // device->host streaming of the output volume (bpm_propagate_to_host): the copy stream,
+  // one "planes ready" event per march stream, and the final join
+  cudaStream_t copy;
+  cudaEvent_t ev_ready[4], ev_copied;
+  int max_pitch;
 };
 
 // field groups a batch may march at the same time (one workspace slot each)
@@ -112,7 +118,7 @@ float taper_value(int dist, int absorb) {  // bpm_3d_kernels.cl:36
 __global__ void build_tables_kernel(int nx, int ny, double dx, double dy, double dz, double n0,
                                     double k0, float n0f, float k0f, int prop_kind, int fresnel,
                                     const float* __restrict__ kx2, const float* __restrict__ ky2,
-                                    float2* __restrict__ H, float* __restrict__ sw,
+                                    float2* __restrict__ H, float2* __restrict__ Ht, float* __restrict__ sw,
                                     float* __restrict__ gw) {
   int x = blockIdx.x * blockDim.x + threadIdx.x;
   int y = blockIdx.y;
@@ -137,7 +143,9 @@ __global__ void build_tables_kernel(int nx, int ny, double dx, double dy, double
   double ph = -dz * kz;
   double s, c;
   sincos(ph, &s, &c);
-  H[(size_t)y * nx + x] = prop ? make_float2((float)c, (float)s) : make_float2(0.f, 0.f);
+  const float2 hv = prop ? make_float2((float)c, (float)s) : make_float2(0.f, 0.f);
+  H[(size_t)y * nx + x] = hv;
+  Ht[(size_t)x * ny + y] = hv;
   // scattering weights (bpm_3d.py:227-244): cos(theta) = real(H0)/n0/k0 with the FP64 host H0
   double h0 = tmp64 >= 0.0 ? sqrt(tmp64) : 0.0;
   if (fresnel) h0 = n0 * k0 - .5 * (kx * kx + ky * ky) / n0 / k0;
@@ -209,16 +217,17 @@ __device__ __forceinline__ float2 load_dn_pair(const void* dn, int dtype, size_t
 // enters as the separate factor exp(+i k0 dz dn0) (row_rot), so M depends on dn alone and
 // can be computed once per dn volume for a whole batch (bpm_mask_precompute); the on-the-fly
 // and precomputed masks are the same FP32 arithmetic, bit for bit.
-__device__ __forceinline__ float2 mask_value(const void* dn, int dtype, size_t idx, float unit_k, int x, int y,
-                                             int nx, int ny, int absorb, const float* taper) {
+__device__ __forceinline__ float2 mask_from_complex(float2 d, float unit_k) {
   float s, c;
-  if (dtype == BPM_DN_C64) {
-    const float2 d = __ldg(reinterpret_cast<const float2*>(dn) + idx);
-    const float m = expf(unit_k * d.y);
-    sincosf((-unit_k) * d.x, &s, &c);
-    return make_float2(m * c, m * s);
-  }
-  sincosf((-unit_k) * load_dn_real(dn, dtype, idx), &s, &c);
+  const float m = expf(unit_k * d.y);
+  sincosf((-unit_k) * d.x, &s, &c);
+  return make_float2(m * c, m * s);
+}
+
+__device__ __forceinline__ float2 mask_from_real(float dnv, float unit_k, int x, int y, int nx, int ny, int absorb,
+                                                 const float* taper) {
+  float s, c;
+  sincosf((-unit_k) * dnv, &s, &c);
   float2 M = make_float2(c, s);
   const int dist = min(min(nx - 1 - x, x), min(ny - 1 - y, y));
   if (dist < absorb) {
@@ -227,6 +236,12 @@ __device__ __forceinline__ float2 mask_value(const void* dn, int dtype, size_t i
     M.y *= a;
   }
   return M;
+}
+
+__device__ __forceinline__ float2 mask_value(const void* dn, int dtype, size_t idx, float unit_k, int x, int y,
+                                             int nx, int ny, int absorb, const float* taper) {
+  if (dtype == BPM_DN_C64) return mask_from_complex(__ldg(reinterpret_cast<const float2*>(dn) + idx), unit_k);
+  return mask_from_real(load_dn_real(dn, dtype, idx), unit_k, x, y, nx, ny, absorb, taper);
 }
 
 // PRE = 1: the masks come precomputed (p.mask); PRE = 0: formed on the fly from dn. The
@@ -260,7 +275,7 @@ __device__ __forceinline__ float2 row_point(const RowParams& p, float2 v, int x,
     }
     if (p.do_mask) {
       const float2 u = p.seg[gl * p.seg_bstride + (size_t)(p.z - p.seg_z0) * plane + pix];
-      p.grad_dn[(size_t)gl * p.nz * plane + zoff + pix] = p.unit_k * (v.x * u.y - v.y * u.x);
+      p.grad_dn[(size_t)gl * p.nz * plane + zoff + pix] = p.unit_k * fmaf(v.x, u.y, -(v.y * u.x));
       const float2 M = row_mask<PRE>(p, x, y, gl, zoff, pix);
       v = cmul(v, make_float2(M.x, -M.y));
       if (dn0 != 0.f) v = cmul(v, make_float2(rot.x, -rot.y));
@@ -392,6 +407,7 @@ struct ColParams {
   int nx, ny, nz, z;         // z = step index: the field goes from plane z to z+1
   int prop_mode;             // 0 = table H, 1 = FP32 recipe with slice_n[z+1], 2 = weighted
   const float2* H;
+  const float2* Ht;          // H transposed (nx, ny), for the warp column kernels
   const float* kx2;
   const float* ky2;
   float k0f, dzf, n00f;
@@ -411,6 +427,7 @@ struct ColParams {
   int conj_h;                // adjoint: multiply by conj(H)
   const float2* tw;
   const float2* wtw;         // stage-ordered twiddles of the warp FFT
+  int dn_stage;              // weighted: dn rows may be staged with 16-byte cp.async
 };
 
 template <int T>
@@ -475,14 +492,17 @@ __device__ __forceinline__ float2 plain_wave(const ColParams& p) {
 
 // k-space element (kx index x, ky index y) times the propagator, with the scattering partial
 // sums of bpm_3d.py:335-341 and the 1/(nx*ny) inverse-FFT normalisation folded in
+// COLUMN: the caller walks one column (x fixed, y over the lanes) and reads the transposed
+// table; ky2: the ky^2 table, in global or shared memory
+template <bool COLUMN = false>
 __device__ __forceinline__ float2 prop_point(const ColParams& p, float2 v, int x, int y, float nk, float2 plain,
-                                             float& S, float& G) {
+                                             float& S, float& G, const float* ky2) {
   float2 h;
   if (p.prop_mode == 0) {
-    h = __ldg(p.H + (size_t)y * p.nx + x);
+    h = COLUMN ? __ldg(p.Ht + (size_t)x * p.ny + y) : __ldg(p.H + (size_t)y * p.nx + x);
     if (p.conj_h) h.y = -h.y;
   } else {
-    const float tmp = __fsub_rn(__fsub_rn(nk, __ldg(p.kx2 + x)), __ldg(p.ky2 + y));
+    const float tmp = __fsub_rn(__fsub_rn(nk, __ldg(p.kx2 + x)), ky2[y]);
     if (tmp >= 0.f) {
       const float ph = __fmul_rn(-p.dzf, __fsqrt_rn(tmp));
       sincosf(ph, &h.y, &h.x);
@@ -496,8 +516,8 @@ __device__ __forceinline__ float2 prop_point(const ColParams& p, float2 v, int x
     if (x == 0 && y == 0) d = csub(d, plain);
     const float a2 = cabs2(d);
     const size_t k = (size_t)y * p.nx + x;
-    S += __ldg(p.sw + k) * a2;
-    G += __ldg(p.gw + k) * a2;
+    S = fmaf(__ldg(p.sw + k), a2, S);
+    G = fmaf(__ldg(p.gw + k), a2, G);
   }
   return cscale(v, p.scale);
 }
@@ -528,7 +548,7 @@ __device__ __forceinline__ void col_propagate(float2* tile, const ColParams& p, 
   for (int e = threadIdx.x; e < 16 * N; e += T) {
     const int y = e >> 4;
     const int c = e & 15;
-    tile[tile_idx(y, c)] = prop_point(p, tile[tile_idx(y, c)], x0 + c, y, nk, plain, S, G);
+    tile[tile_idx(y, c)] = prop_point(p, tile[tile_idx(y, c)], x0 + c, y, nk, plain, S, G, p.ky2);
   }
   if (p.scat) scat_partials_store<T>(p, S, G, gl, red);
   __syncthreads();
@@ -581,7 +601,7 @@ col_fwd_reduce_kernel(ColParams p) {
     const float2 v = tile[tile_idx(y, c)];
     const float a = __fsqrt_rn(cabs2(v));
     su += a;
-    if (p.dn) sdn += a * load_dn_real(p.dn, p.dn_dtype, gl * p.dn_bstride + (size_t)y * p.nx + x0 + c);
+    if (p.dn) sdn = fmaf(a, load_dn_real(p.dn, p.dn_dtype, gl * p.dn_bstride + (size_t)y * p.nx + x0 + c), sdn);
   }
   block_sum2<T>(sdn, su, red);
   if (threadIdx.x == 0) {
@@ -635,7 +655,13 @@ constexpr int kColWarps = 16;  // columns per block (16 columns = one 128-byte s
 template <int N>
 struct WarpCfg {
   static constexpr size_t ROW_SMEM = ((size_t)N + (size_t)kRowWarps * WarpFft<N>::BUF) * sizeof(float2);
-  static constexpr size_t COL_SMEM = ((size_t)N + (size_t)kColWarps * WarpFft<N>::BUF) * sizeof(float2);
+  static constexpr size_t ROW_SMEM_SHARED = ROW_SMEM + (size_t)N * sizeof(float2);  // + the staged row
+  static constexpr size_t COL_F2 = (size_t)N + (size_t)kColWarps * WarpFft<N>::BUF;  // twiddles, tile/exchange
+  static constexpr size_t COL_SMEM = COL_F2 * sizeof(float2);
+  // the weighted-reduction pass also stages the tile's dn slice-0 values (up to 4 bytes each)
+  static constexpr size_t COL_SMEM_DN = COL_SMEM + (size_t)16 * N * sizeof(float);
+  // the propagating passes also stage the ky^2 table
+  static constexpr size_t COL_SMEM_KY = COL_SMEM + (size_t)N * sizeof(float);
 };
 
 // Row pass, one warp per row: coalesced row load straight into registers, [inverse row
@@ -653,14 +679,15 @@ row_warp_kernel(RowParams p) {
   const int gl = blockIdx.y;
   const int y = blockIdx.x * kRowWarps + warp;
   const size_t plane = (size_t)N * p.ny;
-  if (p.do_inv || p.do_fwd) {
-    for (int k = threadIdx.x; k < WarpFft<N>::TW; k += T) tw[k] = p.wtw[k];
-    __syncthreads();
-  }
+  // the row loads go out first, so their latency overlaps the twiddle table's
   float2 v[E];
   const float2* src = p.src + gl * p.src_bstride + (size_t)y * N;
 #pragma unroll
   for (int m = 0; m < E; m++) v[m] = src[t + 32 * m];
+  if (p.do_inv || p.do_fwd) {
+    for (int k = threadIdx.x; k < WarpFft<N>::TW; k += T) tw[k] = p.wtw[k];
+    __syncthreads();
+  }
   if (p.do_inv) warp_fft<N, true>(v, buf, tw, t);
 
   const float dn0 = row_dn0(p, gl);
@@ -676,6 +703,88 @@ row_warp_kernel(RowParams p) {
     v[m] = row_point<ADJ, PRE>(p, v[m], t + 32 * m, y, gl, plane, zoff, ooff, dn0, rot, last, ckp);
   if (!ADJ && p.scat_p && blockIdx.x == 0 && threadIdx.x == 0) row_scatter_finish(p, gl);
 
+  if (!p.do_fwd) return;
+  warp_fft<N, false>(v, buf, tw, t);
+  float2* dst = p.W + gl * plane + (size_t)y * N;
+#pragma unroll
+  for (int m = 0; m < E; m++) dst[t + 32 * m] = v[m];
+}
+
+// the phase mask at (x, y) from the staged row: the precomputed mask or the dn value
+template <int PRE>
+__device__ __forceinline__ float2 staged_mask(const RowParams& p, const void* mland, int x, int y) {
+  if constexpr (PRE == 1) {
+    return static_cast<const float2*>(mland)[x];
+  } else {
+    if (p.dn_dtype == BPM_DN_C64) return mask_from_complex(static_cast<const float2*>(mland)[x], p.unit_k);
+    const float d = p.dn_dtype == BPM_DN_F16 ? __half2float(static_cast<const __half*>(mland)[x])
+                                             : static_cast<const float*>(mland)[x];
+    return mask_from_real(d, p.unit_k, x, y, p.nx, p.ny, p.absorb, p.taper);
+  }
+}
+
+// Forward row pass when the fields of the group share one mask (precomputed, or one dn
+// volume): block (y, b) takes row y of fields 8b .. 8b+7, one field per warp, so the mask
+// row (or dn row) of slice z is staged once per block into shared memory with cp.async at
+// block start and is ready when the warps finish their inverse row FFTs. The arithmetic is
+// row_warp_kernel's.
+template <int N, int PRE>
+__global__ void __launch_bounds__(kRowWarps * 32, 4)
+row_shared_kernel(RowParams p, int nfields) {
+  constexpr int E = N / 32;
+  constexpr int T = kRowWarps * 32;
+  extern __shared__ __align__(16) float2 smem[];
+  float2* tw = smem;
+  const int warp = threadIdx.x >> 5, t = threadIdx.x & 31;
+  float2* buf = smem + N + warp * WarpFft<N>::BUF;
+  float2* mrow = smem + N + kRowWarps * WarpFft<N>::BUF;  // N float2: the staged mask or dn row
+  const int y = blockIdx.x;
+  const int gl = blockIdx.y * kRowWarps + warp;
+  const bool active = gl < nfields;
+  const size_t plane = (size_t)N * p.ny;
+  const size_t zoff = (size_t)p.z * plane;
+  {
+    const int es = PRE ? 8 : (p.dn_dtype == BPM_DN_C64 ? 8 : (p.dn_dtype == BPM_DN_F16 ? 2 : 4));
+    const char* srcm = PRE ? reinterpret_cast<const char*>(p.mask + zoff + (size_t)y * N)
+                           : static_cast<const char*>(p.dn) + (zoff + (size_t)y * N) * es;
+    char* dstm = reinterpret_cast<char*>(mrow);
+    for (int o = threadIdx.x * 16; o < N * es; o += T * 16) cp_async16(dstm + o, srcm + o);
+    cp_async_commit();
+  }
+  float2 v[E];
+  if (active) {
+    const float2* src = p.src + gl * p.src_bstride + (size_t)y * N;
+#pragma unroll
+    for (int m = 0; m < E; m++) v[m] = src[t + 32 * m];
+  }
+  for (int k = threadIdx.x; k < WarpFft<N>::TW; k += T) tw[k] = p.wtw[k];
+  __syncthreads();
+  if (active && p.do_inv) warp_fft<N, true>(v, buf, tw, t);
+  cp_async_wait<0>();
+  __syncthreads();  // the staged row is visible to every warp
+  if (!active) return;
+
+  const float dn0 = row_dn0(p, gl);
+  const float2 rot = row_rot(p, dn0);
+  const bool last = (p.z == p.nz - 1);
+  const size_t ooff = (size_t)(p.z - p.zout0) * plane;
+  float2* ckp = nullptr;
+  if (p.ckpt && p.z % p.ckpt_every == 0) ckp = p.ckpt + ((size_t)gl * p.n_ckpt + p.z / p.ckpt_every) * plane;
+#pragma unroll
+  for (int m = 0; m < E; m++) {
+    const int x = t + 32 * m;
+    const size_t pix = (size_t)y * N + x;
+    float2 u = cmul(v[m], staged_mask<PRE>(p, mrow, x, y));
+    if (dn0 != 0.f) u = cmul(u, rot);
+    if (p.out_kind == BPM_OUT_FIELD)
+      __stcs(reinterpret_cast<float2*>(p.out) + gl * p.out_bstride + ooff + pix, u);
+    else if (p.out_kind == BPM_OUT_INTENSITY)
+      __stcs(reinterpret_cast<float*>(p.out) + gl * p.out_bstride + ooff + pix, cabs2(u));
+    if (last && p.last_plane) p.last_plane[gl * plane + pix] = u;
+    if (ckp) ckp[pix] = u;
+    v[m] = u;
+  }
+  if (p.scat_p && y == 0 && t == 0) row_scatter_finish(p, gl);
   if (!p.do_fwd) return;
   warp_fft<N, false>(v, buf, tw, t);
   float2* dst = p.W + gl * plane + (size_t)y * N;
@@ -702,7 +811,35 @@ col_warp_kernel(ColParams p) {
   const int x0 = blockIdx.x * kColWarps;
   const int x = x0 + warp;
   float2* Wp = p.W + (size_t)gl * p.nx * N;
-  for (int k = threadIdx.x; k < WarpFft<N>::TW; k += T) tw[k] = p.wtw[k];
+  constexpr int PER = 16 * N / T;
+  static_assert(WarpFft<N>::TW <= T && N <= T, "one twiddle and one ky^2 entry per thread");
+  // weighted reduction: dn slice 0 of this tile goes to shared memory with cp.async now and
+  // is read only after the transform
+  const char* dn_stage = nullptr;
+  if (WHICH == 1 && p.dn && p.dn_stage) {
+    const int es = p.dn_dtype == BPM_DN_F16 ? 2 : 4;
+    char* dst = reinterpret_cast<char*>(smem + WarpCfg<N>::COL_F2);
+    const char* srcb = static_cast<const char*>(p.dn) + ((size_t)gl * p.dn_bstride + x0) * es;
+    for (int ch = threadIdx.x; ch < N * es; ch += T) {  // es 16-byte pieces per 16-value row
+      const int n = ch / es, j = ch - n * es;
+      cp_async16(dst + (size_t)ch * 16, srcb + (size_t)n * p.nx * es + j * 16);
+    }
+    cp_async_commit();
+    dn_stage = dst;
+  }
+  // the tile loads, then the twiddle load, go out before any shared-memory store waits on
+  // them, so their latencies overlap
+  float2 ld[PER];
+#pragma unroll
+  for (int i = 0; i < PER; i++) {
+    const int e = threadIdx.x + i * T;
+    ld[i] = Wp[(size_t)(e >> 4) * p.nx + x0 + (e & 15)];
+  }
+  const float2 twv = threadIdx.x < WarpFft<N>::TW ? p.wtw[threadIdx.x] : make_float2(0.f, 0.f);
+  // the propagator recipe's ky^2 column, staged next to the tile
+  float* sky2 = reinterpret_cast<float*>(smem + WarpCfg<N>::COL_F2);
+  const bool stage_ky = WHICH != 1 && p.prop_mode != 0;
+  const float kyv = (stage_ky && threadIdx.x < N) ? p.ky2[threadIdx.x] : 0.f;
   if (WHICH == 2 && threadIdx.x == 0) {
     // every block of the field sums the partials in the same order: identical results
     const float* part = p.red_part + (size_t)gl * (p.nx / 16) * 2;
@@ -715,7 +852,13 @@ col_warp_kernel(ColParams p) {
     s_n = p.n00f + dn0;                // mult_propagator_buff, bpm_3d_kernels.cl:482
     if (blockIdx.x == 0) p.dn0_field[gl] = dn0;
   }
-  col_load<N, T>(tile, Wp, p.nx, x0);
+#pragma unroll
+  for (int i = 0; i < PER; i++) {
+    const int e = threadIdx.x + i * T;
+    tile[tile_idx(e >> 4, e & 15)] = ld[i];
+  }
+  if (threadIdx.x < WarpFft<N>::TW) tw[threadIdx.x] = twv;
+  if (stage_ky && threadIdx.x < N) sky2[threadIdx.x] = kyv;
   __syncthreads();
   float2 v[E];
 #pragma unroll
@@ -729,18 +872,18 @@ col_warp_kernel(ColParams p) {
     const float2 plain = (p.scat && x == 0) ? plain_wave(p) : make_float2(0.f, 0.f);
     float S = 0.f, G = 0.f;
 #pragma unroll
-    for (int m = 0; m < E; m++) v[m] = prop_point(p, v[m], x, t + 32 * m, nk, plain, S, G);
+    for (int m = 0; m < E; m++) v[m] = prop_point<true>(p, v[m], x, t + 32 * m, nk, plain, S, G, sky2);
     if (p.scat) scat_partials_store<T>(p, S, G, gl, red);
     warp_fft<N, true>(v, buf, tw, t);
   }
   __syncthreads();
 #pragma unroll
   for (int m = 0; m < E; m++) tile[tile_idx(t + 32 * m, warp)] = v[m];
+  if (WHICH == 1 && dn_stage) cp_async_wait<0>();  // this thread's dn pieces have landed
   __syncthreads();
   if (WHICH == 1) {
     // weighted mode: sum |u_hat| and |u_hat|*dn over the tile while storing it, with the
     // coalesced tile mapping (dn slice 0 read 16 columns at a time)
-    constexpr int PER = 16 * N / T;
     float sdn = 0.f, su = 0.f;
 #pragma unroll 4
     for (int i = 0; i < PER; i++) {
@@ -751,7 +894,15 @@ col_warp_kernel(ColParams p) {
       Wp[k] = u;
       const float a = __fsqrt_rn(cabs2(u));
       su += a;
-      if (p.dn) sdn += a * load_dn_real(p.dn, p.dn_dtype, gl * p.dn_bstride + k);
+      if (p.dn) {
+        float d;
+        if (dn_stage)
+          d = p.dn_dtype == BPM_DN_F16 ? __half2float(reinterpret_cast<const __half*>(dn_stage)[e])
+                                       : reinterpret_cast<const float*>(dn_stage)[e];
+        else
+          d = load_dn_real(p.dn, p.dn_dtype, gl * p.dn_bstride + k);
+        sdn = fmaf(a, d, sdn);
+      }
     }
     block_sum2<T>(sdn, su, red);
     if (threadIdx.x == 0) {
@@ -765,18 +916,305 @@ col_warp_kernel(ColParams p) {
 }
 
 // ---------------------------------------------------------------------------------------
+// Pipelined persistent kernels (128 <= N <= 512). A launch holds as many blocks as fit on
+// the device at once; each warp (row pass) or block (column pass) walks a strided list of
+// rows or 16-column tiles and copies the next item's inputs into shared memory with
+// cp.async while it transforms the current one, so the global-memory latency of one item
+// hides behind the arithmetic of the previous one instead of stalling every block of a
+// single wave at the same time. Same arithmetic, in the same order, as the warp kernels
+// above; the two agree to FP32 rounding (the compiler is free to contract their complex
+// products into FMAs differently), and each is deterministic on its own.
+// ---------------------------------------------------------------------------------------
+template <int N>
+struct PipeCfg {
+  static constexpr int TWPAD = (WarpFft<N>::TW + 1) & ~1;  // keeps the regions after it 16-byte aligned
+  static constexpr int ROW_WARP_F2 = WarpFft<N>::BUF + 2 * N;  // exchange buffer, row landing, mask landing
+  static constexpr size_t ROW_SMEM = ((size_t)TWPAD + (size_t)kRowWarps * ROW_WARP_F2) * sizeof(float2);
+  static constexpr size_t COL_SMEM =
+      ((size_t)TWPAD + 2 * 16 * (size_t)N + (size_t)kColWarps * WarpFft<N>::BUF) * sizeof(float2);
+  static_assert(WarpFft<N>::BUF % 2 == 0 && TWPAD % 2 == 0, "16-byte aligned regions");
+};
+
+// the warp copies bytes [src, src + bytes) into dst in 16-byte pieces (bytes % 16 == 0,
+// both addresses 16-byte aligned)
+__device__ __forceinline__ void warp_copy_async(void* dst, const void* src, int bytes, int t) {
+  const char* s = static_cast<const char*>(src);
+  char* d = static_cast<char*>(dst);
+  for (int o = t * 16; o < bytes; o += 32 * 16) cp_async16(d + o, s + o);
+}
+
+// Forward row pass over rows r = gw, gw + nw, ... of the group (r = field * ny + y).
+template <int N, int PRE>
+__global__ void __launch_bounds__(kRowWarps * 32, 2)
+row_pipe_kernel(RowParams p, int nrows) {
+  constexpr int E = N / 32;
+  constexpr int T = kRowWarps * 32;
+  extern __shared__ __align__(16) float2 smem[];
+  float2* tw = smem;
+  const int warp = threadIdx.x >> 5, t = threadIdx.x & 31;
+  float2* buf = smem + PipeCfg<N>::TWPAD + warp * PipeCfg<N>::ROW_WARP_F2;
+  float2* land = buf + WarpFft<N>::BUF;
+  float2* mland = land + N;
+  if (p.do_inv || p.do_fwd) {
+    for (int k = threadIdx.x; k < WarpFft<N>::TW; k += T) tw[k] = p.wtw[k];
+    __syncthreads();
+  }
+  const size_t plane = (size_t)N * p.ny;
+  const int dn_es = p.dn_dtype == BPM_DN_C64 ? 8 : (p.dn_dtype == BPM_DN_F16 ? 2 : 4);
+  const size_t zoff = (size_t)p.z * plane;
+  const size_t ooff = (size_t)(p.z - p.zout0) * plane;
+  const bool last = (p.z == p.nz - 1);
+  const int nw = gridDim.x * kRowWarps;
+
+  auto issue_row = [&](int rr) {
+    const int gl = rr / p.ny, y = rr - gl * p.ny;
+    warp_copy_async(land, p.src + gl * p.src_bstride + (size_t)y * N, N * 8, t);
+  };
+  auto issue_mask = [&](int rr) {
+    if (!p.do_mask) return;
+    const int gl = rr / p.ny, y = rr - gl * p.ny;
+    if (PRE)
+      warp_copy_async(mland, p.mask + zoff + (size_t)y * N, N * 8, t);
+    else
+      warp_copy_async(mland,
+                      static_cast<const char*>(p.dn) + ((size_t)gl * p.dn_bstride + zoff + (size_t)y * N) * dn_es,
+                      N * dn_es, t);
+  };
+
+  // commit groups alternate row, mask, row, mask, ...: waiting until one group is pending
+  // completes the older of the two
+  int r = blockIdx.x * kRowWarps + warp;
+  if (r < nrows) issue_row(r);
+  cp_async_commit();
+  if (r < nrows) issue_mask(r);
+  cp_async_commit();
+  for (; r < nrows; r += nw) {
+    const int gl = r / p.ny, y = r - gl * p.ny;
+    cp_async_wait<1>();  // row r
+    __syncwarp();
+    float2 v[E];
+#pragma unroll
+    for (int m = 0; m < E; m++) v[m] = land[t + 32 * m];
+    __syncwarp();
+    const int rn = r + nw;
+    if (rn < nrows) issue_row(rn);
+    cp_async_commit();
+    if (p.do_inv) warp_fft<N, true>(v, buf, tw, t);
+
+    const float dn0 = row_dn0(p, gl);
+    const float2 rot = row_rot(p, dn0);
+    float2* ckp = nullptr;
+    if (p.ckpt && p.z % p.ckpt_every == 0) ckp = p.ckpt + ((size_t)gl * p.n_ckpt + p.z / p.ckpt_every) * plane;
+    cp_async_wait<1>();  // mask row r
+    __syncwarp();
+#pragma unroll
+    for (int m = 0; m < E; m++) {
+      const int x = t + 32 * m;
+      const size_t pix = (size_t)y * N + x;
+      float2 u = v[m];
+      if (p.do_mask) {
+        u = cmul(u, staged_mask<PRE>(p, mland, x, y));
+        if (dn0 != 0.f) u = cmul(u, rot);
+      }
+      if (p.out_kind == BPM_OUT_FIELD)
+        __stcs(reinterpret_cast<float2*>(p.out) + gl * p.out_bstride + ooff + pix, u);
+      else if (p.out_kind == BPM_OUT_INTENSITY)
+        __stcs(reinterpret_cast<float*>(p.out) + gl * p.out_bstride + ooff + pix, cabs2(u));
+      if (last && p.last_plane) p.last_plane[gl * plane + pix] = u;
+      if (ckp) ckp[pix] = u;
+      v[m] = u;
+    }
+    __syncwarp();
+    if (rn < nrows) issue_mask(rn);
+    cp_async_commit();
+    if (p.scat_p && y == 0 && t == 0) row_scatter_finish(p, gl);
+    if (p.do_fwd) {
+      warp_fft<N, false>(v, buf, tw, t);
+      float2* dst = p.W + gl * plane + (size_t)y * N;
+#pragma unroll
+      for (int m = 0; m < E; m++) dst[t + 32 * m] = v[m];
+    }
+  }
+  cp_async_wait<0>();
+}
+
+// Column pass over 16-column tiles it = blockIdx.x, + gridDim.x, ... of the group
+// (it = field * (nx/16) + tile), double-buffered in shared memory. WHICH as col_warp_kernel.
+template <int N, int WHICH>
+__global__ void __launch_bounds__(kColWarps * 32, 1)
+col_pipe_kernel(ColParams p, int ntiles) {
+  constexpr int E = N / 32;
+  constexpr int T = kColWarps * 32;
+  constexpr int PER = 16 * N / T;
+  extern __shared__ __align__(16) float2 smem[];
+  float2* tw = smem;
+  float2* tiles = smem + PipeCfg<N>::TWPAD;
+  __shared__ float red[64];
+  __shared__ float s_n;
+  const int warp = threadIdx.x >> 5, t = threadIdx.x & 31;
+  float2* buf = tiles + 2 * 16 * N + warp * WarpFft<N>::BUF;
+  const int tpf = p.nx / 16;
+  for (int k = threadIdx.x; k < WarpFft<N>::TW; k += T) tw[k] = p.wtw[k];
+  auto issue_tile = [&](float2* dst, int it) {
+    const int gl = it / tpf, x0 = (it - gl * tpf) * 16;
+    const float2* Wp = p.W + (size_t)gl * p.nx * N;
+#pragma unroll
+    for (int i = 0; i < PER; i++) {
+      const int e = threadIdx.x + i * T;
+      cp_async8(dst + tile_idx(e >> 4, e & 15), Wp + (size_t)(e >> 4) * p.nx + x0 + (e & 15));
+    }
+  };
+  int it = blockIdx.x;
+  if (it < ntiles) issue_tile(tiles, it);
+  cp_async_commit();
+  for (int k = 0; it < ntiles; it += gridDim.x, k++) {
+    float2* cur = tiles + (k & 1) * 16 * N;
+    const int nxt = it + gridDim.x;
+    if (nxt < ntiles) issue_tile(tiles + ((k + 1) & 1) * 16 * N, nxt);
+    cp_async_commit();
+    const int gl = it / tpf, ti = it - gl * tpf, x0 = ti * 16, x = x0 + warp;
+    float2* Wp = p.W + (size_t)gl * p.nx * N;
+    if (WHICH == 2 && threadIdx.x == 0) {
+      // every block of the field sums the partials in the same order: identical results
+      const float* part = p.red_part + (size_t)gl * tpf * 2;
+      float dn_sum = 0.f, u_sum = 0.f;
+      for (int i = 0; i < tpf; i++) {
+        dn_sum += part[2 * i];
+        u_sum += part[2 * i + 1];
+      }
+      const float dn0 = dn_sum / u_sum;  // mult_dn_mean_buff, bpm_3d_kernels.cl:117
+      s_n = p.n00f + dn0;                // mult_propagator_buff, bpm_3d_kernels.cl:482
+      if (ti == 0) p.dn0_field[gl] = dn0;
+    }
+    float dnv[WHICH == 1 ? PER : 1];
+    if (WHICH == 1) {
+      // dn slice 0 of this tile, fetched now so the loads overlap the transform
+#pragma unroll
+      for (int i = 0; i < PER; i++) {
+        const int e = threadIdx.x + i * T;
+        dnv[i] = p.dn ? load_dn_real(p.dn, p.dn_dtype, gl * p.dn_bstride + (size_t)(e >> 4) * p.nx + x0 + (e & 15))
+                      : 0.f;
+      }
+    }
+    cp_async_wait<1>();  // tile it
+    __syncthreads();
+    float2 v[E];
+#pragma unroll
+    for (int m = 0; m < E; m++) v[m] = cur[tile_idx(t + 32 * m, warp)];
+    if (WHICH != 2) warp_fft<N, false>(v, buf, tw, t);
+    if (WHICH != 1) {
+      const float n_eff = WHICH == 2 ? s_n : (p.prop_mode == 1 ? p.slice_n[p.z + 1] : p.n00f);
+      const float nk = prop_nk(p, n_eff);
+      const float2 plain = (p.scat && x == 0) ? plain_wave(p) : make_float2(0.f, 0.f);
+      float S = 0.f, G = 0.f;
+#pragma unroll
+      for (int m = 0; m < E; m++) v[m] = prop_point<true>(p, v[m], x, t + 32 * m, nk, plain, S, G, p.ky2);
+      if (p.scat) {
+        block_sum2<T>(S, G, red);
+        if (threadIdx.x == 0) {
+          float* o = p.scat_part + ((size_t)gl * tpf + ti) * 2;
+          o[0] = S;
+          o[1] = G;
+        }
+      }
+      warp_fft<N, true>(v, buf, tw, t);
+    }
+    // each warp writes back the column it read: no other warp touches those slots
+#pragma unroll
+    for (int m = 0; m < E; m++) cur[tile_idx(t + 32 * m, warp)] = v[m];
+    __syncthreads();
+    if (WHICH == 1) {
+      float sdn = 0.f, su = 0.f;
+#pragma unroll
+      for (int i = 0; i < PER; i++) {
+        const int e = threadIdx.x + i * T;
+        const int n = e >> 4, c = e & 15;
+        const float2 u = cur[tile_idx(n, c)];
+        Wp[(size_t)n * p.nx + x0 + c] = u;
+        const float a = __fsqrt_rn(cabs2(u));
+        su += a;
+        if (p.dn) sdn = fmaf(a, dnv[i], sdn);
+      }
+      block_sum2<T>(sdn, su, red);
+      if (threadIdx.x == 0) {
+        float* o = p.red_part + ((size_t)gl * tpf + ti) * 2;
+        o[0] = sdn;
+        o[1] = su;
+      }
+    } else {
+      col_store<N, T>(cur, Wp, p.nx, x0);
+    }
+    __syncthreads();  // cur is refilled by the next iteration's prefetch
+  }
+  cp_async_wait<0>();
+}
+
+// ---------------------------------------------------------------------------------------
 // dispatch over power-of-two sizes
 // ---------------------------------------------------------------------------------------
 template <template <int> class K>
 struct SizeDispatch;
 
+// Which row/column kernels a march uses for 128 <= N <= 512. The pipelined persistent
+// kernels hide each item's load latency behind the previous item but hold the whole device
+// at half the warps of the single-wave warp kernels; several field groups marching at once
+// on their own streams hide that latency better by overlapping each other's waves. So the
+// pipelined kernels serve marches of a single group, the warp kernels concurrent groups
+// (measured on GB300, 512x512: one field 8.0 vs 6.6 G voxel-updates/s; 64 fields in 4
+// concurrent groups of 8: 74 vs 57 ms). Both compute the same bits (explicit fmaf in all
+// shared arithmetic), so a field's result does not depend on the batch it marched in.
+// BPM_GB300_KERNELS=warp / =pipe forces one family.
+thread_local bool t_single_group = false;
+
+bool pipe_enabled() {
+  static const int forced = [] {
+    const char* e = getenv("BPM_GB300_KERNELS");
+    if (e && strcmp(e, "warp") == 0) return 0;
+    if (e && strcmp(e, "pipe") == 0) return 1;
+    return -1;
+  }();
+  return forced >= 0 ? forced == 1 : t_single_group;
+}
+
+// blocks of `kernel` resident on the whole device at once
+template <class Kern>
+int resident_blocks(Kern kernel, int threads, size_t smem) {
+  int dev = 0, nsm = 1, occ = 0;
+  cudaGetDevice(&dev);
+  cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
+  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, kernel, threads, smem);
+  cudaGetLastError();
+  return std::max(1, occ) * std::max(1, nsm);
+}
+
+// workers for `items` work items with at most `cap` workers, every worker taking the same
+// number of items (the last one possibly fewer)
+inline int balanced_workers(int items, int cap) {
+  const int per = (items + cap - 1) / cap;
+  return (items + per - 1) / per;
+}
+
 template <int N>
 struct RowK {
   static constexpr bool WARP = N >= 128 && N <= 512;
+  static int& pipe_cap(int pre) {
+    static int cap[2] = {0, 0};
+    return cap[pre];
+  }
   static void prepare() {
     static bool attr = false;
     if (!attr) {
       if constexpr (WARP) {
+        cudaFuncSetAttribute(row_shared_kernel<N, 0>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                             (int)WarpCfg<N>::ROW_SMEM_SHARED);
+        cudaFuncSetAttribute(row_shared_kernel<N, 1>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                             (int)WarpCfg<N>::ROW_SMEM_SHARED);
+        cudaFuncSetAttribute(row_pipe_kernel<N, 0>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                             (int)PipeCfg<N>::ROW_SMEM);
+        cudaFuncSetAttribute(row_pipe_kernel<N, 1>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                             (int)PipeCfg<N>::ROW_SMEM);
+        pipe_cap(0) = resident_blocks(row_pipe_kernel<N, 0>, kRowWarps * 32, PipeCfg<N>::ROW_SMEM);
+        pipe_cap(1) = resident_blocks(row_pipe_kernel<N, 1>, kRowWarps * 32, PipeCfg<N>::ROW_SMEM);
         cudaFuncSetAttribute(row_warp_kernel<N, false, 0>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                              (int)WarpCfg<N>::ROW_SMEM);
         cudaFuncSetAttribute(row_warp_kernel<N, true, 0>, cudaFuncAttributeMaxDynamicSharedMemorySize,
@@ -794,10 +1232,42 @@ struct RowK {
       attr = true;
     }
   }
+  // the pipelined kernel copies rows of src and of the mask (or dn) with 16-byte cp.async
+  static bool pipe_ok(const RowParams& p) {
+    if (!pipe_enabled() || !aligned16(p.src) || ((size_t)p.src_bstride * 8) % 16) return false;
+    if (!p.do_mask) return true;
+    if (p.mask) return aligned16(p.mask);
+    const int es = p.dn_dtype == BPM_DN_C64 ? 8 : (p.dn_dtype == BPM_DN_F16 ? 2 : 4);
+    return aligned16(p.dn) && ((size_t)p.dn_bstride * es) % 16 == 0;
+  }
+  // all fields of the group share the slice-z mask row: the precomputed mask, or one dn
+  // volume (dn_batch_stride 0); the row is staged with 16-byte cp.async
+  static bool shared_ok(const RowParams& p) {
+    if (!p.do_mask) return false;
+    if (p.mask) return aligned16(p.mask);
+    return p.dn_bstride == 0 && aligned16(p.dn);
+  }
   // g.x counts 16-row tiles; the warp kernel covers kRowWarps rows per block
   static int launch(dim3 g, cudaStream_t s, const RowParams& p, bool adj) {
     prepare();
     if constexpr (WARP) {
+      if (!adj && pipe_ok(p)) {
+        const int pre = p.mask ? 1 : 0;
+        const int nrows = (int)g.y * p.ny;
+        const int warps = balanced_workers(nrows, pipe_cap(pre) * kRowWarps);
+        const int blocks = (warps + kRowWarps - 1) / kRowWarps;
+        auto fn = pre ? row_pipe_kernel<N, 1> : row_pipe_kernel<N, 0>;
+        fn<<<blocks, kRowWarps * 32, PipeCfg<N>::ROW_SMEM, s>>>(p, nrows);
+        BPM_LAUNCH_CHECK("row_pipe_kernel");
+        return BPM_OK;
+      }
+      if (!adj && shared_ok(p) && g.y >= 2) {
+        const dim3 gs(p.ny, (g.y + kRowWarps - 1) / kRowWarps);
+        auto fn = p.mask ? row_shared_kernel<N, 1> : row_shared_kernel<N, 0>;
+        fn<<<gs, kRowWarps * 32, WarpCfg<N>::ROW_SMEM_SHARED, s>>>(p, (int)g.y);
+        BPM_LAUNCH_CHECK("row_shared_kernel");
+        return BPM_OK;
+      }
       const dim3 gw(g.x * 16 / kRowWarps, g.y);
       auto fn = adj ? (p.mask ? row_warp_kernel<N, true, 1> : row_warp_kernel<N, true, 0>)
                     : (p.mask ? row_warp_kernel<N, false, 1> : row_warp_kernel<N, false, 0>);
@@ -821,16 +1291,36 @@ struct ColK {
     return WHICH == 0 ? col_pass_kernel<N> : (WHICH == 1 ? col_fwd_reduce_kernel<N> : col_inv_kernel<N>);
   }
   static constexpr int threads() { return WARP ? kColWarps * 32 : TileCfg<N>::THREADS; }
-  static constexpr size_t smem() { return WARP ? WarpCfg<N>::COL_SMEM : TileCfg<N>::SMEM; }
+  static constexpr size_t smem() {
+    return WARP ? (WHICH == 1 ? WarpCfg<N>::COL_SMEM_DN : WarpCfg<N>::COL_SMEM_KY) : TileCfg<N>::SMEM;
+  }
+  static int& pipe_cap() {
+    static int cap = 0;
+    return cap;
+  }
   static void prepare() {
     static bool attr = false;
     if (!attr) {
       cudaFuncSetAttribute(fn(), cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem());
+      if constexpr (WARP) {
+        cudaFuncSetAttribute(col_pipe_kernel<N, WHICH>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                             (int)PipeCfg<N>::COL_SMEM);
+        pipe_cap() = resident_blocks(col_pipe_kernel<N, WHICH>, kColWarps * 32, PipeCfg<N>::COL_SMEM);
+      }
       attr = true;
     }
   }
   static int launch(dim3 g, cudaStream_t s, const ColParams& p) {
     prepare();
+    if constexpr (WARP) {
+      if (pipe_enabled() && aligned16(p.W)) {
+        const int ntiles = (int)(g.x * g.y);
+        col_pipe_kernel<N, WHICH><<<balanced_workers(ntiles, pipe_cap()), kColWarps * 32, PipeCfg<N>::COL_SMEM,
+                                    s>>>(p, ntiles);
+        BPM_LAUNCH_CHECK("col_pipe_kernel");
+        return BPM_OK;
+      }
+    }
     fn()<<<g, threads(), smem(), s>>>(p);
     BPM_LAUNCH_CHECK("col_pass_kernel");
     return BPM_OK;
@@ -1034,6 +1524,7 @@ MarchCtx make_ctx(const bpm_plan* pl, const bpm_request* r, void* ws, int b0, in
   cp.nx = nx; cp.ny = ny; cp.nz = nz;
   cp.prop_mode = d.mean_mode == BPM_MEAN_IGNORE ? 0 : (d.mean_mode == BPM_MEAN_SIMPLE ? 1 : 2);
   cp.H = pl->H;
+  cp.Ht = pl->Ht;
   cp.kx2 = pl->kx2;
   cp.ky2 = pl->ky2;
   cp.k0f = pl->k0f;
@@ -1054,6 +1545,11 @@ MarchCtx make_ctx(const bpm_plan* pl, const bpm_request* r, void* ws, int b0, in
   cp.spi = r->scattering_plane_ind;
   cp.tw = pl->tw_y;
   cp.wtw = pl->wtw_y;
+  {
+    const int es = r->dn_dtype == BPM_DN_F16 ? 2 : 4;
+    cp.dn_stage = (r->dn_dtype == BPM_DN_F32 || r->dn_dtype == BPM_DN_F16) && cp.dn && aligned16(cp.dn) &&
+                  ((size_t)r->dn_batch_stride * es) % 16 == 0 && ((size_t)nx * es) % 16 == 0;
+  }
 
   c.grow = dim3(ny / 16, Gc);
   c.gcol = dim3(nx / 16, Gc);
@@ -1094,14 +1590,32 @@ int launch_row_z(const bpm_plan* pl, const bpm_request* r, MarchCtx& c, int z, c
   return launch_row(pl->d.nx, c.grow, s, rp);
 }
 
-// The march of one group of fields [b0, b0+Gc) on stream s with workspace slot ws.
-int enqueue_group(bpm_plan* pl, const bpm_request* r, void* ws, int b0, int Gc, cudaStream_t s) {
-  int rc;
-  MarchCtx c = make_ctx(pl, r, ws, b0, Gc);
-  if ((rc = launch_first_row(pl, r, c, b0, s))) return rc;
-  for (int i = 0; i + 1 < pl->d.nz; i++) {
-    if ((rc = launch_cols(pl, c, i, 0, s))) return rc;
-    if ((rc = launch_row_z(pl, r, c, i + 1, s))) return rc;
+// Destination of bpm_propagate_to_host: the output volume is also copied, run of `chunk`
+// planes by run of `chunk` planes, to host memory laid out like req->out.
+struct HostSink {
+  char* host;
+  int chunk;
+};
+
+// After the group's stream s has produced planes [z0, z1) of fields [b0, b0+Gc), the
+// copy stream moves them to the host: one strided copy (a row per field) when the batch
+// stride fits the copy engine's pitch limit, else one copy per field.
+int sink_copy(bpm_plan* pl, const bpm_request* r, const HostSink& h, int b0, int Gc, int z0, int z1,
+              cudaStream_t s, cudaEvent_t ev) {
+  const size_t es = r->out_kind == BPM_OUT_FIELD ? 8 : 4;
+  const size_t plane = (size_t)pl->d.nx * pl->d.ny;
+  const size_t pitch = (size_t)r->out_batch_stride * es;
+  const size_t off = (size_t)b0 * pitch + (size_t)z0 * plane * es;
+  const size_t width = (size_t)(z1 - z0) * plane * es;
+  const char* src = static_cast<const char*>(r->out) + off;
+  BPM_CUDA_TRY(cudaEventRecord(ev, s));
+  BPM_CUDA_TRY(cudaStreamWaitEvent(pl->copy, ev, 0));
+  if (Gc == 1 || pitch <= (size_t)pl->max_pitch) {
+    BPM_CUDA_TRY(cudaMemcpy2DAsync(h.host + off, pitch, src, pitch, width, Gc, cudaMemcpyDeviceToHost, pl->copy));
+  } else {
+    for (int g = 0; g < Gc; g++)
+      BPM_CUDA_TRY(cudaMemcpyAsync(h.host + off + g * pitch, src + g * pitch, width, cudaMemcpyDeviceToHost,
+                                   pl->copy));
   }
   return BPM_OK;
 }
@@ -1110,29 +1624,63 @@ int enqueue_group(bpm_plan* pl, const bpm_request* r, void* ws, int b0, int Gc, 
 // concurrently on the plan's auxiliary streams (forked from and joined back to s through
 // events, which also captures into a CUDA graph as parallel branches), so one group's
 // kernels fill the device while another's run their tail waves; otherwise they march one
-// after the other on s.
-int enqueue_march(bpm_plan* pl, const bpm_request* r, void* ws, size_t ws_bytes, cudaStream_t s) {
+// after the other on s. Groups marching at the same time are enqueued step by step in
+// turn, so work (and, with a host sink, the finished planes handed to the copy stream)
+// reaches the device in the order it can run.
+int enqueue_march(bpm_plan* pl, const bpm_request* r, void* ws, size_t ws_bytes, cudaStream_t s,
+                  const HostSink* sink = nullptr) {
   int rc = check_workspace(pl, r, ws, ws_bytes);
   if (rc) return rc;
+  const int nz = pl->d.nz;
   const int G = group_size(pl, r);
   const int ngroups = (r->batch + G - 1) / G;
   const size_t slot = ws_layout(pl, G).total;
-  const int conc = (int)std::min<size_t>({(size_t)ngroups, ws_bytes / slot, (size_t)kMaxConcurrentGroups});
-  if (conc <= 1) {
-    for (int b0 = 0; b0 < r->batch; b0 += G)
-      if ((rc = enqueue_group(pl, r, ws, b0, std::min(G, r->batch - b0), s))) return rc;
-    return BPM_OK;
+  const int conc = std::max(
+      1, (int)std::min<size_t>({(size_t)ngroups, ws_bytes / slot, (size_t)kMaxConcurrentGroups}));
+  struct SingleGroupScope {  // kernel family of this march (pipe_enabled)
+    explicit SingleGroupScope(bool v) { t_single_group = v; }
+    ~SingleGroupScope() { t_single_group = false; }
+  } scope(conc == 1);
+  cudaStream_t st[kMaxConcurrentGroups];
+  for (int j = 0; j < conc; j++) st[j] = conc > 1 ? pl->aux[j] : s;
+  if (conc > 1 || sink) BPM_CUDA_TRY(cudaEventRecord(pl->ev_fork, s));
+  if (conc > 1)
+    for (int j = 0; j < conc; j++) BPM_CUDA_TRY(cudaStreamWaitEvent(st[j], pl->ev_fork, 0));
+  if (sink) BPM_CUDA_TRY(cudaStreamWaitEvent(pl->copy, pl->ev_fork, 0));
+  for (int w0 = 0; w0 < ngroups; w0 += conc) {
+    const int nwave = std::min(conc, ngroups - w0);
+    MarchCtx c[kMaxConcurrentGroups];
+    int b0[kMaxConcurrentGroups], Gc[kMaxConcurrentGroups], zdone[kMaxConcurrentGroups];
+    for (int j = 0; j < nwave; j++) {
+      b0[j] = (w0 + j) * G;
+      Gc[j] = std::min(G, r->batch - b0[j]);
+      zdone[j] = 0;
+      c[j] = make_ctx(pl, r, static_cast<char*>(ws) + (size_t)j * slot, b0[j], Gc[j]);
+      if ((rc = launch_first_row(pl, r, c[j], b0[j], st[j]))) return rc;
+    }
+    for (int i = 0; i + 1 < nz || (i == 0 && nz == 1); i++) {
+      for (int j = 0; j < nwave; j++) {
+        if (i + 1 < nz) {
+          if ((rc = launch_cols(pl, c[j], i, 0, st[j]))) return rc;
+          if ((rc = launch_row_z(pl, r, c[j], i + 1, st[j]))) return rc;
+        }
+        const int z1 = std::min(i + 2, nz);  // planes [0, z1) of the group are written
+        if (sink && (z1 - zdone[j] >= sink->chunk || z1 == nz) && z1 > zdone[j]) {
+          if ((rc = sink_copy(pl, r, *sink, b0[j], Gc[j], zdone[j], z1, st[j], pl->ev_ready[j]))) return rc;
+          zdone[j] = z1;
+        }
+      }
+    }
   }
-  BPM_CUDA_TRY(cudaEventRecord(pl->ev_fork, s));
-  for (int i = 0; i < conc; i++) BPM_CUDA_TRY(cudaStreamWaitEvent(pl->aux[i], pl->ev_fork, 0));
-  for (int g = 0; g < ngroups; g++) {
-    const int b0 = g * G;
-    char* wsg = static_cast<char*>(ws) + (size_t)(g % conc) * slot;
-    if ((rc = enqueue_group(pl, r, wsg, b0, std::min(G, r->batch - b0), pl->aux[g % conc]))) return rc;
+  if (conc > 1) {
+    for (int j = 0; j < conc; j++) {
+      BPM_CUDA_TRY(cudaEventRecord(pl->ev_join[j], st[j]));
+      BPM_CUDA_TRY(cudaStreamWaitEvent(s, pl->ev_join[j], 0));
+    }
   }
-  for (int i = 0; i < conc; i++) {
-    BPM_CUDA_TRY(cudaEventRecord(pl->ev_join[i], pl->aux[i]));
-    BPM_CUDA_TRY(cudaStreamWaitEvent(s, pl->ev_join[i], 0));
+  if (sink) {
+    BPM_CUDA_TRY(cudaEventRecord(pl->ev_copied, pl->copy));
+    BPM_CUDA_TRY(cudaStreamWaitEvent(s, pl->ev_copied, 0));
   }
   return BPM_OK;
 }
@@ -1360,6 +1908,7 @@ extern "C" int bpm_plan_create(const bpm_grid_desc* d, bpm_plan** out) {
   if ((e = cudaMalloc(&pl->ky2, ny * sizeof(float)))) return fail(e, "cudaMalloc");
   if ((e = cudaMalloc(&pl->taper, taper.size() * sizeof(float)))) return fail(e, "cudaMalloc");
   if ((e = cudaMalloc(&pl->H, (size_t)nx * ny * sizeof(float2)))) return fail(e, "cudaMalloc");
+  if ((e = cudaMalloc(&pl->Ht, (size_t)nx * ny * sizeof(float2)))) return fail(e, "cudaMalloc");
   if ((e = cudaMalloc(&pl->sw, (size_t)nx * ny * sizeof(float)))) return fail(e, "cudaMalloc");
   if ((e = cudaMalloc(&pl->gw, (size_t)nx * ny * sizeof(float)))) return fail(e, "cudaMalloc");
   if ((e = cudaMemcpy(pl->tw_x, twx.data(), nx * sizeof(float2), cudaMemcpyHostToDevice))) return fail(e, "cudaMemcpy");
@@ -1379,7 +1928,7 @@ extern "C" int bpm_plan_create(const bpm_grid_desc* d, bpm_plan** out) {
   }
   dim3 tb(128), tg((nx + 127) / 128, ny);
   build_tables_kernel<<<tg, tb>>>(nx, ny, d->dx, d->dy, d->dz, d->n0, pl->k0, pl->n0f, pl->k0f, d->prop_kind,
-                                  d->use_fresnel_approx, pl->kx2, pl->ky2, pl->H, pl->sw, pl->gw);
+                                  d->use_fresnel_approx, pl->kx2, pl->ky2, pl->H, pl->Ht, pl->sw, pl->gw);
   if ((e = cudaGetLastError())) return fail(e, "build_tables_kernel");
   count_launch();
   if ((e = cudaDeviceSynchronize())) return fail(e, "build_tables_kernel");
@@ -1387,8 +1936,12 @@ extern "C" int bpm_plan_create(const bpm_grid_desc* d, bpm_plan** out) {
   for (int i = 0; i < kMaxConcurrentGroups; i++) {
     if ((e = cudaStreamCreateWithFlags(&pl->aux[i], cudaStreamNonBlocking))) return fail(e, "cudaStreamCreate");
     if ((e = cudaEventCreateWithFlags(&pl->ev_join[i], cudaEventDisableTiming))) return fail(e, "cudaEventCreate");
+    if ((e = cudaEventCreateWithFlags(&pl->ev_ready[i], cudaEventDisableTiming))) return fail(e, "cudaEventCreate");
   }
   if ((e = cudaEventCreateWithFlags(&pl->ev_fork, cudaEventDisableTiming))) return fail(e, "cudaEventCreate");
+  if ((e = cudaStreamCreateWithFlags(&pl->copy, cudaStreamNonBlocking))) return fail(e, "cudaStreamCreate");
+  if ((e = cudaEventCreateWithFlags(&pl->ev_copied, cudaEventDisableTiming))) return fail(e, "cudaEventCreate");
+  if ((e = cudaDeviceGetAttribute(&pl->max_pitch, cudaDevAttrMaxPitch, pl->device))) return fail(e, "cudaDeviceGetAttribute");
   *out = pl;
   return BPM_OK;
 }
@@ -1402,12 +1955,16 @@ extern "C" int bpm_plan_destroy(bpm_plan* pl) {
   for (int i = 0; i < kMaxConcurrentGroups; i++) {
     if (pl->aux[i]) cudaStreamDestroy(pl->aux[i]);
     if (pl->ev_join[i]) cudaEventDestroy(pl->ev_join[i]);
+    if (pl->ev_ready[i]) cudaEventDestroy(pl->ev_ready[i]);
   }
   if (pl->ev_fork) cudaEventDestroy(pl->ev_fork);
+  if (pl->copy) cudaStreamDestroy(pl->copy);
+  if (pl->ev_copied) cudaEventDestroy(pl->ev_copied);
   cudaFree(pl->kx2);
   cudaFree(pl->ky2);
   cudaFree(pl->taper);
   cudaFree(pl->H);
+  cudaFree(pl->Ht);
   cudaFree(pl->sw);
   cudaFree(pl->gw);
   delete pl;
@@ -1432,6 +1989,31 @@ extern "C" int bpm_propagate(bpm_plan* pl, const bpm_request* r, void* ws, size_
   int rc = check_request(pl, r);
   if (rc) return rc;
   return enqueue_march(pl, r, ws, ws_bytes, static_cast<cudaStream_t>(stream));
+}
+
+extern "C" int bpm_propagate_to_host(bpm_plan* pl, const bpm_request* r, void* host_out, int chunk_planes,
+                                     void* ws, size_t ws_bytes, void* stream) {
+  clear_error();
+  if (!pl) { set_error("plan is NULL"); return BPM_ERR_ARG; }
+  int rc = check_request(pl, r);
+  if (rc) return rc;
+  if (!host_out || !r->out || r->out_kind == BPM_OUT_NONE) {
+    set_error("bpm_propagate_to_host needs host_out and a device output volume (out, out_kind)");
+    return BPM_ERR_ARG;
+  }
+  if (chunk_planes < 1) { set_error("chunk_planes must be >= 1"); return BPM_ERR_ARG; }
+  if (r->out_batch_stride < (long long)pl->d.nz * pl->d.nx * pl->d.ny) {
+    set_error("out_batch_stride must hold nz planes");
+    return BPM_ERR_ARG;
+  }
+  cudaPointerAttributes a;
+  if (cudaPointerGetAttributes(&a, r->out) != cudaSuccess || a.type != cudaMemoryTypeDevice) {
+    cudaGetLastError();
+    set_error("out must be device memory for bpm_propagate_to_host");
+    return BPM_ERR_ARG;
+  }
+  HostSink h{static_cast<char*>(host_out), chunk_planes};
+  return enqueue_march(pl, r, ws, ws_bytes, static_cast<cudaStream_t>(stream), &h);
 }
 
 extern "C" int bpm_launch_pass(bpm_plan* pl, const bpm_request* r, void* ws, size_t ws_bytes, int pass, int z,

@@ -25,3 +25,13 @@ extern "C" int bpm_version(void) { return BPM_GB300_VERSION; }
 extern "C" const char* bpm_last_error(void) { return bpmgb::t_error.c_str(); }
 
 extern "C" unsigned long long bpm_launch_count(void) { return bpmgb::g_launches.load(); }
+
+extern "C" int bpm_host_ptr_mapped(const void* p) {
+  if (!p) return 0;
+  cudaPointerAttributes a;
+  if (cudaPointerGetAttributes(&a, p) != cudaSuccess) {
+    cudaGetLastError();
+    return 0;
+  }
+  return (a.type == cudaMemoryTypeHost && a.devicePointer == p) ? 1 : 0;
+}

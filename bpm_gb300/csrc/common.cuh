@@ -35,15 +35,36 @@ inline void count_launch(unsigned long long n = 1) { g_launches.fetch_add(n, std
   } while (0)
 
 // ---- complex helpers -------------------------------------------------------------------
+// Every multiply-add is written as an explicit fmaf: left implicit, the compiler may fuse
+// either product of a*b - c*d depending on the surrounding code, so the same formula could
+// round differently in two kernels. Spelled out, every kernel gets the same bits.
 __device__ __forceinline__ float2 cmul(float2 a, float2 b) {
-  return make_float2(a.x * b.x - a.y * b.y, a.x * b.y + a.y * b.x);
+  return make_float2(fmaf(a.x, b.x, -(a.y * b.y)), fmaf(a.x, b.y, a.y * b.x));
 }
 __device__ __forceinline__ float2 cadd(float2 a, float2 b) { return make_float2(a.x + b.x, a.y + b.y); }
 __device__ __forceinline__ float2 csub(float2 a, float2 b) { return make_float2(a.x - b.x, a.y - b.y); }
 __device__ __forceinline__ float2 cscale(float2 a, float s) { return make_float2(a.x * s, a.y * s); }
-__device__ __forceinline__ float cabs2(float2 a) { return a.x * a.x + a.y * a.y; }
+__device__ __forceinline__ float cabs2(float2 a) { return fmaf(a.x, a.x, a.y * a.y); }
+
+// ---- asynchronous global -> shared copies (cp.async) ------------------------------------
+// Each thread's copies complete with cp.async.wait_group, which waits for that thread's own
+// copies only (no spin on a flag); a barrier afterwards publishes them to the other threads.
+__device__ __forceinline__ void cp_async16(void* smem_dst, const void* gsrc) {
+  const unsigned s = (unsigned)__cvta_generic_to_shared(smem_dst);
+  asm volatile("cp.async.cg.shared.global [%0], [%1], 16;\n" ::"r"(s), "l"(gsrc) : "memory");
+}
+__device__ __forceinline__ void cp_async8(void* smem_dst, const void* gsrc) {
+  const unsigned s = (unsigned)__cvta_generic_to_shared(smem_dst);
+  asm volatile("cp.async.ca.shared.global [%0], [%1], 8;\n" ::"r"(s), "l"(gsrc) : "memory");
+}
+__device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;\n" ::: "memory"); }
+template <int PENDING>
+__device__ __forceinline__ void cp_async_wait() {
+  asm volatile("cp.async.wait_group %0;\n" ::"n"(PENDING) : "memory");
+}
 
 inline bool is_pow2(int n) { return n > 0 && (n & (n - 1)) == 0; }
+inline bool aligned16(const void* p) { return ((uintptr_t)p & 15) == 0; }
 
 inline size_t align256(size_t n) { return (n + 255) & ~size_t(255); }
 

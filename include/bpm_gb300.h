@@ -114,6 +114,13 @@ const char* bpm_last_error(void);
 /* Number of kernels this library has launched in the calling process (all threads). */
 unsigned long long bpm_launch_count(void);
 
+/* 1 if p is page-locked host memory that the current device reaches through the same
+ * address (cudaHostAlloc / cudaHostRegister under unified addressing), else 0. Such a
+ * buffer may be passed as bpm_request.out: the march then writes its output planes
+ * straight into host memory over the CPU-GPU link, with no staging copy. (No reference
+ * counterpart: the reference always reads its output back with a separate copy.) */
+int bpm_host_ptr_mapped(const void* p);
+
 /* Validate a grid description without touching the device (BPM_OK or an error). */
 int bpm_grid_check(const bpm_grid_desc* desc);
 
@@ -145,6 +152,17 @@ size_t bpm_workspace_bytes(const bpm_plan* plan, int batch, int group);
  * mask of dn slice z (reference quirk Q8). */
 int bpm_propagate(bpm_plan* plan, const bpm_request* req, void* workspace, size_t workspace_bytes,
                   void* stream);
+
+/* bpm_propagate whose output volume also lands in host memory while the march runs:
+ * req->out is the device volume; every time a group of fields has written another
+ * chunk_planes planes, a plan-owned copy stream moves them to host_out (same layout and
+ * element type as req->out: (batch, nz, ny, nx) with req->out_batch_stride). The copies
+ * overlap the rest of the march; `stream` waits for the last one. host_out should be
+ * page-locked for the copies to run asynchronously. Replaces the march + read-back of
+ * bpm/bpm/bpm_3d.py:_bpm_3d (:283-381, then u_g.get() at :388-391), with the read-back
+ * overlapped. */
+int bpm_propagate_to_host(bpm_plan* plan, const bpm_request* req, void* host_out, int chunk_planes,
+                          void* workspace, size_t workspace_bytes, void* stream);
 
 /* Allocation-free march, for callers that may not allocate device memory where they
  * march (a host that gives this library a fixed device budget and forbids it cudaMalloc,

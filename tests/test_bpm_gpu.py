@@ -273,3 +273,74 @@ def test_linearity_at_full_size(bpm):
     assert float(r) < 1e-5
     s = bpm.bpm_3d(size, (.1, .1, .1), u0=u0[1], dn=dn, return_full=False)
     assert torch.equal(s, a[1])
+
+
+def test_pipelined_kernels_match_warp_kernels(bpm, tmp_path):
+    """The pipelined persistent row/column kernels (BPM_GB300_KERNELS=pipe) against the
+    single-wave warp kernels (=warp), each in a child process, over the three mean modes,
+    f32 / f16 / complex dn, precomputed and on-the-fly masks: the same bits (every
+    multiply-add of the shared arithmetic is an explicit fmaf, so no kernel can round a
+    formula differently), and the pipelined path is deterministic."""
+    import os
+    import subprocess
+    import sys
+    here = os.path.dirname(os.path.abspath(__file__))
+    script = os.path.join(here, "_march_cases.py")
+    paths = {}
+    for tag, fam in (("pipe", "pipe"), ("pipe2", "pipe"), ("warp", "warp")):
+        paths[tag] = str(tmp_path / (tag + ".npz"))
+        subprocess.run([sys.executable, script, paths[tag]], check=True, timeout=600,
+                       env=dict(os.environ, BPM_GB300_KERNELS=fam))
+    A, A2, B = (np.load(paths[t]) for t in ("pipe", "pipe2", "warp"))
+    assert sorted(A.files) == sorted(B.files)
+    for k in A.files:
+        assert np.array_equal(A[k], A2[k]), k
+        assert np.array_equal(A[k], B[k]), k
+
+
+@pytest.mark.parametrize("nz,chunk,group,field", [(37, 16, 2, False), (1, 16, 3, True), (20, 1, 4, True),
+                                                  (33, 64, 0, False)])
+def test_streamed_host_out(bpm, nz, chunk, group, field):
+    """bpm_propagate_to_host: z-runs of every group's fields are copied to the page-locked
+    host buffer while the march goes on (chunk boundaries that do not divide nz, a single
+    plane, one-plane chunks, concurrent groups in several waves); the host volume equals
+    the device result bit for bit."""
+    import torch
+    from bpm_gb300.bpm3d import _run_streamed_to_host, _dn_kind, get_plan, precompute_mask, _h2d
+    from bpm_gb300 import _native as N
+    size = (64, 32, nz)
+    dn = random_spheres(64, 32, nz, 4, 17)
+    u0 = np.exp(1j * np.linspace(0, 5, 9 * 32 * 64)).reshape(9, 32, 64).astype(np.complex64)
+    want = bpm.bpm_3d_batched(size, (.1, .1, .1), u0=u0, dn=dn, return_field=field, group=group)
+    plan = get_plan(size, (.1, .1, .1), .5, 1., 0, "weighted", N.PROP_FUNCTIONAL, False)
+    kind, tdt = _dn_kind(dn, False)
+    dn_t = _h2d(dn, tdt, torch.device("cuda"))
+    u0_t = _h2d(u0, torch.complex64, torch.device("cuda"))
+    host = torch.full((9, nz, 32, 64), float("nan"), dtype=torch.complex64 if field else torch.float32,
+                      pin_memory=True)
+    _run_streamed_to_host(plan, u0_t, dn_t, kind, 0, N.OUT_FIELD if field else N.OUT_INTENSITY, (None, None),
+                          group, precompute_mask(plan, dn_t, kind), host, chunk_planes=chunk)
+    assert bool(np.array_equal(host.numpy(), want))
+
+
+def test_streamed_host_out_errors(bpm):
+    import ctypes
+    import torch
+    from bpm_gb300 import _native as N
+    from bpm_gb300.bpm3d import get_plan, _ptr
+    plan = get_plan((64, 32, 4), (.1, .1, .1), .5, 1., 0, "ignore", N.PROP_FUNCTIONAL, False)
+    u0 = torch.ones((1, 32, 64), dtype=torch.complex64, device="cuda")
+    host = torch.empty((1, 4, 32, 64), dtype=torch.float32, pin_memory=True)
+    ws = torch.empty(plan.workspace_bytes(1, 0), dtype=torch.uint8, device="cuda")
+    # out in host memory is refused (it must be the device volume)
+    req = N.Request(1, _ptr(u0), None, N.DN_NONE, 0, None, None, _ptr(host), N.OUT_INTENSITY, 4 * 32 * 64, None,
+                    None, None, 0, 0, None, 0, None)
+    rc = N.lib().bpm_propagate_to_host(plan.handle, ctypes.byref(req), ctypes.c_void_p(host.data_ptr()), 4, _ptr(ws),
+                                       ws.numel(), None)
+    assert rc == N.BPM_ERR_ARG
+    vol = torch.empty((1, 4, 32, 64), dtype=torch.float32, device="cuda")
+    req.out = vol.data_ptr()
+    assert N.lib().bpm_propagate_to_host(plan.handle, ctypes.byref(req), None, 4, _ptr(ws), ws.numel(),
+                                         None) == N.BPM_ERR_ARG
+    assert N.lib().bpm_propagate_to_host(plan.handle, ctypes.byref(req), ctypes.c_void_p(host.data_ptr()), 0,
+                                         _ptr(ws), ws.numel(), None) == N.BPM_ERR_ARG
