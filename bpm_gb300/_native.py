@@ -64,6 +64,7 @@ SIGNATURES = {
     "bpm_launch_count": (ctypes.c_ulonglong, []),
     "bpm_grid_check": (c_int, [ctypes.POINTER(GridDesc)]),
     "bpm_plan_create": (c_int, [ctypes.POINTER(GridDesc), ctypes.POINTER(c_vp)]),
+    "bpm_plan_derive": (c_int, [c_vp, c_int, ctypes.POINTER(c_vp)]),
     "bpm_plan_destroy": (c_int, [c_vp]),
     "bpm_group_size": (c_int, [c_vp, c_int, c_int]),
     "bpm_workspace_bytes": (c_size, [c_vp, c_int, c_int]),

@@ -82,7 +82,7 @@ class Plan:
     device (bpm_plan_create)."""
 
     def __init__(self, size, units, lam, n0, absorbing_width=0, mean_mode="weighted",
-                 prop_kind=N.PROP_FUNCTIONAL, use_fresnel_approx=False):
+                 prop_kind=N.PROP_FUNCTIONAL, use_fresnel_approx=False, base=None):
         if mean_mode not in N.MEAN_MODES:
             raise NotImplementedError("mean_mode  '%s' unknown" % mean_mode)
         Nx, Ny, Nz = (int(s) for s in size)
@@ -97,9 +97,13 @@ class Plan:
         L = N.lib()
         N.check(L.bpm_grid_check(ctypes.byref(self.desc)), "bpm_grid_check")
         self.device = _device()
+        self._base = base  # a derived plan shares (and keeps alive) its base's tables
         h = ctypes.c_void_p()
         with torch.cuda.device(self.device):
-            N.check(L.bpm_plan_create(ctypes.byref(self.desc), ctypes.byref(h)), "bpm_plan_create")
+            if base is not None:
+                N.check(L.bpm_plan_derive(base.handle, Nz, ctypes.byref(h)), "bpm_plan_derive")
+            else:
+                N.check(L.bpm_plan_create(ctypes.byref(self.desc), ctypes.byref(h)), "bpm_plan_create")
         self.handle = h
 
     def workspace_bytes(self, batch, group=0):
@@ -115,23 +119,40 @@ class Plan:
             self.handle = None
 
 
-_plans = OrderedDict()
-_PLAN_CACHE = 32
+_plans = OrderedDict()       # (grid incl. nz) -> Plan
+_bases = OrderedDict()       # (grid without nz) -> Plan that owns the device tables
+_PLAN_CACHE = 64
+_BASE_CACHE = 16
 
 
 def get_plan(size, units, lam, n0, absorbing_width=0, mean_mode="weighted",
              prop_kind=N.PROP_FUNCTIONAL, use_fresnel_approx=False):
-    key = (torch.cuda.current_device() if torch.cuda.is_available() else -1,
-           tuple(int(s) for s in size), tuple(float(u) for u in units), float(lam), float(n0),
-           int(absorbing_width), mean_mode, int(prop_kind), bool(use_fresnel_approx))
+    """Cached plan for this grid and physics. The device tables do not depend on Nz: one
+    base plan per (Nx, Ny, units, physics) builds them, and a request with another Nz gets
+    a derived plan (bpm_plan_derive) that shares them, created without any device
+    allocation or synchronisation."""
+    Nx, Ny, Nz = (int(s) for s in size)
+    dev = torch.cuda.current_device() if torch.cuda.is_available() else -1
+    rest = (tuple(float(u) for u in units), float(lam), float(n0), int(absorbing_width), mean_mode,
+            int(prop_kind), bool(use_fresnel_approx))
+    key = (dev, (Nx, Ny, Nz)) + rest
     p = _plans.get(key)
-    if p is None:
-        p = Plan(size, units, lam, n0, absorbing_width, mean_mode, prop_kind, use_fresnel_approx)
-        _plans[key] = p
-        while len(_plans) > _PLAN_CACHE:
-            _plans.popitem(last=False)
-    else:
+    if p is not None:
         _plans.move_to_end(key)
+        return p
+    bkey = (dev, (Nx, Ny)) + rest
+    base = _bases.get(bkey)
+    if base is None:
+        p = Plan(size, units, lam, n0, absorbing_width, mean_mode, prop_kind, use_fresnel_approx)
+        _bases[bkey] = p
+        while len(_bases) > _BASE_CACHE:
+            _bases.popitem(last=False)
+    else:
+        _bases.move_to_end(bkey)
+        p = Plan(size, units, lam, n0, absorbing_width, mean_mode, prop_kind, use_fresnel_approx, base=base)
+    _plans[key] = p
+    while len(_plans) > _PLAN_CACHE:
+        _plans.popitem(last=False)
     return p
 
 

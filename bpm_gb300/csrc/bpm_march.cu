@@ -60,6 +60,8 @@ struct bpm_plan {
   cudaStream_t copy;
   cudaEvent_t ev_ready[4], ev_copied;
   int max_pitch;
+  // false for a plan made by bpm_plan_derive: the device tables belong to its base plan
+  bool owns_tables;
 };
 
 // field groups a batch may march at the same time (one workspace slot each)
@@ -1857,6 +1859,19 @@ extern "C" int bpm_grid_check(const bpm_grid_desc* d) {
   return BPM_OK;
 }
 
+// the plan's own streams and events (no device synchronisation)
+static cudaError_t create_plan_streams(bpm_plan* pl) {
+  cudaError_t e;
+  for (int i = 0; i < kMaxConcurrentGroups; i++) {
+    if ((e = cudaStreamCreateWithFlags(&pl->aux[i], cudaStreamNonBlocking))) return e;
+    if ((e = cudaEventCreateWithFlags(&pl->ev_join[i], cudaEventDisableTiming))) return e;
+    if ((e = cudaEventCreateWithFlags(&pl->ev_ready[i], cudaEventDisableTiming))) return e;
+  }
+  if ((e = cudaEventCreateWithFlags(&pl->ev_fork, cudaEventDisableTiming))) return e;
+  if ((e = cudaStreamCreateWithFlags(&pl->copy, cudaStreamNonBlocking))) return e;
+  return cudaEventCreateWithFlags(&pl->ev_copied, cudaEventDisableTiming);
+}
+
 extern "C" int bpm_plan_create(const bpm_grid_desc* d, bpm_plan** out) {
   int rc = bpm_grid_check(d);
   if (rc) return rc;
@@ -1865,6 +1880,7 @@ extern "C" int bpm_plan_create(const bpm_grid_desc* d, bpm_plan** out) {
   bpm_plan* pl = new bpm_plan();
   memset(pl, 0, sizeof(*pl));
   pl->d = *d;
+  pl->owns_tables = true;
   const int nx = d->nx, ny = d->ny;
   pl->k0 = 2. * M_PI / d->lam;
   pl->k0f = (float)pl->k0;
@@ -1933,25 +1949,50 @@ extern "C" int bpm_plan_create(const bpm_grid_desc* d, bpm_plan** out) {
   count_launch();
   if ((e = cudaDeviceSynchronize())) return fail(e, "build_tables_kernel");
   prepare_kernels(nx, ny);
-  for (int i = 0; i < kMaxConcurrentGroups; i++) {
-    if ((e = cudaStreamCreateWithFlags(&pl->aux[i], cudaStreamNonBlocking))) return fail(e, "cudaStreamCreate");
-    if ((e = cudaEventCreateWithFlags(&pl->ev_join[i], cudaEventDisableTiming))) return fail(e, "cudaEventCreate");
-    if ((e = cudaEventCreateWithFlags(&pl->ev_ready[i], cudaEventDisableTiming))) return fail(e, "cudaEventCreate");
-  }
-  if ((e = cudaEventCreateWithFlags(&pl->ev_fork, cudaEventDisableTiming))) return fail(e, "cudaEventCreate");
-  if ((e = cudaStreamCreateWithFlags(&pl->copy, cudaStreamNonBlocking))) return fail(e, "cudaStreamCreate");
-  if ((e = cudaEventCreateWithFlags(&pl->ev_copied, cudaEventDisableTiming))) return fail(e, "cudaEventCreate");
+  if ((e = create_plan_streams(pl))) return fail(e, "stream/event creation");
   if ((e = cudaDeviceGetAttribute(&pl->max_pitch, cudaDevAttrMaxPitch, pl->device))) return fail(e, "cudaDeviceGetAttribute");
+  *out = pl;
+  return BPM_OK;
+}
+
+extern "C" int bpm_plan_derive(const bpm_plan* base, int nz, bpm_plan** out) {
+  clear_error();
+  if (!base || !out) { set_error("base or out is NULL"); return BPM_ERR_ARG; }
+  *out = nullptr;
+  bpm_grid_desc d = base->d;
+  d.nz = nz;
+  int rc = bpm_grid_check(&d);
+  if (rc) return rc;
+  bpm_plan* pl = new bpm_plan(*base);  // the same device tables, read only
+  pl->d = d;
+  pl->owns_tables = false;
+  for (int i = 0; i < kMaxConcurrentGroups; i++) pl->aux[i] = nullptr, pl->ev_join[i] = pl->ev_ready[i] = nullptr;
+  pl->ev_fork = pl->ev_copied = nullptr;
+  pl->copy = nullptr;
+  cudaError_t e = create_plan_streams(pl);
+  if (e) {
+    bpm_plan_destroy(pl);
+    return cuda_fail(e, "stream/event creation");
+  }
   *out = pl;
   return BPM_OK;
 }
 
 extern "C" int bpm_plan_destroy(bpm_plan* pl) {
   if (!pl) return BPM_OK;
-  cudaFree(pl->tw_x);
-  cudaFree(pl->tw_y);
-  cudaFree(pl->wtw_x);
-  cudaFree(pl->wtw_y);
+  if (pl->owns_tables) {
+    cudaFree(pl->tw_x);
+    cudaFree(pl->tw_y);
+    cudaFree(pl->wtw_x);
+    cudaFree(pl->wtw_y);
+    cudaFree(pl->kx2);
+    cudaFree(pl->ky2);
+    cudaFree(pl->taper);
+    cudaFree(pl->H);
+    cudaFree(pl->Ht);
+    cudaFree(pl->sw);
+    cudaFree(pl->gw);
+  }
   for (int i = 0; i < kMaxConcurrentGroups; i++) {
     if (pl->aux[i]) cudaStreamDestroy(pl->aux[i]);
     if (pl->ev_join[i]) cudaEventDestroy(pl->ev_join[i]);
@@ -1960,13 +2001,6 @@ extern "C" int bpm_plan_destroy(bpm_plan* pl) {
   if (pl->ev_fork) cudaEventDestroy(pl->ev_fork);
   if (pl->copy) cudaStreamDestroy(pl->copy);
   if (pl->ev_copied) cudaEventDestroy(pl->ev_copied);
-  cudaFree(pl->kx2);
-  cudaFree(pl->ky2);
-  cudaFree(pl->taper);
-  cudaFree(pl->H);
-  cudaFree(pl->Ht);
-  cudaFree(pl->sw);
-  cudaFree(pl->gw);
   delete pl;
   return BPM_OK;
 }

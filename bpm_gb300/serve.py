@@ -5,9 +5,11 @@ returns a future. A scheduler thread
   * admits requests in arrival order while their HBM footprint (inputs, outputs and
     workspace, estimated before launch) fits the budget and an execution slot is free;
   * merges admitted BPM requests that share a grid and physics (size, units, lam, n0,
-    mean mode, taper, dn dtype) into one batched launch (per-field dn volumes,
-    bpm_propagate with dn_batch_stride), so a late arrival joins the next launch
-    instead of waiting for a whole queue to drain;
+    mean mode, taper, dn dtype) into one batched launch, so a late arrival joins the
+    next launch instead of waiting for a whole queue to drain. Fields whose dn is the
+    same resident CUDA volume march it in place (no copy; for several fields its phase
+    masks are computed once); other dn volumes are gathered into one per-field buffer
+    (bpm_propagate with dn_batch_stride);
   * runs every launch on its own CUDA stream from a pool, so requests of different grid
     sizes and PSFs overlap on the device, and retires launches as their CUDA events
     complete, returning memory and slots to admission.
@@ -30,7 +32,7 @@ import numpy as np
 import torch
 
 from . import _native as N
-from .bpm3d import _dn_kind, _ptr, get_plan
+from .bpm3d import _dn_kind, _ptr, get_plan, precompute_mask
 from .psf import _debye
 
 __all__ = ["BpmRequest", "PsfRequest", "Server"]
@@ -40,7 +42,8 @@ __all__ = ["BpmRequest", "PsfRequest", "Server"]
 class BpmRequest:
     """One bpm_3d call: size=(Nx, Ny, Nz), units, lam, n0, u0 (Ny, Nx) or None, dn
     (Nz, Ny, Nx) or None, mean_mode ("ignore" or "weighted"; "simple" is not merged),
-    absorbing_width, return_field, return_full, host (return numpy)."""
+    absorbing_width, return_field, return_full, host (return numpy). A contiguous CUDA
+    dn tensor is read in place until the request completes: do not modify it meanwhile."""
     size: tuple
     units: tuple
     lam: float = .5
@@ -280,11 +283,21 @@ class Server:
             else:
                 u0[i].copy_(torch.as_tensor(r.u0).to(torch.complex64), non_blocking=True)
         kind, tdt = _dn_kind(r0.dn, False)
-        dn = None
+        dn, dn_stride, mask = None, 0, None
         if kind != N.DN_NONE:
-            dn = torch.empty((B, Nz, Ny, Nx), dtype=tdt, device=dev)
-            for i, r in enumerate(reqs):
-                dn[i].copy_(torch.as_tensor(r.dn).to(tdt), non_blocking=True)
+            vols = [r.dn for r in reqs]
+            if all(_device_volume(v, tdt, (Nz, Ny, Nx), dev) for v in vols) and \
+                    all(v.data_ptr() == vols[0].data_ptr() for v in vols):
+                # every field reads the same resident volume: march it in place, no copy;
+                # several fields share its phase masks, computed once
+                dn = vols[0]
+                if B >= 2:
+                    mask = precompute_mask(plan, dn, kind)
+            else:
+                dn = torch.empty((B, Nz, Ny, Nx), dtype=tdt, device=dev)
+                for i, r in enumerate(reqs):
+                    dn[i].copy_(torch.as_tensor(r.dn).to(tdt), non_blocking=True)
+                dn_stride = Nz * Ny * Nx
         ok = (N.OUT_FIELD if r0.return_field else N.OUT_INTENSITY) if r0.return_full else N.OUT_NONE
         out = None
         if ok == N.OUT_FIELD:
@@ -294,14 +307,21 @@ class Server:
         last = torch.empty((B, Ny, Nx), dtype=torch.complex64, device=dev)
         wsb = plan.workspace_bytes(B, 0)
         ws = torch.empty(wsb, dtype=torch.uint8, device=dev)
-        req = N.Request(B, _ptr(u0), _ptr(dn), kind, Nz * Ny * Nx if dn is not None else 0, None, None,
-                        _ptr(out), ok, Nz * Ny * Nx, _ptr(last), None, None, 0, 0)
+        req = N.Request(B, _ptr(u0), _ptr(dn), kind, dn_stride, None, None,
+                        _ptr(out), ok, Nz * Ny * Nx, _ptr(last), None, None, 0, 0, None, 0, _ptr(mask))
         N.check(N.lib().bpm_propagate(plan.handle, ctypes.byref(req), _ptr(ws), wsb,
                                       ctypes.c_void_p(stream.cuda_stream)), "bpm_propagate")
-        la.keep += [u0, dn, ws]
+        la.keep += [u0, dn, ws, mask]
         if r0.return_full:
             return [out[i] for i in range(B)]
         return [last[i] if r0.return_field else (last[i].abs() ** 2) for i in range(B)]
+
+
+def _device_volume(v, dtype, shape, dev):
+    """v can be marched in place: a contiguous, 16-byte aligned CUDA tensor of the request's
+    dn dtype and (Nz, Ny, Nx) shape on the server's device."""
+    return (torch.is_tensor(v) and v.is_cuda and v.device == dev and v.dtype == dtype and v.is_contiguous()
+            and tuple(v.shape) == tuple(shape) and v.data_ptr() % 16 == 0)
 
 
 def _to_host(res):

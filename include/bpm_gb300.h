@@ -131,7 +131,13 @@ int bpm_grid_check(const bpm_grid_desc* desc);
  * + _bpm3d_ocl.py:_setup_impl (:35-56). */
 int bpm_plan_create(const bpm_grid_desc* desc, bpm_plan** out);
 
-/* Release a plan and its device tables. */
+/* A plan for the same grid with another number of planes nz, sharing the device tables
+ * of `base` (none of them depends on nz): no device allocation and no synchronisation,
+ * only the plan's own streams and events are created. `base` must outlive it. (No
+ * reference counterpart: the reference rebuilds its propagator for every bpm_3d call.) */
+int bpm_plan_derive(const bpm_plan* base, int nz, bpm_plan** out);
+
+/* Release a plan: its streams and events, and its device tables unless it was derived. */
 int bpm_plan_destroy(bpm_plan* plan);
 
 /* Fields the march advances together per kernel launch for a request of `batch` fields

@@ -344,3 +344,32 @@ def test_streamed_host_out_errors(bpm):
                                          None) == N.BPM_ERR_ARG
     assert N.lib().bpm_propagate_to_host(plan.handle, ctypes.byref(req), ctypes.c_void_p(host.data_ptr()), 0,
                                          _ptr(ws), ws.numel(), None) == N.BPM_ERR_ARG
+
+
+def test_derived_plan_equals_fresh_plan(bpm):
+    """bpm_plan_derive: a plan for another nz sharing the base plan's tables marches exactly
+    like a plan created from scratch for that nz (get_plan derives it from the cached base)."""
+    import ctypes
+    import torch
+    from bpm_gb300 import _native as N
+    from bpm_gb300.bpm3d import Plan, get_plan, _ptr
+    size0, units = (128, 64, 9), (.1, .11, .12)
+    base = get_plan(size0, units, .5, 1.33, 3, "weighted")
+    derived = get_plan((128, 64, 23), units, .5, 1.33, 3, "weighted")
+    assert derived._base is base
+    fresh = Plan((128, 64, 23), units, .5, 1.33, 3, "weighted")
+    dn = torch.from_numpy(random_spheres(128, 64, 23, 5, 31)).cuda()
+    u0 = torch.ones((2, 64, 128), dtype=torch.complex64, device="cuda")
+    outs = []
+    for plan in (derived, fresh):
+        out = torch.empty((2, 23, 64, 128), dtype=torch.float32, device="cuda")
+        ws = torch.empty(plan.workspace_bytes(2, 0), dtype=torch.uint8, device="cuda")
+        req = N.Request(2, _ptr(u0), _ptr(dn), N.DN_F32, 0, None, None, _ptr(out), N.OUT_INTENSITY,
+                        23 * 64 * 128, None, None, None, 0, 0, None, 0, None)
+        N.check(N.lib().bpm_propagate(plan.handle, ctypes.byref(req), _ptr(ws), ws.numel(),
+                                      ctypes.c_void_p(torch.cuda.current_stream().cuda_stream)))
+        outs.append(out)
+    torch.cuda.synchronize()
+    assert torch.equal(outs[0], outs[1])
+    h = ctypes.c_void_p()
+    assert N.lib().bpm_plan_derive(base.handle, 0, ctypes.byref(h)) == N.BPM_ERR_SHAPE
