@@ -61,6 +61,7 @@ enum MirrorKind { MIR_STD = 0, MIR_GAUSS = 1 };
 struct DebyeLayout {
   size_t si, ct, wf, kr, trig, J, E, I, total;
   int T, M, Zo, nxo, nyo, nzo;
+  int Mp, Zp;  // row pitches of J (radii, multiple of 4) and E (planes, even): 16-byte rows
 };
 
 DebyeLayout debye_layout(const debye_desc* d, bool gauss = false) {
@@ -77,14 +78,16 @@ DebyeLayout debye_layout(const debye_desc* d, bool gauss = false) {
   L.T = (d->n_na / 2) * (d->n_integration_steps + 1);
   L.M = L.nxo * L.nyo;
   L.Zo = L.nzo;
+  L.Mp = (L.M + 3) & ~3;
+  L.Zp = (L.Zo + 1) & ~1;
   size_t off = 0;
   L.si = off; off += align256(sizeof(double) * L.T);
   L.ct = off; off += align256(sizeof(double) * L.T);
   L.wf = off; off += align256(sizeof(float) * 3 * L.T);
   L.kr = off; off += align256(sizeof(double) * L.M);
   L.trig = off; off += align256(sizeof(float) * 4 * L.M);
-  L.J = off; off += align256(sizeof(float) * 3 * (size_t)L.T * L.M);
-  L.E = off; off += align256(sizeof(float2) * (size_t)L.T * L.Zo);
+  L.J = off; off += align256(sizeof(float) * 3 * (size_t)L.T * L.Mp);
+  L.E = off; off += align256(sizeof(float2) * (size_t)L.T * L.Zp);
   L.I = off; off += align256(sizeof(float2) * 3 * (size_t)L.Zo * L.M);
   L.total = off;
   return L;
@@ -142,10 +145,15 @@ __global__ void debye_radii_kernel(OctGeom g, double k, double* kr, float* trig,
 }
 
 // E(t, z) = exp(i kz cos t), phase formed and reduced in FP64
-__global__ void debye_phase_kernel(int Zo, float z1, float z2, double k, const double* ct, float2* E, int T) {
+__global__ void debye_phase_kernel(int Zo, int Zp, float z1, float z2, double k, const double* ct, float2* E,
+                                   int T) {
   int idx = blockIdx.x * blockDim.x + threadIdx.x;
-  if (idx >= T * Zo) return;
-  const int t = idx / Zo, z = idx - t * Zo;
+  if (idx >= T * Zp) return;
+  const int t = idx / Zp, z = idx - t * Zp;
+  if (z >= Zo) {  // row padding
+    E[idx] = make_float2(0.f, 0.f);
+    return;
+  }
   const double kz = k * (double)(Zo == 1 ? z1 : coord_f32(z, z1, z2, Zo));
   double s, c;
   sincos(kz * ct[t], &s, &c);
@@ -172,30 +180,62 @@ __device__ __forceinline__ float bessel_j2(float x, float j0, float j1) {
 }
 
 // A_n(t, m) = p_n(t) J_n(kr_m sin t_t)
-__global__ void debye_bessel_kernel(int T, int M, const double* si, const double* kr, const float* wf, float* J) {
+__global__ void debye_bessel_kernel(int T, int M, int Mp, const double* si, const double* kr, const float* wf,
+                                    float* J) {
   const int m = blockIdx.x * blockDim.x + threadIdx.x;
   const int t = blockIdx.y;
-  if (m >= M) return;
+  if (m >= Mp) return;
+  const size_t TM = (size_t)T * Mp, o = (size_t)t * Mp + m;
+  if (m >= M) {  // row padding
+    J[o] = J[TM + o] = J[2 * TM + o] = 0.f;
+    return;
+  }
   const float x = (float)(kr[m] * si[t]);
   const float j0 = j0f(x), j1 = j1f(x);
   const float j2 = bessel_j2(x, j0, j1);
-  const size_t TM = (size_t)T * M, o = (size_t)t * M + m;
   J[o] = wf[t] * j0;
   J[TM + o] = wf[T + t] * j1;
   J[2 * TM + o] = wf[2 * T + t] * j2;
 }
 
 // I_n(z, m) = sum_t A_n(t, m) E(t, z): tile of 64 radii x 32 planes per block, each thread
-// owning 4 radii x 2 planes x 3 components.
+// owning 4 radii x 2 planes x 3 components. The node slices of A and E are double-buffered
+// in shared memory: while the block multiplies slice k, cp.async fetches slice k+1 (rows
+// past the last node, radius or plane are zero-filled), so the loads of one slice hide
+// behind the arithmetic of the previous one.
 constexpr int AM = 64, AZ = 32, AT = 16;
+constexpr int ACC_STAGE_F = 3 * AT * AM + 2 * AT * AZ;  // floats per stage: A slice, E slice
+constexpr size_t ACC_SMEM = 2 * ACC_STAGE_F * sizeof(float);
 
-__global__ void __launch_bounds__(256) debye_accum_kernel(int T, int M, int Zo, const float* __restrict__ J,
-                                                          const float2* __restrict__ E, float2* __restrict__ I) {
-  __shared__ __align__(16) float Js[3][AT][AM];
-  __shared__ __align__(16) float2 Es[AT][AZ];
+__global__ void __launch_bounds__(256, 2) debye_accum_kernel(int T, int M, int Mp, int Zo, int Zp,
+                                                             const float* __restrict__ J,
+                                                             const float2* __restrict__ E,
+                                                             float2* __restrict__ I) {
+  extern __shared__ __align__(16) float acc_smem[];
   const int tid = threadIdx.x;
   const int tm = tid & 15, tz = tid >> 4;
   const int m0 = blockIdx.x * AM, z0 = blockIdx.y * AZ;
+  const size_t TM = (size_t)T * Mp;
+  // one slice of nodes [t0, t0 + AT) into stage st: A rows are 16 pieces of 16 bytes (64
+  // radii), E rows 16 pieces (32 planes of complex64)
+  auto issue = [&](int st, int t0) {
+    float* Js = acc_smem + st * ACC_STAGE_F;
+    float* Es = Js + 3 * AT * AM;
+    for (int c = tid; c < 3 * AT * 16; c += 256) {
+      const int n = c / (AT * 16), r = c - n * AT * 16;
+      const int tt = r >> 4, q = r & 15;
+      const int t = t0 + tt, m = m0 + q * 4;
+      const bool ok = t < T && m < Mp;
+      cp_async16_zfill(Js + (n * AT + tt) * AM + q * 4, ok ? J + n * TM + (size_t)t * Mp + m : J, ok ? 16 : 0);
+    }
+    for (int c = tid; c < AT * 16; c += 256) {
+      const int tt = c >> 4, q = c & 15;
+      const int t = t0 + tt, z = z0 + q * 2;
+      const bool ok = t < T && z < Zp;
+      cp_async16_zfill(Es + (tt * AZ + q * 2) * 2, ok ? E + (size_t)t * Zp + z : E, ok ? 16 : 0);
+    }
+    cp_async_commit();
+  };
   float2 acc[3][4][2];
 #pragma unroll
   for (int n = 0; n < 3; n++)
@@ -203,27 +243,23 @@ __global__ void __launch_bounds__(256) debye_accum_kernel(int T, int M, int Zo, 
     for (int a = 0; a < 4; a++)
 #pragma unroll
       for (int b = 0; b < 2; b++) acc[n][a][b] = make_float2(0.f, 0.f);
-  const size_t TM = (size_t)T * M;
-  for (int t0 = 0; t0 < T; t0 += AT) {
-    for (int e = tid; e < 3 * AT * AM; e += 256) {
-      const int n = e / (AT * AM), r = e - n * AT * AM;
-      const int tt = r / AM, mm = r - tt * AM;
-      const int t = t0 + tt, m = m0 + mm;
-      Js[n][tt][mm] = (t < T && m < M) ? J[n * TM + (size_t)t * M + m] : 0.f;
-    }
-    for (int e = tid; e < AT * AZ; e += 256) {
-      const int tt = e / AZ, zz = e - tt * AZ;
-      const int t = t0 + tt, z = z0 + zz;
-      Es[tt][zz] = (t < T && z < Zo) ? E[(size_t)t * Zo + z] : make_float2(0.f, 0.f);
-    }
+  issue(0, 0);
+  for (int k = 0, t0 = 0; t0 < T; k++, t0 += AT) {
+    if (t0 + AT < T)
+      issue((k + 1) & 1, t0 + AT);
+    else
+      cp_async_commit();  // keep one group per iteration
+    cp_async_wait<1>();   // slice k has landed (slice k+1 may be in flight)
     __syncthreads();
+    const float* Js = acc_smem + (k & 1) * ACC_STAGE_F;
+    const float2* Es = reinterpret_cast<const float2*>(Js + 3 * AT * AM);
 #pragma unroll 4
     for (int tt = 0; tt < AT; tt++) {
-      const float4 e4 = *reinterpret_cast<const float4*>(&Es[tt][tz * 2]);
+      const float4 e4 = *reinterpret_cast<const float4*>(&Es[tt * AZ + tz * 2]);
       const float2 ev[2] = {make_float2(e4.x, e4.y), make_float2(e4.z, e4.w)};
 #pragma unroll
       for (int n = 0; n < 3; n++) {
-        const float4 j4 = *reinterpret_cast<const float4*>(&Js[n][tt][tm * 4]);
+        const float4 j4 = *reinterpret_cast<const float4*>(&Js[(n * AT + tt) * AM + tm * 4]);
         const float jv[4] = {j4.x, j4.y, j4.z, j4.w};
 #pragma unroll
         for (int a = 0; a < 4; a++)
@@ -234,8 +270,9 @@ __global__ void __launch_bounds__(256) debye_accum_kernel(int T, int M, int Zo, 
           }
       }
     }
-    __syncthreads();
+    __syncthreads();  // this stage is refilled two slices later
   }
+  cp_async_wait<0>();
   const size_t ZM = (size_t)Zo * M;
 #pragma unroll
   for (int n = 0; n < 3; n++)
@@ -490,11 +527,17 @@ int run_octant(const debye_desc* d, bool gauss, double sig, float* u, void* ex, 
   BPM_LAUNCH_CHECK("debye_nodes_kernel");
   debye_radii_kernel<<<(L.M + 127) / 128, 128, 0, s>>>(g, k, kr, trig, L.M);
   BPM_LAUNCH_CHECK("debye_radii_kernel");
-  debye_phase_kernel<<<(L.T * L.Zo + 127) / 128, 128, 0, s>>>(L.Zo, g.z1, g.z2, k, ct, E, L.T);
+  debye_phase_kernel<<<(L.T * L.Zp + 127) / 128, 128, 0, s>>>(L.Zo, L.Zp, g.z1, g.z2, k, ct, E, L.T);
   BPM_LAUNCH_CHECK("debye_phase_kernel");
-  debye_bessel_kernel<<<dim3((L.M + 127) / 128, L.T), 128, 0, s>>>(L.T, L.M, si, kr, wf, J);
+  debye_bessel_kernel<<<dim3((L.Mp + 127) / 128, L.T), 128, 0, s>>>(L.T, L.M, L.Mp, si, kr, wf, J);
   BPM_LAUNCH_CHECK("debye_bessel_kernel");
-  debye_accum_kernel<<<dim3((L.M + AM - 1) / AM, (L.Zo + AZ - 1) / AZ), 256, 0, s>>>(L.T, L.M, L.Zo, J, E, I);
+  static bool attr = false;
+  if (!attr) {
+    cudaFuncSetAttribute(debye_accum_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)ACC_SMEM);
+    attr = true;
+  }
+  debye_accum_kernel<<<dim3((L.M + AM - 1) / AM, (L.Zo + AZ - 1) / AZ), 256, ACC_SMEM, s>>>(L.T, L.M, L.Mp, L.Zo,
+                                                                                          L.Zp, J, E, I);
   BPM_LAUNCH_CHECK("debye_accum_kernel");
   if (u || ex || ey || ez) {
     const dim3 grid((d->nx + 127) / 128, d->ny, d->nz);
@@ -562,7 +605,7 @@ int run_points(const debye_desc* d, bool grid, double zplane, const float* xs, c
     a.x2 = (float)((double)(d->nx - d->nx / 2) * d->dx);
     a.y1 = (float)(-(double)(d->ny / 2) * d->dy);
     a.y2 = (float)((double)(d->ny - d->ny / 2) * d->dy);
-    debye_phase_kernel<<<(L.T + 127) / 128, 128, 0, s>>>(1, (float)zplane, 0.f, k, ct, E, L.T);
+    debye_phase_kernel<<<(L.T + 127) / 128, 128, 0, s>>>(1, 1, (float)zplane, 0.f, k, ct, E, L.T);
     BPM_LAUNCH_CHECK("debye_phase_kernel");
     debye_points_kernel<true><<<(unsigned)blocks, PT_THREADS, 0, s>>>(a, nullptr, nullptr, nullptr, si, ct, wf, E,
                                                                       u, static_cast<float2*>(ex),
