@@ -46,38 +46,71 @@ struct WarpFft {
   static constexpr int TW = wtw_size(N);    // stage-ordered twiddle entries
 };
 
+// Exchange-buffer addressing. Every index a stage touches splits exactly into a per-lane
+// part (computed once) and a compile-time offset, so each shared-memory access is one
+// instruction with an immediate offset instead of recomputing p + p/16 per access.
+//   loads:  wpad(q*32 + t + r*(N/RS))              = (t + t/16) + wpad(q*32 + r*N/RS)
+//   stores: wpad((j/NS)*NS*RS + j%NS + r*NS), j = q*32 + t
+//           NS >= 32: (t + t/16) + wpad((q*32/NS)*NS*RS + (q*32)%NS + r*NS)
+//           NS <  32: B + (((t/NS)*NS*RS) >> 4) + wpad(q*32*RS) + r*NS + ((r*NS) >> 4),
+//                     B = (t/NS)*NS*RS + t%NS
+// (warp_index_check verifies both against the direct formula for every lane at compile time.)
+__host__ __device__ constexpr int wpad_c(int p) { return p + (p >> 4); }
+__host__ __device__ constexpr int ld_lane(int t) { return t + (t >> 4); }
+__host__ __device__ constexpr int ld_off(int N, int RS, int q, int r) { return wpad_c(q * 32 + r * (N / RS)); }
+__host__ __device__ constexpr int st_lane(int RS, int NS, int t) {
+  return NS >= 32 ? t + (t >> 4) : (t / NS) * NS * RS + t % NS + (((t / NS) * NS * RS) >> 4);
+}
+__host__ __device__ constexpr int st_off(int RS, int NS, int q, int r) {
+  return NS >= 32 ? wpad_c((q * 32 / NS) * NS * RS + (q * 32) % NS + r * NS)
+                  : wpad_c(q * 32 * RS) + r * NS + ((r * NS) >> 4);
+}
+__host__ __device__ constexpr bool warp_index_check(int N, int RS, int NS) {
+  const int Q = (N / 32) / RS;
+  for (int t = 0; t < 32; t++)
+    for (int q = 0; q < Q; q++)
+      for (int r = 0; r < RS; r++) {
+        if (ld_lane(t) + ld_off(N, RS, q, r) != wpad_c(q * 32 + t + r * (N / RS))) return false;
+        const int j = q * 32 + t;
+        if (st_lane(RS, NS, t) + st_off(RS, NS, q, r) != wpad_c((j / NS) * NS * RS + j % NS + r * NS)) return false;
+      }
+  return true;
+}
+
 template <int N, int RS, int NS, bool INV, bool FIRST, bool LAST>
 __device__ __forceinline__ void warp_stage(float2 (&v)[N / 32], float2* buf, const float2* __restrict__ tw,
                                            int t) {
   constexpr int E = N / 32;
   constexpr int Q = E / RS;                 // butterflies per lane
-  constexpr int STRIDE_IN = N / RS;
   constexpr int TWOFF = wtw_offset(N, NS);  // this stage's twiddle block
+  static_assert(warp_index_check(N, RS, NS), "exchange-buffer index split");
   float2 a[E];
+  if constexpr (FIRST) {
 #pragma unroll
-  for (int q = 0; q < Q; q++) {
+    for (int q = 0; q < Q; q++)
 #pragma unroll
-    for (int r = 0; r < RS; r++) {
-      if constexpr (FIRST)
-        a[q * RS + r] = v[q + r * Q];
-      else
-        a[q * RS + r] = buf[wpad(q * 32 + t + r * STRIDE_IN)];
-    }
+      for (int r = 0; r < RS; r++) a[q * RS + r] = v[q + r * Q];
+  } else {
+    const float2* bl = buf + ld_lane(t);
+#pragma unroll
+    for (int q = 0; q < Q; q++)
+#pragma unroll
+      for (int r = 0; r < RS; r++) a[q * RS + r] = bl[ld_off(N, RS, q, r)];
   }
+  if constexpr (NS > 1) {
+    // twiddle W^{(j mod NS) r N/(NS RS)} for j = q*32 + t: entry (r-1)*NS + jm of the stage
+    const float2* twl = tw + TWOFF + (NS >= 32 ? t : (t & (NS - 1)));
 #pragma unroll
-  for (int q = 0; q < Q; q++) {
-    const int j = q * 32 + t;
-    if constexpr (NS > 1) {
-      const int jm = j & (NS - 1);
+    for (int q = 0; q < Q; q++)
 #pragma unroll
       for (int r = 1; r < RS; r++) {
-        float2 w = tw[TWOFF + (r - 1) * NS + jm];
+        float2 w = twl[(r - 1) * NS + (NS >= 32 ? (q * 32) % NS : 0)];
         if (INV) w.y = -w.y;
         a[q * RS + r] = cmul(a[q * RS + r], w);
       }
-    }
-    Dft<RS, INV>::run(&a[q * RS]);
   }
+#pragma unroll
+  for (int q = 0; q < Q; q++) Dft<RS, INV>::run(&a[q * RS]);
   if constexpr (LAST) {
 #pragma unroll
     for (int q = 0; q < Q; q++)
@@ -85,14 +118,11 @@ __device__ __forceinline__ void warp_stage(float2 (&v)[N / 32], float2* buf, con
       for (int r = 0; r < RS; r++) v[q + r * (NS / 32)] = a[q * RS + r];
   } else {
     __syncwarp();  // every lane is done reading the buffer (previous stage or transform)
+    float2* bs = buf + st_lane(RS, NS, t);
 #pragma unroll
-    for (int q = 0; q < Q; q++) {
-      const int j = q * 32 + t;
-      const int jm = j & (NS - 1);
-      const int base = (j / NS) * NS * RS + jm;
+    for (int q = 0; q < Q; q++)
 #pragma unroll
-      for (int r = 0; r < RS; r++) buf[wpad(base + r * NS)] = a[q * RS + r];
-    }
+      for (int r = 0; r < RS; r++) bs[st_off(RS, NS, q, r)] = a[q * RS + r];
     __syncwarp();
   }
 }
