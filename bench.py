@@ -310,7 +310,7 @@ def bench_ours(args, rank, world, local_rank):
         "batched_over_plain": value / world / plain_value,
         "kernels_ms": {"row_pass": t_row, "col_fwd_reduce": t_cr, "col_inv": t_cp,
                        "per_launch_group_fields": grp, "sum_over_step_ms": t_step_sum},
-        "roofline": {"bound": "hbm", "kernel": "row_pass_kernel<512>", "achieved": row_gbs,
+        "roofline": {"bound": "hbm", "kernel": "row_shared_kernel<512, 1>", "achieved": row_gbs,
                      "peak": hbm_peak, "unit": "GB/s", "frac": row_gbs / hbm_peak,
                      "traffic": traffic, "peak_kind": peak_kind + " (MEASURED_PEAKS.json hbm_gbs)",
                      "algorithmic_bytes_per_launch": row_bytes,
