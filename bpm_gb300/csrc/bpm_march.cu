@@ -28,6 +28,8 @@
 #include <string>
 #include <vector>
 
+#include <cooperative_groups.h>
+
 #include "common.cuh"
 #include "fft_tile.cuh"
 #include "warp_fft.cuh"
@@ -1152,6 +1154,206 @@ col_pipe_kernel(ColParams p, int ntiles) {
 }
 
 // ---------------------------------------------------------------------------------------
+// Whole-march cluster kernel for square grids N = 64, 128, 256: one thread-block cluster of
+// C = N/32 blocks per field holds the field in distributed shared memory for all nz steps.
+// Block c owns rows [32c, 32c+32) (row slab R, 32 x N) and columns [32c, 32c+32) (column
+// slab K, N x 33 with one pad column). A step: cluster barrier (row slabs ready) -> every
+// block gathers its column slab from the other blocks' row slabs through DSMEM -> column
+// FFT, [weighted: per-16-column-tile partial sums, exchanged through DSMEM after a cluster
+// barrier], propagator, inverse column FFT -> cluster barrier (column slabs ready) -> every
+// block gathers its row slab back -> inverse row FFT, phase mask, plane output, forward row
+// FFT. The field never leaves the chip; one launch runs the whole march of every field of
+// the request. The FFTs, pointwise helpers and the weighted partial sums (same 16-column
+// tiles, same 512-thread element order, same fixed-order total) are those of the warp
+// kernels, so the results are the same bits. Cluster barriers are hardware barriers over
+// blocks the launch co-schedules; a final barrier keeps every block's shared memory alive
+// until the others have finished reading it.
+// ---------------------------------------------------------------------------------------
+constexpr int kClusterThreads = 512;  // 16 warps
+constexpr int kSlab = 32;             // rows (or columns) per block
+
+struct ClusterArgs {
+  RowParams rp;
+  ColParams cp;
+  const float2* u0;  // (batch, N, N)
+  int nz;
+};
+
+template <int N>
+struct ClusterCfg {
+  static constexpr int C = N / kSlab;
+  static constexpr int TWPAD = (WarpFft<N>::TW + 1) & ~1;
+  static constexpr int KP = kSlab + 1;  // column-slab row pitch (float2)
+  static constexpr size_t F2 = 2 * (size_t)TWPAD + (size_t)kSlab * N + (size_t)N * KP +
+                               (size_t)(kClusterThreads / 32) * WarpFft<N>::BUF;
+  static constexpr size_t SMEM = F2 * sizeof(float2);
+};
+
+template <int N>
+__global__ void __launch_bounds__(kClusterThreads, 1) cluster_march_kernel(ClusterArgs a) {
+  namespace cg = cooperative_groups;
+  using Cfg = ClusterCfg<N>;
+  constexpr int E = N / 32;
+  constexpr int T = kClusterThreads;
+  constexpr int NW = T / 32;
+  constexpr int KP = Cfg::KP;
+  cg::cluster_group cl = cg::this_cluster();
+  const int c = (int)cl.block_rank();
+  const int gl = blockIdx.x / Cfg::C;
+  const RowParams& p = a.rp;
+  const ColParams& q = a.cp;
+  extern __shared__ __align__(16) float2 csm[];
+  float2* twr = csm;
+  float2* twc = twr + Cfg::TWPAD;
+  float2* R = twc + Cfg::TWPAD;       // kSlab x N
+  float2* K = R + kSlab * N;          // N x KP
+  float2* X = K + (size_t)N * KP;     // NW exchange buffers
+  __shared__ float red[64];
+  __shared__ float part[2 * (kSlab / 16)];  // this block's tile partials (weighted)
+  const int warp = threadIdx.x >> 5, t = threadIdx.x & 31;
+  float2* buf = X + warp * WarpFft<N>::BUF;
+  for (int k = threadIdx.x; k < WarpFft<N>::TW; k += T) {
+    twr[k] = p.wtw[k];
+    twc[k] = q.wtw[k];
+  }
+  const size_t plane = (size_t)N * N;
+  const int nz = a.nz;
+  float dn0 = 0.f;  // weighted: dn0 of the last column pass
+
+  // the row pass producing plane z over this block's rows (z = 0: plane 0 is the input)
+  auto row_phase = [&](int z) {
+    const bool first = z == 0;
+    const float dz0 = first ? 0.f : (p.mean_mode == BPM_MEAN_WEIGHTED ? dn0 : row_dn0(p, gl));
+    const float2 rot = row_rot(p, dz0);
+    const size_t zoff = (size_t)z * plane;
+    for (int yl = warp; yl < kSlab; yl += NW) {
+      const int y = c * kSlab + yl;
+      float2 v[E];
+      if (first) {
+        const float2* src = a.u0 + gl * plane + (size_t)y * N;
+#pragma unroll
+        for (int m = 0; m < E; m++) v[m] = src[t + 32 * m];
+      } else {
+#pragma unroll
+        for (int m = 0; m < E; m++) v[m] = R[yl * N + t + 32 * m];
+        warp_fft<N, true>(v, buf, twr, t);
+      }
+#pragma unroll
+      for (int m = 0; m < E; m++) {
+        const int x = t + 32 * m;
+        const size_t pix = (size_t)y * N + x;
+        float2 u = v[m];
+        if (!first && p.do_mask) {
+          const float2 M = p.mask ? p.mask[zoff + pix]
+                                  : mask_value(p.dn, p.dn_dtype, gl * p.dn_bstride + zoff + pix, p.unit_k, x, y,
+                                               p.nx, p.ny, p.absorb, p.taper);
+          u = cmul(u, M);
+          if (dz0 != 0.f) u = cmul(u, rot);
+        }
+        if (p.out_kind == BPM_OUT_FIELD)
+          __stcs(reinterpret_cast<float2*>(p.out) + gl * p.out_bstride + zoff + pix, u);
+        else if (p.out_kind == BPM_OUT_INTENSITY)
+          __stcs(reinterpret_cast<float*>(p.out) + gl * p.out_bstride + zoff + pix, cabs2(u));
+        if (z == nz - 1 && p.last_plane) p.last_plane[gl * plane + pix] = u;
+        v[m] = u;
+      }
+      if (z + 1 < nz) {
+        warp_fft<N, false>(v, buf, twr, t);
+#pragma unroll
+        for (int m = 0; m < E; m++) R[yl * N + t + 32 * m] = v[m];
+      }
+    }
+  };
+
+  __syncthreads();  // twiddles
+  row_phase(0);
+  for (int i = 0; i + 1 < nz; i++) {
+    cl.sync();  // every row slab holds the row-transformed field
+    // gather the column slab: K[y][xl] = R_{y/32}[y%32][32c + xl]
+    for (int e = threadIdx.x; e < N * kSlab; e += T) {
+      const int y = e >> 5, xl = e & 31;
+      const float2* Rr = cl.map_shared_rank(R, y >> 5);
+      K[y * KP + xl] = Rr[(y & 31) * N + c * kSlab + xl];
+    }
+    __syncthreads();
+    float n_eff = q.prop_mode == 1 ? q.slice_n[i + 1] : q.n00f;
+    if (q.prop_mode == 2) {
+      // weighted: forward transforms, k-space back into the slab, tile partial sums
+      for (int xl = warp; xl < kSlab; xl += NW) {
+        float2 v[E];
+#pragma unroll
+        for (int m = 0; m < E; m++) v[m] = K[(t + 32 * m) * KP + xl];
+        warp_fft<N, false>(v, buf, twc, t);
+#pragma unroll
+        for (int m = 0; m < E; m++) K[(t + 32 * m) * KP + xl] = v[m];
+      }
+      __syncthreads();
+      constexpr int PER = 16 * N / T;  // the warp kernels' element order within a tile
+      for (int tile = 0; tile < kSlab / 16; tile++) {
+        const int x0 = c * kSlab + tile * 16;
+        float sdn = 0.f, su = 0.f;
+#pragma unroll
+        for (int ii = 0; ii < PER; ii++) {
+          const int e = threadIdx.x + ii * T;
+          const int n = e >> 4, cc = e & 15;
+          const float2 u = K[n * KP + tile * 16 + cc];
+          const float aa = __fsqrt_rn(cabs2(u));
+          su += aa;
+          if (q.dn)
+            sdn = fmaf(aa, load_dn_real(q.dn, q.dn_dtype, gl * q.dn_bstride + (size_t)n * N + x0 + cc), sdn);
+        }
+        block_sum2<T>(sdn, su, red);
+        if (threadIdx.x == 0) {
+          part[2 * tile] = sdn;
+          part[2 * tile + 1] = su;
+        }
+        __syncthreads();
+      }
+      cl.sync();  // every block's partials are visible
+      if (threadIdx.x == 0) {
+        float dn_sum = 0.f, u_sum = 0.f;
+        for (int r = 0; r < Cfg::C; r++) {
+          const float* pr = cl.map_shared_rank(part, r);
+          for (int tile = 0; tile < kSlab / 16; tile++) {
+            dn_sum += pr[2 * tile];
+            u_sum += pr[2 * tile + 1];
+          }
+        }
+        red[0] = dn_sum / u_sum;  // mult_dn_mean_buff, bpm_3d_kernels.cl:117
+      }
+      __syncthreads();
+      dn0 = red[0];
+      n_eff = q.n00f + dn0;  // mult_propagator_buff, bpm_3d_kernels.cl:482
+    }
+    const float nk = prop_nk(q, n_eff);
+    for (int xl = warp; xl < kSlab; xl += NW) {
+      const int x = c * kSlab + xl;
+      float2 v[E];
+#pragma unroll
+      for (int m = 0; m < E; m++) v[m] = K[(t + 32 * m) * KP + xl];
+      if (q.prop_mode != 2) warp_fft<N, false>(v, buf, twc, t);
+      float S = 0.f, G = 0.f;
+#pragma unroll
+      for (int m = 0; m < E; m++)
+        v[m] = prop_point<true>(q, v[m], x, t + 32 * m, nk, make_float2(0.f, 0.f), S, G, q.ky2);
+      warp_fft<N, true>(v, buf, twc, t);
+#pragma unroll
+      for (int m = 0; m < E; m++) K[(t + 32 * m) * KP + xl] = v[m];
+    }
+    cl.sync();  // every column slab holds the propagated field
+    // gather the row slab back: R[yl][x] = K_{x/32}[32c + yl][x%32]
+    for (int e = threadIdx.x; e < kSlab * N; e += T) {
+      const int yl = e / N, x = e - yl * N;
+      const float2* Kr = cl.map_shared_rank(K, x >> 5);
+      R[yl * N + x] = Kr[(c * kSlab + yl) * KP + (x & 31)];
+    }
+    __syncthreads();
+    row_phase(i + 1);
+  }
+  cl.sync();  // no block leaves while another may still read its slabs
+}
+
+// ---------------------------------------------------------------------------------------
 // dispatch over power-of-two sizes
 // ---------------------------------------------------------------------------------------
 template <template <int> class K>
@@ -1622,6 +1824,84 @@ int sink_copy(bpm_plan* pl, const bpm_request* r, const HostSink& h, int b0, int
   return BPM_OK;
 }
 
+// The whole-march cluster kernel serves square grids of 64, 128 or 256 without scattering
+// sums or checkpoints. BPM_GB300_CLUSTER=1 turns it on (off by default until measured on
+// the device), =0 off.
+bool cluster_enabled() {
+  static const bool on = [] {
+    const char* e = getenv("BPM_GB300_CLUSTER");
+    return e && strcmp(e, "1") == 0;
+  }();
+  return on;
+}
+
+template <int N>
+struct ClusterK {
+  static cudaLaunchConfig_t config(unsigned batch, cudaStream_t s, cudaLaunchAttribute* at) {
+    using Cfg = ClusterCfg<N>;
+    cudaLaunchConfig_t cfg = {};
+    cfg.gridDim = dim3(batch * Cfg::C);
+    cfg.blockDim = dim3(kClusterThreads);
+    cfg.dynamicSmemBytes = Cfg::SMEM;
+    cfg.stream = s;
+    at[0].id = cudaLaunchAttributeClusterDimension;
+    at[0].val.clusterDim.x = Cfg::C;
+    at[0].val.clusterDim.y = 1;
+    at[0].val.clusterDim.z = 1;
+    cfg.attrs = at;
+    cfg.numAttrs = 1;
+    return cfg;
+  }
+  // -1: not checked yet; 0: no cluster of this shape fits on the device; 1: launchable
+  static int& state() {
+    static int st = -1;
+    return st;
+  }
+  static bool ready() {
+    if (state() < 0) {
+      int ok = 0;
+      if (cudaFuncSetAttribute(cluster_march_kernel<N>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                               (int)ClusterCfg<N>::SMEM) == cudaSuccess) {
+        cudaLaunchAttribute at[1];
+        cudaLaunchConfig_t cfg = config(1, nullptr, at);
+        int clusters = 0;
+        if (cudaOccupancyMaxActiveClusters(&clusters, cluster_march_kernel<N>, &cfg) == cudaSuccess)
+          ok = clusters > 0;
+      }
+      cudaGetLastError();
+      state() = ok;
+    }
+    return state() == 1;
+  }
+  static int launch(const bpm_plan* pl, const bpm_request* r, void* ws, cudaStream_t s) {
+    MarchCtx c = make_ctx(pl, r, ws, 0, r->batch);
+    ClusterArgs a;
+    a.rp = c.rp;
+    a.rp.do_mask = r->dn_dtype != BPM_DN_NONE;
+    a.cp = c.cp;
+    a.u0 = static_cast<const float2*>(r->u0);
+    a.nz = pl->d.nz;
+    cudaLaunchAttribute at[1];
+    cudaLaunchConfig_t cfg = config((unsigned)r->batch, s, at);
+    BPM_CUDA_TRY(cudaLaunchKernelEx(&cfg, cluster_march_kernel<N>, a));
+    BPM_LAUNCH_CHECK("cluster_march_kernel");
+    return BPM_OK;
+  }
+};
+
+// kNotCluster when the request is not for the cluster kernel, else its launch status
+constexpr int kNotCluster = 1;
+int try_cluster_march(const bpm_plan* pl, const bpm_request* r, void* ws, cudaStream_t s) {
+  const bpm_grid_desc& d = pl->d;
+  if (!cluster_enabled() || d.nx != d.ny || r->scatter_p || r->ckpt) return kNotCluster;
+  switch (d.nx) {
+    case 64: return ClusterK<64>::ready() ? ClusterK<64>::launch(pl, r, ws, s) : kNotCluster;
+    case 128: return ClusterK<128>::ready() ? ClusterK<128>::launch(pl, r, ws, s) : kNotCluster;
+    case 256: return ClusterK<256>::ready() ? ClusterK<256>::launch(pl, r, ws, s) : kNotCluster;
+  }
+  return kNotCluster;
+}
+
 // All groups of a request. With room for several workspace slots, groups march
 // concurrently on the plan's auxiliary streams (forked from and joined back to s through
 // events, which also captures into a CUDA graph as parallel branches), so one group's
@@ -1634,6 +1914,18 @@ int enqueue_march(bpm_plan* pl, const bpm_request* r, void* ws, size_t ws_bytes,
   int rc = check_workspace(pl, r, ws, ws_bytes);
   if (rc) return rc;
   const int nz = pl->d.nz;
+  {
+    const int crc = try_cluster_march(pl, r, ws, s);
+    if (crc != kNotCluster) {
+      if (crc != BPM_OK) return crc;
+      if (sink) {
+        if ((rc = sink_copy(pl, r, *sink, 0, r->batch, 0, nz, s, pl->ev_ready[0]))) return rc;
+        BPM_CUDA_TRY(cudaEventRecord(pl->ev_copied, pl->copy));
+        BPM_CUDA_TRY(cudaStreamWaitEvent(s, pl->ev_copied, 0));
+      }
+      return BPM_OK;
+    }
+  }
   const int G = group_size(pl, r);
   const int ngroups = (r->batch + G - 1) / G;
   const size_t slot = ws_layout(pl, G).total;

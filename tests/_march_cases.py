@@ -27,6 +27,42 @@ def cases():
     return out
 
 
+def cluster_cases():
+    """Square grids the whole-march cluster kernel serves (64, 128, 256), every mean mode
+    and dn kind, batched (shared and per-field dn) and single."""
+    rng = np.random.default_rng(5)
+    out = []
+    for n, nz, mode, kind, B in [(64, 7, "weighted", "f32", 3), (128, 12, "simple", "f16", 2),
+                                 (128, 9, "ignore", "c64", 3), (256, 6, "weighted", "f32", 2),
+                                 (256, 5, "ignore", "none", 1), (64, 1, "weighted", "f32", 2),
+                                 (128, 8, "weighted", "per-field", 3)]:
+        dn = None
+        if kind != "none":
+            dn = (.03 * rng.standard_normal((nz, n, n))).astype(np.float32)
+            if kind == "c64":
+                dn = (dn - 1j * np.abs(.002 * rng.standard_normal((nz, n, n)))).astype(np.complex64)
+            if kind == "per-field":
+                dn = (.03 * rng.standard_normal((B, nz, n, n))).astype(np.float32)
+        x = np.arange(n) * .1
+        u0 = np.exp(2j * np.pi * rng.uniform(-.3, .3, (B, 1, 1)) * x[None, None, :]).repeat(n, 1)
+        out.append(dict(size=(n, n, nz), mode=mode, dn=dn, half=kind == "f16", u0=u0.astype(np.complex64)))
+    return out
+
+
+def run_cluster(path):
+    import bpm_gb300 as bpm
+    res = {}
+    for i, c in enumerate(cluster_cases()):
+        res["f%d" % i] = bpm.bpm_3d_batched(c["size"], (.1, .1, .1), u0=c["u0"], dn=c["dn"], mean_mode=c["mode"],
+                                            store_dn_as_half=c["half"], return_field=True)
+        res["l%d" % i] = bpm.bpm_3d_batched(c["size"], (.1, .1, .1), u0=c["u0"], dn=c["dn"], mean_mode=c["mode"],
+                                            store_dn_as_half=c["half"], return_full=False, absorbing_width=4)
+        if c["dn"] is None or c["dn"].ndim == 3:
+            res["i%d" % i] = bpm.bpm_3d(c["size"], (.1, .1, .1), u0=c["u0"][0], dn=c["dn"], mean_mode=c["mode"],
+                                        store_dn_as_half=c["half"], return_field=False, absorbing_width=3)
+    np.savez(path, **res)
+
+
 def run(path):
     import bpm_gb300 as bpm
     res = {}
@@ -39,4 +75,7 @@ def run(path):
 
 
 if __name__ == "__main__":
-    run(sys.argv[1])
+    if len(sys.argv) > 2 and sys.argv[2] == "cluster":
+        run_cluster(sys.argv[1])
+    else:
+        run(sys.argv[1])

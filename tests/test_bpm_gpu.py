@@ -373,3 +373,24 @@ def test_derived_plan_equals_fresh_plan(bpm):
     assert torch.equal(outs[0], outs[1])
     h = ctypes.c_void_p()
     assert N.lib().bpm_plan_derive(base.handle, 0, ctypes.byref(h)) == N.BPM_ERR_SHAPE
+
+
+def test_cluster_march_matches_pass_kernels(bpm, tmp_path):
+    """The whole-march cluster kernel (square grids 64..256, the field in distributed shared
+    memory; BPM_GB300_CLUSTER=1) against the row/column pass kernels (=0), each in a child
+    process: the same bits for every mean mode, real / half / complex / no / per-field dn,
+    field and |u|^2 volumes, exit planes with a taper, batched and single."""
+    import os
+    import subprocess
+    import sys
+    here = os.path.dirname(os.path.abspath(__file__))
+    script = os.path.join(here, "_march_cases.py")
+    a, b = str(tmp_path / "cluster.npz"), str(tmp_path / "passes.npz")
+    subprocess.run([sys.executable, script, a, "cluster"], check=True, timeout=600,
+                   env=dict(os.environ, BPM_GB300_CLUSTER="1"))
+    subprocess.run([sys.executable, script, b, "cluster"], check=True, timeout=600,
+                   env=dict(os.environ, BPM_GB300_CLUSTER="0"))
+    A, B = np.load(a), np.load(b)
+    assert sorted(A.files) == sorted(B.files) and len(A.files) >= 18
+    for k in A.files:
+        assert np.array_equal(A[k], B[k]), k

@@ -63,7 +63,7 @@ def run(torch, N, plan, u0, dn, out_kind, noalloc, tabs=(None, None)):
 
 
 @pytest.mark.parametrize("size,batch,mode,out_kind", [
-    ((256, 256, 12), 5, "weighted", "intensity"),   # all fields in one group
+    ((256, 128, 12), 5, "weighted", "intensity"),   # all fields in one group
     ((512, 512, 8), 4, "ignore", "field"),          # the scratch holds 3 fields: two groups
     ((64, 128, 20), 3, "simple", "intensity"),
 ])
