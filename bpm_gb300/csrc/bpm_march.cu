@@ -1893,7 +1893,7 @@ struct ClusterK {
 constexpr int kNotCluster = 1;
 int try_cluster_march(const bpm_plan* pl, const bpm_request* r, void* ws, cudaStream_t s) {
   const bpm_grid_desc& d = pl->d;
-  if (!cluster_enabled() || d.nx != d.ny || r->scatter_p || r->ckpt) return kNotCluster;
+  if (!cluster_enabled() || d.nx != d.ny || r->scatter_p || r->ckpt || !pl->wtw_x || !pl->wtw_y) return kNotCluster;
   switch (d.nx) {
     case 64: return ClusterK<64>::ready() ? ClusterK<64>::launch(pl, r, ws, s) : kNotCluster;
     case 128: return ClusterK<128>::ready() ? ClusterK<128>::launch(pl, r, ws, s) : kNotCluster;
@@ -2227,7 +2227,7 @@ extern "C" int bpm_plan_create(const bpm_grid_desc* d, bpm_plan** out) {
     return fail(e, "cudaMemcpy");
   for (int axis = 0; axis < 2; axis++) {
     const int n = axis == 0 ? nx : ny;
-    if (n < 128 || n > 512) continue;
+    if (n < 64 || n > 512) continue;  // the warp FFT's sizes (the cluster kernel uses 64 too)
     std::vector<float2> w = warp_twiddles(n);
     float2** dst = axis == 0 ? &pl->wtw_x : &pl->wtw_y;
     if ((e = cudaMalloc(dst, w.size() * sizeof(float2)))) return fail(e, "cudaMalloc");
