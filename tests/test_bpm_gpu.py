@@ -378,8 +378,10 @@ def test_derived_plan_equals_fresh_plan(bpm):
 def test_cluster_march_matches_pass_kernels(bpm, tmp_path):
     """The whole-march cluster kernel (square grids 64..256, the field in distributed shared
     memory; BPM_GB300_CLUSTER=1) against the row/column pass kernels (=0), each in a child
-    process: the same bits for every mean mode, real / half / complex / no / per-field dn,
-    field and |u|^2 volumes, exit planes with a taper, batched and single."""
+    process, for every mean mode, real / half / complex / no / per-field dn, field and |u|^2
+    volumes, exit planes with a taper, batched and single. At 128 and 256 both paths run
+    the same warp FFT and give the same bits; at 64 the pass kernels use the shared-memory
+    tile FFT (another radix order), so the two agree to FP32 rounding."""
     import os
     import subprocess
     import sys
@@ -392,5 +394,11 @@ def test_cluster_march_matches_pass_kernels(bpm, tmp_path):
                    env=dict(os.environ, BPM_GB300_CLUSTER="0"))
     A, B = np.load(a), np.load(b)
     assert sorted(A.files) == sorted(B.files) and len(A.files) >= 18
+    bad = []
     for k in A.files:
-        assert np.array_equal(A[k], B[k]), k
+        if A[k].shape[-1] == 64:
+            if not rel_l2(A[k], B[k]) < 2e-6:
+                bad.append((k, rel_l2(A[k], B[k])))
+        elif not np.array_equal(A[k], B[k]):
+            bad.append((k, rel_l2(A[k], B[k])))
+    assert not bad, bad
