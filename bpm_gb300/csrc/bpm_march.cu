@@ -1223,7 +1223,14 @@ __global__ void __launch_bounds__(kClusterThreads, 1) cluster_march_kernel(Clust
   // the row pass producing plane z over this block's rows (z = 0: plane 0 is the input)
   auto row_phase = [&](int z) {
     const bool first = z == 0;
-    const float dz0 = first ? 0.f : (p.mean_mode == BPM_MEAN_WEIGHTED ? dn0 : row_dn0(p, gl));
+    // the mean-index shift of plane z (row_dn0 of the pass kernels, whose p.z is the plane)
+    float dz0 = 0.f;
+    if (!first) {
+      if (p.mean_mode == BPM_MEAN_WEIGHTED)
+        dz0 = dn0;
+      else if (p.mean_mode == BPM_MEAN_SIMPLE && p.slice_dn0)
+        dz0 = p.slice_dn0[z];
+    }
     const float2 rot = row_rot(p, dz0);
     const size_t zoff = (size_t)z * plane;
     for (int yl = warp; yl < kSlab; yl += NW) {
