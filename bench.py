@@ -350,6 +350,51 @@ def psf_timing(reps=3):
             "output_gbs": out_bytes / (t * 1e-3) / 1e9}
 
 
+def single_request_timing(reps=5):
+    """The single-request configurations through the public API (device-resident inputs,
+    and host numpy in / numpy out):
+    config 1, 128x128x128, dx=dz=0.1, lambda 0.5, n0 1.33, unit plane wave, one centred
+    sphere of radius 20 px and dn 0.05, weighted mean mode, |u|^2 volume + exit field;
+    config 2 (BPM part), 256^3, 50 seeded spheres with radius U[3,15] px and complex dn
+    (Re U[0.01,0.05], Im U[0,1e-3]), input a Gaussian focus of NA 0.4 at mid-depth
+    (psf_u0), mean mode 'ignore' (the one complex dn is defined for)."""
+    import torch
+    import bpm_gb300
+    out = {}
+    n = 128
+    z, y, x = np.meshgrid(np.arange(n), np.arange(n), np.arange(n), indexing="ij")
+    dn1 = (.05 * (((x - n / 2) ** 2 + (y - n / 2) ** 2 + (z - n / 2) ** 2) <= 20 ** 2)).astype(np.float32)
+    dn2 = sphere_pool(256, 256, SEED + 2).contiguous()
+    u02 = bpm_gb300.psf_u0((256, 256), (.1, .1), zfoc=12.8, NA=.4, lam=.5, n0=1.33, device=True)
+    cases = [("config1_128cube_plain", (n, n, n), torch.from_numpy(dn1).cuda(), None, "weighted", dn1),
+             ("config2_256cube_bpm", (256, 256, 256), dn2, u02, "ignore", None)]
+    for name, size, dn_d, u0_d, mode, dn_h in cases:
+        def call():
+            return bpm_gb300.bpm_3d(size, UNITS, lam=LAM, n0=N0, u0=u0_d, dn=dn_d, mean_mode=mode,
+                                    return_field=False)
+        call()
+        torch.cuda.synchronize()
+        a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        a.record()
+        for _ in range(reps):
+            call()
+        b.record()
+        torch.cuda.synchronize()
+        t = a.elapsed_time(b) / reps
+        vu = size[0] * size[1] * (size[2] - 1)
+        rec = {"ms": t, "voxel_updates_per_s": vu / (t * 1e-3), "api": "bpm_gb300.bpm_3d, CUDA tensors in/out"}
+        if dn_h is not None:
+            # host numpy in, numpy out (the reference's own calling convention)
+            bpm_gb300.bpm_3d(size, UNITS, lam=LAM, n0=N0, dn=dn_h, mean_mode=mode, return_field=False)
+            t0 = time.perf_counter()
+            for _ in range(reps):
+                bpm_gb300.bpm_3d(size, UNITS, lam=LAM, n0=N0, dn=dn_h, mean_mode=mode, return_field=False)
+            th = (time.perf_counter() - t0) / reps
+            rec["e2e_numpy"] = {"ms": th * 1e3, "voxel_updates_per_s": vu / th}
+        out[name] = rec
+    return out
+
+
 def adjoint_timing():
     """Config 4: d(loss)/d(dn) on 256x256x128 for 16 angles within NA 0.6, checkpoints
     every 16 slices: forward march + hand-written adjoint (recompute + backward)."""
@@ -562,6 +607,7 @@ def main():
         if not args.no_serve:
             res["serve"] = serve_trace()
         res["psf"] = psf_timing()
+        res["single_requests"] = single_request_timing()
         res["adjoint"] = adjoint_timing()
         if not args.no_cpu_baseline:
             v, t, sample = cpu_sample(4, NZ - 1)
