@@ -359,6 +359,8 @@ row_pass_kernel(RowParams p) {
   constexpr int PER = 16 * N / T;
   if (p.do_inv || p.do_fwd)
     for (int k = tid; k < N; k += T) tw[k] = p.tw[k];
+  dep_wait();
+  dep_release();
   {
     const float2* src = p.src + gl * p.src_bstride + (size_t)y0 * N;
     float2 buf[PER];
@@ -571,6 +573,8 @@ col_pass_kernel(ColParams p) {
   const int x0 = blockIdx.x * 16;
   float2* Wp = p.W + (size_t)gl * p.nx * N;
   for (int k = threadIdx.x; k < N; k += TileCfg<N>::THREADS) tw[k] = p.tw[k];
+  dep_wait();
+  dep_release();
   col_load<N>(tile, Wp, p.nx, x0);
   __syncthreads();
   tile_fft<N, R, false>(tile, tw);
@@ -595,6 +599,8 @@ col_fwd_reduce_kernel(ColParams p) {
   const int x0 = blockIdx.x * 16;
   float2* Wp = p.W + (size_t)gl * p.nx * N;
   for (int k = threadIdx.x; k < N; k += T) tw[k] = p.tw[k];
+  dep_wait();
+  dep_release();
   col_load<N>(tile, Wp, p.nx, x0);
   __syncthreads();
   tile_fft<N, R, false>(tile, tw);
@@ -629,6 +635,9 @@ col_inv_kernel(ColParams p) {
   const int gl = blockIdx.y;
   const int x0 = blockIdx.x * 16;
   float2* Wp = p.W + (size_t)gl * p.nx * N;
+  for (int k = threadIdx.x; k < N; k += TileCfg<N>::THREADS) tw[k] = p.tw[k];
+  dep_wait();
+  dep_release();
   if (threadIdx.x == 0) {
     // every block of the field sums the partials in the same order: identical results
     const float* part = p.red_part + (size_t)gl * (p.nx / 16) * 2;
@@ -641,7 +650,6 @@ col_inv_kernel(ColParams p) {
     s_n = p.n00f + dn0;                // mult_propagator_buff, bpm_3d_kernels.cl:482
     if (blockIdx.x == 0) p.dn0_field[gl] = dn0;
   }
-  for (int k = threadIdx.x; k < N; k += TileCfg<N>::THREADS) tw[k] = p.tw[k];
   col_load<N>(tile, Wp, p.nx, x0);
   __syncthreads();
   col_propagate<N>(tile, p, s_n, x0, gl, red);
@@ -683,15 +691,18 @@ row_warp_kernel(RowParams p) {
   const int gl = blockIdx.y;
   const int y = blockIdx.x * kRowWarps + warp;
   const size_t plane = (size_t)N * p.ny;
-  // the row loads go out first, so their latency overlaps the twiddle table's
+  // the twiddle table (a plan constant) is fetched before the wait for the previous pass;
+  // the row loads go out before the barrier, so their latency overlaps the table's
+  const bool fft = p.do_inv || p.do_fwd;
+  if (fft)
+    for (int k = threadIdx.x; k < WarpFft<N>::TW; k += T) tw[k] = p.wtw[k];
+  dep_wait();
+  dep_release();
   float2 v[E];
   const float2* src = p.src + gl * p.src_bstride + (size_t)y * N;
 #pragma unroll
   for (int m = 0; m < E; m++) v[m] = src[t + 32 * m];
-  if (p.do_inv || p.do_fwd) {
-    for (int k = threadIdx.x; k < WarpFft<N>::TW; k += T) tw[k] = p.wtw[k];
-    __syncthreads();
-  }
+  if (fft) __syncthreads();
   if (p.do_inv) warp_fft<N, true>(v, buf, tw, t);
 
   const float dn0 = row_dn0(p, gl);
@@ -747,6 +758,9 @@ row_shared_kernel(RowParams p, int nfields) {
   const bool active = gl < nfields;
   const size_t plane = (size_t)N * p.ny;
   const size_t zoff = (size_t)p.z * plane;
+  for (int k = threadIdx.x; k < WarpFft<N>::TW; k += T) tw[k] = p.wtw[k];  // plan constant
+  dep_wait();
+  dep_release();
   {
     const int es = PRE ? 8 : (p.dn_dtype == BPM_DN_C64 ? 8 : (p.dn_dtype == BPM_DN_F16 ? 2 : 4));
     const char* srcm = PRE ? reinterpret_cast<const char*>(p.mask + zoff + (size_t)y * N)
@@ -761,7 +775,6 @@ row_shared_kernel(RowParams p, int nfields) {
 #pragma unroll
     for (int m = 0; m < E; m++) v[m] = src[t + 32 * m];
   }
-  for (int k = threadIdx.x; k < WarpFft<N>::TW; k += T) tw[k] = p.wtw[k];
   __syncthreads();
   if (active && p.do_inv) warp_fft<N, true>(v, buf, tw, t);
   cp_async_wait<0>();
@@ -817,6 +830,14 @@ col_warp_kernel(ColParams p) {
   float2* Wp = p.W + (size_t)gl * p.nx * N;
   constexpr int PER = 16 * N / T;
   static_assert(WarpFft<N>::TW <= T && N <= T, "one twiddle and one ky^2 entry per thread");
+  // plan constants first (the twiddle table; the propagator recipe's ky^2 column, staged
+  // next to the tile), then the wait for the previous pass
+  const float2 twv = threadIdx.x < WarpFft<N>::TW ? p.wtw[threadIdx.x] : make_float2(0.f, 0.f);
+  float* sky2 = reinterpret_cast<float*>(smem + WarpCfg<N>::COL_F2);
+  const bool stage_ky = WHICH != 1 && p.prop_mode != 0;
+  const float kyv = (stage_ky && threadIdx.x < N) ? p.ky2[threadIdx.x] : 0.f;
+  dep_wait();
+  dep_release();
   // weighted reduction: dn slice 0 of this tile goes to shared memory with cp.async now and
   // is read only after the transform
   const char* dn_stage = nullptr;
@@ -831,19 +852,13 @@ col_warp_kernel(ColParams p) {
     cp_async_commit();
     dn_stage = dst;
   }
-  // the tile loads, then the twiddle load, go out before any shared-memory store waits on
-  // them, so their latencies overlap
+  // the tile loads go out before any shared-memory store waits on them
   float2 ld[PER];
 #pragma unroll
   for (int i = 0; i < PER; i++) {
     const int e = threadIdx.x + i * T;
     ld[i] = Wp[(size_t)(e >> 4) * p.nx + x0 + (e & 15)];
   }
-  const float2 twv = threadIdx.x < WarpFft<N>::TW ? p.wtw[threadIdx.x] : make_float2(0.f, 0.f);
-  // the propagator recipe's ky^2 column, staged next to the tile
-  float* sky2 = reinterpret_cast<float*>(smem + WarpCfg<N>::COL_F2);
-  const bool stage_ky = WHICH != 1 && p.prop_mode != 0;
-  const float kyv = (stage_ky && threadIdx.x < N) ? p.ky2[threadIdx.x] : 0.f;
   if (WHICH == 2 && threadIdx.x == 0) {
     // every block of the field sums the partials in the same order: identical results
     const float* part = p.red_part + (size_t)gl * (p.nx / 16) * 2;
@@ -963,6 +978,8 @@ row_pipe_kernel(RowParams p, int nrows) {
     for (int k = threadIdx.x; k < WarpFft<N>::TW; k += T) tw[k] = p.wtw[k];
     __syncthreads();
   }
+  dep_wait();
+  dep_release();
   const size_t plane = (size_t)N * p.ny;
   const int dn_es = p.dn_dtype == BPM_DN_C64 ? 8 : (p.dn_dtype == BPM_DN_F16 ? 2 : 4);
   const size_t zoff = (size_t)p.z * plane;
@@ -1068,6 +1085,8 @@ col_pipe_kernel(ColParams p, int ntiles) {
       cp_async8(dst + tile_idx(e >> 4, e & 15), Wp + (size_t)(e >> 4) * p.nx + x0 + (e & 15));
     }
   };
+  dep_wait();
+  dep_release();
   int it = blockIdx.x;
   if (it < ntiles) issue_tile(tiles, it);
   cp_async_commit();
@@ -1468,26 +1487,26 @@ struct RowK {
         const int warps = balanced_workers(nrows, pipe_cap(pre) * kRowWarps);
         const int blocks = (warps + kRowWarps - 1) / kRowWarps;
         auto fn = pre ? row_pipe_kernel<N, 1> : row_pipe_kernel<N, 0>;
-        fn<<<blocks, kRowWarps * 32, PipeCfg<N>::ROW_SMEM, s>>>(p, nrows);
+        BPM_CUDA_TRY(launch_dep(fn, dim3(blocks), dim3(kRowWarps * 32), PipeCfg<N>::ROW_SMEM, s, p, nrows));
         BPM_LAUNCH_CHECK("row_pipe_kernel");
         return BPM_OK;
       }
       if (!adj && shared_ok(p) && g.y >= 2) {
         const dim3 gs(p.ny, (g.y + kRowWarps - 1) / kRowWarps);
         auto fn = p.mask ? row_shared_kernel<N, 1> : row_shared_kernel<N, 0>;
-        fn<<<gs, kRowWarps * 32, WarpCfg<N>::ROW_SMEM_SHARED, s>>>(p, (int)g.y);
+        BPM_CUDA_TRY(launch_dep(fn, gs, dim3(kRowWarps * 32), WarpCfg<N>::ROW_SMEM_SHARED, s, p, (int)g.y));
         BPM_LAUNCH_CHECK("row_shared_kernel");
         return BPM_OK;
       }
       const dim3 gw(g.x * 16 / kRowWarps, g.y);
       auto fn = adj ? (p.mask ? row_warp_kernel<N, true, 1> : row_warp_kernel<N, true, 0>)
                     : (p.mask ? row_warp_kernel<N, false, 1> : row_warp_kernel<N, false, 0>);
-      fn<<<gw, kRowWarps * 32, WarpCfg<N>::ROW_SMEM, s>>>(p);
+      BPM_CUDA_TRY(launch_dep(fn, gw, dim3(kRowWarps * 32), WarpCfg<N>::ROW_SMEM, s, p));
     } else {
       if (adj)
-        row_pass_kernel<N, true><<<g, TileCfg<N>::THREADS, TileCfg<N>::SMEM, s>>>(p);
+        BPM_CUDA_TRY(launch_dep(row_pass_kernel<N, true>, g, dim3(TileCfg<N>::THREADS), TileCfg<N>::SMEM, s, p));
       else
-        row_pass_kernel<N, false><<<g, TileCfg<N>::THREADS, TileCfg<N>::SMEM, s>>>(p);
+        BPM_CUDA_TRY(launch_dep(row_pass_kernel<N, false>, g, dim3(TileCfg<N>::THREADS), TileCfg<N>::SMEM, s, p));
     }
     BPM_LAUNCH_CHECK("row_pass_kernel");
     return BPM_OK;
@@ -1526,13 +1545,13 @@ struct ColK {
     if constexpr (WARP) {
       if (pipe_enabled() && aligned16(p.W)) {
         const int ntiles = (int)(g.x * g.y);
-        col_pipe_kernel<N, WHICH><<<balanced_workers(ntiles, pipe_cap()), kColWarps * 32, PipeCfg<N>::COL_SMEM,
-                                    s>>>(p, ntiles);
+        BPM_CUDA_TRY(launch_dep(col_pipe_kernel<N, WHICH>, dim3(balanced_workers(ntiles, pipe_cap())),
+                                dim3(kColWarps * 32), PipeCfg<N>::COL_SMEM, s, p, ntiles));
         BPM_LAUNCH_CHECK("col_pipe_kernel");
         return BPM_OK;
       }
     }
-    fn()<<<g, threads(), smem(), s>>>(p);
+    BPM_CUDA_TRY(launch_dep(fn(), g, dim3(threads()), smem(), s, p));
     BPM_LAUNCH_CHECK("col_pass_kernel");
     return BPM_OK;
   }

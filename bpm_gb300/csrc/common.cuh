@@ -7,6 +7,7 @@
 #include <stdint.h>
 #include <atomic>
 #include <string>
+#include <utility>
 
 #include "../../include/bpm_gb300.h"
 
@@ -66,6 +67,31 @@ __device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commi
 template <int PENDING>
 __device__ __forceinline__ void cp_async_wait() {
   asm volatile("cp.async.wait_group %0;\n" ::"n"(PENDING) : "memory");
+}
+
+// ---- programmatic dependent launch ---------------------------------------------------
+// A kernel launched with launch_dep may start while the previous kernel on its stream is
+// still running. It loads only plan constants (tables built before any march) until
+// dep_wait(), which blocks in hardware until the previous grid has completed and its
+// memory is visible; dep_release() then lets the next grid start its own prologue. Both are
+// no-ops in a kernel launched without the attribute.
+__device__ __forceinline__ void dep_wait() { asm volatile("griddepcontrol.wait;\n" ::: "memory"); }
+__device__ __forceinline__ void dep_release() { asm volatile("griddepcontrol.launch_dependents;\n" ::: "memory"); }
+
+template <typename... KArgs, typename... Args>
+inline cudaError_t launch_dep(void (*kernel)(KArgs...), dim3 grid, dim3 block, size_t smem, cudaStream_t s,
+                              Args&&... args) {
+  cudaLaunchConfig_t cfg = {};
+  cfg.gridDim = grid;
+  cfg.blockDim = block;
+  cfg.dynamicSmemBytes = smem;
+  cfg.stream = s;
+  cudaLaunchAttribute at[1];
+  at[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+  at[0].val.programmaticStreamSerializationAllowed = 1;
+  cfg.attrs = at;
+  cfg.numAttrs = 1;
+  return cudaLaunchKernelEx(&cfg, kernel, std::forward<Args>(args)...);
 }
 
 inline bool is_pow2(int n) { return n > 0 && (n & (n - 1)) == 0; }
