@@ -500,12 +500,14 @@ __device__ __forceinline__ float2 plain_wave(const ColParams& p) {
 // sums of bpm_3d.py:335-341 and the 1/(nx*ny) inverse-FFT normalisation folded in
 // COLUMN: the caller walks one column (x fixed, y over the lanes) and reads the transposed
 // table; ky2: the ky^2 table, in global or shared memory
+// htcol (COLUMN only, optional): the column's entries of the transposed table, staged
 template <bool COLUMN = false>
 __device__ __forceinline__ float2 prop_point(const ColParams& p, float2 v, int x, int y, float nk, float2 plain,
-                                             float& S, float& G, const float* ky2) {
+                                             float& S, float& G, const float* ky2,
+                                             const float2* htcol = nullptr) {
   float2 h;
   if (p.prop_mode == 0) {
-    h = COLUMN ? __ldg(p.Ht + (size_t)x * p.ny + y) : __ldg(p.H + (size_t)y * p.nx + x);
+    h = COLUMN ? (htcol ? htcol[y] : __ldg(p.Ht + (size_t)x * p.ny + y)) : __ldg(p.H + (size_t)y * p.nx + x);
     if (p.conj_h) h.y = -h.y;
   } else {
     const float tmp = __fsub_rn(__fsub_rn(nk, __ldg(p.kx2 + x)), ky2[y]);
@@ -1189,23 +1191,32 @@ col_pipe_kernel(ColParams p, int ntiles) {
 // until the others have finished reading it.
 // ---------------------------------------------------------------------------------------
 constexpr int kClusterThreads = 512;  // 16 warps
-constexpr int kSlab = 32;             // rows (or columns) per block
 
 struct ClusterArgs {
   RowParams rp;
   ColParams cp;
   const float2* u0;  // (batch, N, N)
   int nz;
+  int stage_mask;    // the next plane's mask (or dn) rows may be staged with 16-byte cp.async
 };
 
 template <int N>
 struct ClusterCfg {
-  static constexpr int C = N / kSlab;
+  static constexpr int SLAB = N <= 128 ? 16 : 32;  // rows (and columns) per block
+  static constexpr int C = N / SLAB;               // blocks per field
+  static constexpr int NW = kClusterThreads / 32;
   static constexpr int TWPAD = (WarpFft<N>::TW + 1) & ~1;
-  static constexpr int KP = kSlab + 1;  // column-slab row pitch (float2)
-  static constexpr size_t F2 = 2 * (size_t)TWPAD + (size_t)kSlab * N + (size_t)N * KP +
-                               (size_t)(kClusterThreads / 32) * WarpFft<N>::BUF;
+  static constexpr int KP = SLAB + 1;              // column-slab row pitch (float2)
+  static constexpr int GATHER = N * SLAB / kClusterThreads;  // slab elements per thread
+  // up to 128: the next plane's mask rows and this block's propagator-table columns are
+  // staged in shared memory as well (at 256 they would not fit)
+  static constexpr bool STAGE = N <= 128;
+  static constexpr size_t HT_F2 = STAGE ? (size_t)SLAB * N : 0;
+  static constexpr size_t MS_F2 = STAGE ? (size_t)SLAB * N : 0;  // up to 8 bytes per element
+  static constexpr size_t F2 = 2 * (size_t)TWPAD + (size_t)SLAB * N + (size_t)N * KP +
+                               (size_t)NW * WarpFft<N>::BUF + HT_F2 + MS_F2 + N / 2;
   static constexpr size_t SMEM = F2 * sizeof(float2);
+  static_assert(N * SLAB % kClusterThreads == 0 && SLAB % 16 == 0, "slab shape");
 };
 
 template <int N>
@@ -1214,8 +1225,10 @@ __global__ void __launch_bounds__(kClusterThreads, 1) cluster_march_kernel(Clust
   using Cfg = ClusterCfg<N>;
   constexpr int E = N / 32;
   constexpr int T = kClusterThreads;
-  constexpr int NW = T / 32;
+  constexpr int NW = Cfg::NW;
+  constexpr int SLAB = Cfg::SLAB;
   constexpr int KP = Cfg::KP;
+  constexpr int GA = Cfg::GATHER;
   cg::cluster_group cl = cg::this_cluster();
   const int c = (int)cl.block_rank();
   const int gl = blockIdx.x / Cfg::C;
@@ -1224,19 +1237,28 @@ __global__ void __launch_bounds__(kClusterThreads, 1) cluster_march_kernel(Clust
   extern __shared__ __align__(16) float2 csm[];
   float2* twr = csm;
   float2* twc = twr + Cfg::TWPAD;
-  float2* R = twc + Cfg::TWPAD;       // kSlab x N
-  float2* K = R + kSlab * N;          // N x KP
+  float2* R = twc + Cfg::TWPAD;       // SLAB x N
+  float2* K = R + SLAB * N;           // N x KP
   float2* X = K + (size_t)N * KP;     // NW exchange buffers
+  float2* HT = X + NW * WarpFft<N>::BUF;  // SLAB x N: propagator table columns (STAGE)
+  char* MS = reinterpret_cast<char*>(HT + Cfg::HT_F2);  // next plane's mask / dn rows (STAGE)
+  float* KY = reinterpret_cast<float*>(HT + Cfg::HT_F2 + Cfg::MS_F2);  // ky^2 (N floats)
   __shared__ float red[64];
-  __shared__ float part[2 * (kSlab / 16)];  // this block's tile partials (weighted)
+  __shared__ float part[2 * (SLAB / 16)];  // this block's tile partials (weighted)
   const int warp = threadIdx.x >> 5, t = threadIdx.x & 31;
   float2* buf = X + warp * WarpFft<N>::BUF;
   for (int k = threadIdx.x; k < WarpFft<N>::TW; k += T) {
     twr[k] = p.wtw[k];
     twc[k] = q.wtw[k];
   }
+  for (int k = threadIdx.x; k < N; k += T) KY[k] = q.ky2[k];
+  const bool stage_ht = Cfg::STAGE && q.prop_mode == 0;
+  if (stage_ht)
+    for (int k = threadIdx.x; k < SLAB * N; k += T) HT[k] = q.Ht[(size_t)c * SLAB * N + k];
   const size_t plane = (size_t)N * N;
   const int nz = a.nz;
+  const bool stage_mask = Cfg::STAGE && a.stage_mask && p.do_mask;
+  const int mes = p.mask ? 8 : (p.dn_dtype == BPM_DN_C64 ? 8 : (p.dn_dtype == BPM_DN_F16 ? 2 : 4));
   float dn0 = 0.f;  // weighted: dn0 of the last column pass
 
   // the row pass producing plane z over this block's rows (z = 0: plane 0 is the input)
@@ -1252,8 +1274,8 @@ __global__ void __launch_bounds__(kClusterThreads, 1) cluster_march_kernel(Clust
     }
     const float2 rot = row_rot(p, dz0);
     const size_t zoff = (size_t)z * plane;
-    for (int yl = warp; yl < kSlab; yl += NW) {
-      const int y = c * kSlab + yl;
+    for (int yl = warp; yl < SLAB; yl += NW) {
+      const int y = c * SLAB + yl;
       float2 v[E];
       if (first) {
         const float2* src = a.u0 + gl * plane + (size_t)y * N;
@@ -1264,15 +1286,28 @@ __global__ void __launch_bounds__(kClusterThreads, 1) cluster_march_kernel(Clust
         for (int m = 0; m < E; m++) v[m] = R[yl * N + t + 32 * m];
         warp_fft<N, true>(v, buf, twr, t);
       }
+      const char* mrow = MS + (size_t)yl * N * mes;
 #pragma unroll
       for (int m = 0; m < E; m++) {
         const int x = t + 32 * m;
         const size_t pix = (size_t)y * N + x;
         float2 u = v[m];
         if (!first && p.do_mask) {
-          const float2 M = p.mask ? p.mask[zoff + pix]
-                                  : mask_value(p.dn, p.dn_dtype, gl * p.dn_bstride + zoff + pix, p.unit_k, x, y,
-                                               p.nx, p.ny, p.absorb, p.taper);
+          float2 M;
+          if (stage_mask) {
+            if (p.mask)
+              M = reinterpret_cast<const float2*>(mrow)[x];
+            else if (p.dn_dtype == BPM_DN_C64)
+              M = mask_from_complex(reinterpret_cast<const float2*>(mrow)[x], p.unit_k);
+            else
+              M = mask_from_real(p.dn_dtype == BPM_DN_F16 ? __half2float(reinterpret_cast<const __half*>(mrow)[x])
+                                                          : reinterpret_cast<const float*>(mrow)[x],
+                                 p.unit_k, x, y, p.nx, p.ny, p.absorb, p.taper);
+          } else {
+            M = p.mask ? p.mask[zoff + pix]
+                       : mask_value(p.dn, p.dn_dtype, gl * p.dn_bstride + zoff + pix, p.unit_k, x, y, p.nx, p.ny,
+                                    p.absorb, p.taper);
+          }
           u = cmul(u, M);
           if (dz0 != 0.f) u = cmul(u, rot);
         }
@@ -1291,21 +1326,41 @@ __global__ void __launch_bounds__(kClusterThreads, 1) cluster_march_kernel(Clust
     }
   };
 
-  __syncthreads();  // twiddles
+  __syncthreads();  // tables
   row_phase(0);
   for (int i = 0; i + 1 < nz; i++) {
     cl.sync();  // every row slab holds the row-transformed field
-    // gather the column slab: K[y][xl] = R_{y/32}[y%32][32c + xl]
-    for (int e = threadIdx.x; e < N * kSlab; e += T) {
-      const int y = e >> 5, xl = e & 31;
-      const float2* Rr = cl.map_shared_rank(R, y >> 5);
-      K[y * KP + xl] = Rr[(y & 31) * N + c * kSlab + xl];
+    {
+      // gather the column slab K[y][xl] = R_{y/SLAB}[y%SLAB][SLAB c + xl]: all remote loads
+      // first, then the stores
+      float2 g[GA];
+#pragma unroll
+      for (int k = 0; k < GA; k++) {
+        const int e = threadIdx.x + k * T;
+        const int y = e / SLAB, xl = e % SLAB;
+        const float2* Rr = cl.map_shared_rank(R, y / SLAB);
+        g[k] = Rr[(y % SLAB) * N + c * SLAB + xl];
+      }
+#pragma unroll
+      for (int k = 0; k < GA; k++) {
+        const int e = threadIdx.x + k * T;
+        K[(e / SLAB) * KP + e % SLAB] = g[k];
+      }
+    }
+    if (stage_mask) {
+      // the rows of plane i+1's mask (or dn) this block will apply, fetched during the
+      // column pass
+      const size_t off = (size_t)(i + 1) * plane + (size_t)c * SLAB * N;
+      const char* src = p.mask ? reinterpret_cast<const char*>(p.mask + off)
+                               : static_cast<const char*>(p.dn) + ((size_t)gl * p.dn_bstride + off) * mes;
+      for (int o = threadIdx.x * 16; o < SLAB * N * mes; o += T * 16) cp_async16(MS + o, src + o);
+      cp_async_commit();
     }
     __syncthreads();
     float n_eff = q.prop_mode == 1 ? q.slice_n[i + 1] : q.n00f;
     if (q.prop_mode == 2) {
       // weighted: forward transforms, k-space back into the slab, tile partial sums
-      for (int xl = warp; xl < kSlab; xl += NW) {
+      for (int xl = warp; xl < SLAB; xl += NW) {
         float2 v[E];
 #pragma unroll
         for (int m = 0; m < E; m++) v[m] = K[(t + 32 * m) * KP + xl];
@@ -1315,8 +1370,8 @@ __global__ void __launch_bounds__(kClusterThreads, 1) cluster_march_kernel(Clust
       }
       __syncthreads();
       constexpr int PER = 16 * N / T;  // the warp kernels' element order within a tile
-      for (int tile = 0; tile < kSlab / 16; tile++) {
-        const int x0 = c * kSlab + tile * 16;
+      for (int tile = 0; tile < SLAB / 16; tile++) {
+        const int x0 = c * SLAB + tile * 16;
         float sdn = 0.f, su = 0.f;
 #pragma unroll
         for (int ii = 0; ii < PER; ii++) {
@@ -1340,7 +1395,7 @@ __global__ void __launch_bounds__(kClusterThreads, 1) cluster_march_kernel(Clust
         float dn_sum = 0.f, u_sum = 0.f;
         for (int r = 0; r < Cfg::C; r++) {
           const float* pr = cl.map_shared_rank(part, r);
-          for (int tile = 0; tile < kSlab / 16; tile++) {
+          for (int tile = 0; tile < SLAB / 16; tile++) {
             dn_sum += pr[2 * tile];
             u_sum += pr[2 * tile + 1];
           }
@@ -1352,27 +1407,36 @@ __global__ void __launch_bounds__(kClusterThreads, 1) cluster_march_kernel(Clust
       n_eff = q.n00f + dn0;  // mult_propagator_buff, bpm_3d_kernels.cl:482
     }
     const float nk = prop_nk(q, n_eff);
-    for (int xl = warp; xl < kSlab; xl += NW) {
-      const int x = c * kSlab + xl;
+    for (int xl = warp; xl < SLAB; xl += NW) {
+      const int x = c * SLAB + xl;
       float2 v[E];
 #pragma unroll
       for (int m = 0; m < E; m++) v[m] = K[(t + 32 * m) * KP + xl];
       if (q.prop_mode != 2) warp_fft<N, false>(v, buf, twc, t);
       float S = 0.f, G = 0.f;
+      const float2* htc = stage_ht ? HT + (size_t)xl * N : nullptr;
 #pragma unroll
       for (int m = 0; m < E; m++)
-        v[m] = prop_point<true>(q, v[m], x, t + 32 * m, nk, make_float2(0.f, 0.f), S, G, q.ky2);
+        v[m] = prop_point<true>(q, v[m], x, t + 32 * m, nk, make_float2(0.f, 0.f), S, G, KY, htc);
       warp_fft<N, true>(v, buf, twc, t);
 #pragma unroll
       for (int m = 0; m < E; m++) K[(t + 32 * m) * KP + xl] = v[m];
     }
     cl.sync();  // every column slab holds the propagated field
-    // gather the row slab back: R[yl][x] = K_{x/32}[32c + yl][x%32]
-    for (int e = threadIdx.x; e < kSlab * N; e += T) {
-      const int yl = e / N, x = e - yl * N;
-      const float2* Kr = cl.map_shared_rank(K, x >> 5);
-      R[yl * N + x] = Kr[(c * kSlab + yl) * KP + (x & 31)];
+    {
+      // gather the row slab back: R[yl][x] = K_{x/SLAB}[SLAB c + yl][x%SLAB]
+      float2 g[GA];
+#pragma unroll
+      for (int k = 0; k < GA; k++) {
+        const int e = threadIdx.x + k * T;
+        const int yl = e / N, x = e % N;
+        const float2* Kr = cl.map_shared_rank(K, x / SLAB);
+        g[k] = Kr[(c * SLAB + yl) * KP + x % SLAB];
+      }
+#pragma unroll
+      for (int k = 0; k < GA; k++) R[threadIdx.x + k * T] = g[k];
     }
+    if (stage_mask) cp_async_wait<0>();  // this thread's pieces of the next plane's mask rows
     __syncthreads();
     row_phase(i + 1);
   }
@@ -1908,6 +1972,11 @@ struct ClusterK {
     a.cp = c.cp;
     a.u0 = static_cast<const float2*>(r->u0);
     a.nz = pl->d.nz;
+    {
+      const int es = r->mask ? 8 : (r->dn_dtype == BPM_DN_C64 ? 8 : (r->dn_dtype == BPM_DN_F16 ? 2 : 4));
+      a.stage_mask = r->mask ? aligned16(r->mask)
+                             : (aligned16(r->dn) && ((size_t)r->dn_batch_stride * es) % 16 == 0);
+    }
     cudaLaunchAttribute at[1];
     cudaLaunchConfig_t cfg = config((unsigned)r->batch, s, at);
     BPM_CUDA_TRY(cudaLaunchKernelEx(&cfg, cluster_march_kernel<N>, a));
