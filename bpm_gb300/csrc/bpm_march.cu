@@ -1202,15 +1202,15 @@ struct ClusterArgs {
 
 template <int N>
 struct ClusterCfg {
-  static constexpr int SLAB = N <= 128 ? 16 : 32;  // rows (and columns) per block
-  static constexpr int C = N / SLAB;               // blocks per field
+  static constexpr int SLAB = 16;                  // rows (and columns) per block
+  static constexpr int C = N / SLAB;               // blocks per field (16 at 256: a non-portable size)
   static constexpr int NW = kClusterThreads / 32;
   static constexpr int TWPAD = (WarpFft<N>::TW + 1) & ~1;
   static constexpr int KP = SLAB + 1;              // column-slab row pitch (float2)
   static constexpr int GATHER = N * SLAB / kClusterThreads;  // slab elements per thread
-  // up to 128: the next plane's mask rows and this block's propagator-table columns are
-  // staged in shared memory as well (at 256 they would not fit)
-  static constexpr bool STAGE = N <= 128;
+  // the next plane's mask rows and this block's propagator-table columns are staged in
+  // shared memory as well
+  static constexpr bool STAGE = true;
   static constexpr size_t HT_F2 = STAGE ? (size_t)SLAB * N : 0;
   static constexpr size_t MS_F2 = STAGE ? (size_t)SLAB * N : 0;  // up to 8 bytes per element
   static constexpr size_t F2 = 2 * (size_t)TWPAD + (size_t)SLAB * N + (size_t)N * KP +
@@ -1951,6 +1951,8 @@ struct ClusterK {
   static bool ready() {
     if (state() < 0) {
       int ok = 0;
+      if (ClusterCfg<N>::C > 8)
+        cudaFuncSetAttribute(cluster_march_kernel<N>, cudaFuncAttributeNonPortableClusterSizeAllowed, 1);
       if (cudaFuncSetAttribute(cluster_march_kernel<N>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                (int)ClusterCfg<N>::SMEM) == cudaSuccess) {
         cudaLaunchAttribute at[1];
