@@ -1914,16 +1914,19 @@ int sink_copy(bpm_plan* pl, const bpm_request* r, const HostSink& h, int b0, int
   return BPM_OK;
 }
 
-// The whole-march cluster kernel serves square grids of 64, 128 or 256 without scattering
-// sums or checkpoints when BPM_GB300_CLUSTER=1. It is off by default: measured on GB300
-// (one field, Nz 128) it marches 128^2 at 1.1 and 256^2 at 2.5 G voxel-updates/s against
-// 2.0 and 5.6 for the pass kernels, since a field's march is confined to its N/32 SMs.
-bool cluster_enabled() {
-  static const bool on = [] {
+// The whole-march cluster kernel serves square grids without scattering sums or
+// checkpoints. Measured on GB300 (one field, Nz 128): at 128^2 it beats the pass kernels
+// (one 128^3 weighted request 1.26 vs 1.51 ms), at 256^2 it does not (1.60 vs 1.38 ms per
+// march), so by default it takes N = 64 and 128. BPM_GB300_CLUSTER=1 extends it to 256,
+// =0 turns it off.
+bool cluster_enabled(int n) {
+  static const int mode = [] {
     const char* e = getenv("BPM_GB300_CLUSTER");
-    return e && strcmp(e, "1") == 0;
+    if (e && strcmp(e, "0") == 0) return 0;
+    if (e && strcmp(e, "1") == 0) return 2;
+    return 1;
   }();
-  return on;
+  return mode == 2 || (mode == 1 && n <= 128);
 }
 
 template <int N>
@@ -1991,7 +1994,7 @@ struct ClusterK {
 constexpr int kNotCluster = 1;
 int try_cluster_march(const bpm_plan* pl, const bpm_request* r, void* ws, cudaStream_t s) {
   const bpm_grid_desc& d = pl->d;
-  if (!cluster_enabled() || d.nx != d.ny || r->scatter_p || r->ckpt || !pl->wtw_x || !pl->wtw_y) return kNotCluster;
+  if (d.nx != d.ny || !cluster_enabled(d.nx) || r->scatter_p || r->ckpt || !pl->wtw_x || !pl->wtw_y) return kNotCluster;
   switch (d.nx) {
     case 64: return ClusterK<64>::ready() ? ClusterK<64>::launch(pl, r, ws, s) : kNotCluster;
     case 128: return ClusterK<128>::ready() ? ClusterK<128>::launch(pl, r, ws, s) : kNotCluster;
