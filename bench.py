@@ -362,8 +362,7 @@ def single_request_timing(reps=5):
     import bpm_gb300
     out = {}
     n = 128
-    z, y, x = np.meshgrid(np.arange(n), np.arange(n), np.arange(n), indexing="ij")
-    dn1 = (.05 * (((x - n / 2) ** 2 + (y - n / 2) ** 2 + (z - n / 2) ** 2) <= 20 ** 2)).astype(np.float32)
+    dn1 = config1_dn(n)
     dn2 = sphere_pool(256, 256, SEED + 2).contiguous()
     u02 = bpm_gb300.psf_u0((256, 256), (.1, .1), zfoc=12.8, NA=.4, lam=.5, n0=1.33, device=True)
     cases = [("config1_128cube_plain", (n, n, n), torch.from_numpy(dn1).cuda(), None, "weighted", dn1),
@@ -495,11 +494,27 @@ def serve_trace(n=2000, rate=200., seed=0):
             "workload": "config-5 trace, seeded Poisson arrivals, all requests latency-measured"}
 
 
+def config1_dn(n=128):
+    """Config 1's dn: one centred sphere of radius 20 px and dn 0.05 in an n^3 grid."""
+    z, y, x = np.meshgrid(np.arange(n), np.arange(n), np.arange(n), indexing="ij")
+    return (.05 * (((x - n / 2) ** 2 + (y - n / 2) ** 2 + (z - n / 2) ** 2) <= 20 ** 2)).astype(np.float32)
+
+
 def profile_run(args):
-    """The device march alone (same buffers as the timed region), for ncu captures."""
+    """The device march alone (same buffers as the timed region), for ncu captures;
+    --profile-case config1: one 128^3 weighted request through bpm_3d per step instead."""
     import torch
     import bpm_gb300
     torch.cuda.set_device(0)
+    if args.profile_case == "config1":
+        dn1 = torch.from_numpy(config1_dn()).cuda()
+        for _ in range(args.warmup + args.steps):
+            u = bpm_gb300.bpm_3d((128, 128, 128), UNITS, lam=LAM, n0=N0, dn=dn1, mean_mode="weighted",
+                                 return_field=False)
+        torch.cuda.synchronize()
+        print(json.dumps({"profile_run": True, "case": "config1", "sum": float(u.sum()),
+                          "launches": bpm_gb300.launch_count()}))
+        return
     dn = make_dn_device(NX, NY, NZ, SEED)
     march = bpm_gb300.BatchedMarch((NX, NY, NZ), UNITS, LAM, N0, BATCH, dn=dn, mean_mode=MODE,
                                    out_kind="intensity", group=args.group)
@@ -579,6 +594,8 @@ def main():
     ap.add_argument("--nz", type=int, default=NZ, help="z planes (smaller for profiling)")
     ap.add_argument("--profile", action="store_true",
                     help="only the device march (warm-up + steps), for ncu launch lists")
+    ap.add_argument("--profile-case", default="batched", choices=["batched", "config1"],
+                    help="with --profile: the batched march, or one 128^3 weighted request per step")
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3

@@ -24,6 +24,7 @@
 // dn slice is read from HBM once for the whole group.
 #include <algorithm>
 #include <cmath>
+#include <cstdlib>
 #include <cstring>
 #include <string>
 #include <vector>
@@ -37,6 +38,18 @@
 using namespace bpmgb;
 
 static const float PI_F = 3.14159265358979f;  // bpm_3d_kernels.cl:3
+
+// field groups a batch may march at the same time (one workspace slot and stream each):
+// conc_limit() of them, 4 unless BPM_GB300_CONC (1..8) says otherwise
+constexpr int kMaxConcurrentGroups = 8;
+static int conc_limit() {
+  static const int v = [] {
+    const char* e = getenv("BPM_GB300_CONC");
+    const int c = e ? atoi(e) : 4;
+    return c < 1 ? 1 : (c > kMaxConcurrentGroups ? kMaxConcurrentGroups : c);
+  }();
+  return v;
+}
 
 struct bpm_plan {
   bpm_grid_desc d;
@@ -55,19 +68,16 @@ struct bpm_plan {
   float k0f, dzf, n0f, unit_k;
   double k0;
   // streams on which groups of fields march concurrently, with their fork/join events
-  cudaStream_t aux[4];
-  cudaEvent_t ev_fork, ev_join[4];
+  cudaStream_t aux[kMaxConcurrentGroups];
+  cudaEvent_t ev_fork, ev_join[kMaxConcurrentGroups];
   // device->host streaming of the output volume (bpm_propagate_to_host): the copy stream,
   // one "planes ready" event per march stream, and the final join
   cudaStream_t copy;
-  cudaEvent_t ev_ready[4], ev_copied;
+  cudaEvent_t ev_ready[kMaxConcurrentGroups], ev_copied;
   int max_pitch;
   // false for a plan made by bpm_plan_derive: the device tables belong to its base plan
   bool owns_tables;
 };
-
-// field groups a batch may march at the same time (one workspace slot each)
-constexpr int kMaxConcurrentGroups = 4;
 
 struct bpm_exec {
   cudaGraphExec_t exec;
@@ -202,13 +212,6 @@ struct RowParams {
 __device__ __forceinline__ float load_dn_real(const void* dn, int dtype, size_t idx) {
   if (dtype == BPM_DN_F16) return __half2float(reinterpret_cast<const __half*>(dn)[idx]);
   return __ldg(reinterpret_cast<const float*>(dn) + idx);
-}
-
-// two consecutive real dn values (x even)
-__device__ __forceinline__ float2 load_dn_pair(const void* dn, int dtype, size_t idx) {
-  if (dtype == BPM_DN_F16)
-    return __half22float2(*reinterpret_cast<const __half2*>(reinterpret_cast<const __half*>(dn) + idx));
-  return __ldg(reinterpret_cast<const float2*>(reinterpret_cast<const float*>(dn) + idx));
 }
 
 // The pointwise work of a row pass on one element v = u(x, y) of plane z, shared by the
@@ -815,11 +818,18 @@ row_shared_kernel(RowParams p, int nfields) {
 // memory, then every warp takes its column into registers. WHICH: 0 = forward FFT,
 // propagator, inverse FFT; 1 = forward FFT + weighted-mode partial sums (k-space stored
 // back); 2 = n from the partial sums, propagator, inverse FFT.
+// Addressing: in the coalesced mapping thread (r0, cc) = (tid / 16, tid % 16) handles rows
+// r0 + 32 i of column x0 + cc, so its tile slots are tile_idx(r0, cc) + 512 i and its plane
+// elements gofs + 32 nx i (32-bit: a plane has at most 2^19 elements here); warp w's column
+// slots are tile_idx(t, w) + 512 m. The common cases (table propagator, FP32 recipe without
+// scattering sums, staged dn) run loops free of per-element branches with the arithmetic
+// of the general path in the same order, so they give the same bits.
 template <int N, int WHICH>
 __global__ void __launch_bounds__(kColWarps * 32, 2)
 col_warp_kernel(ColParams p) {
   constexpr int E = N / 32;
   constexpr int T = kColWarps * 32;
+  static_assert(T == 512, "the coalesced mapping steps 32 rows at a time");
   extern __shared__ float2 smem[];
   float2* tw = smem;
   float2* tile = smem + N;  // the 16 x N tile, then the warps' exchange buffers
@@ -831,6 +841,10 @@ col_warp_kernel(ColParams p) {
   const int x = x0 + warp;
   float2* Wp = p.W + (size_t)gl * p.nx * N;
   constexpr int PER = 16 * N / T;
+  const int r0 = threadIdx.x >> 4, cc = threadIdx.x & 15;
+  const unsigned gstep = 32u * (unsigned)p.nx;
+  const int ts = (r0 << 4) + (cc ^ (r0 & 15));  // tile_idx(r0 + 32 i, cc) - 512 i
+  const int tc = (t << 4) + (warp ^ (t & 15));  // tile_idx(t + 32 m, warp) - 512 m
   static_assert(WarpFft<N>::TW <= T && N <= T, "one twiddle and one ky^2 entry per thread");
   // plan constants first (the twiddle table; the propagator recipe's ky^2 column, staged
   // next to the tile), then the wait for the previous pass
@@ -841,88 +855,129 @@ col_warp_kernel(ColParams p) {
   dep_wait();
   dep_release();
   // weighted reduction: dn slice 0 of this tile goes to shared memory with cp.async now and
-  // is read only after the transform
+  // is read only after the transform; a 16-value row is 2^lg 16-byte pieces
   const char* dn_stage = nullptr;
   if (WHICH == 1 && p.dn && p.dn_stage) {
-    const int es = p.dn_dtype == BPM_DN_F16 ? 2 : 4;
+    const int lg = p.dn_dtype == BPM_DN_F16 ? 1 : 2;
+    const int es = 1 << lg;
     char* dst = reinterpret_cast<char*>(smem + WarpCfg<N>::COL_F2);
     const char* srcb = static_cast<const char*>(p.dn) + ((size_t)gl * p.dn_bstride + x0) * es;
-    for (int ch = threadIdx.x; ch < N * es; ch += T) {  // es 16-byte pieces per 16-value row
-      const int n = ch / es, j = ch - n * es;
-      cp_async16(dst + (size_t)ch * 16, srcb + (size_t)n * p.nx * es + j * 16);
-    }
+    const size_t rowb = (size_t)p.nx * es;
+    for (int ch = threadIdx.x; ch < (N << lg); ch += T)
+      cp_async16(dst + (size_t)ch * 16, srcb + (size_t)(ch >> lg) * rowb + (ch & (es - 1)) * 16);
     cp_async_commit();
     dn_stage = dst;
   }
   // the tile loads go out before any shared-memory store waits on them
   float2 ld[PER];
+  {
+    const unsigned gofs = (unsigned)r0 * (unsigned)p.nx + (unsigned)(x0 + cc);
 #pragma unroll
-  for (int i = 0; i < PER; i++) {
-    const int e = threadIdx.x + i * T;
-    ld[i] = Wp[(size_t)(e >> 4) * p.nx + x0 + (e & 15)];
+    for (int i = 0; i < PER; i++) ld[i] = Wp[gofs + i * gstep];
   }
-  if (WHICH == 2 && threadIdx.x == 0) {
-    // every block of the field sums the partials in the same order: identical results
-    const float* part = p.red_part + (size_t)gl * (p.nx / 16) * 2;
+  if (WHICH == 2 && warp == 0) {
+    // every block of the field sums the partials in index order, so all get the same n; the
+    // lanes fetch them at once (at most 64: nx <= 1024) and pass them on by shuffles
+    const int np = p.nx / 16;
+    const float* part = p.red_part + (size_t)gl * np * 2;
+    const float d0 = t < np ? part[2 * t] : 0.f, u0 = t < np ? part[2 * t + 1] : 0.f;
+    const float d1 = t + 32 < np ? part[2 * t + 64] : 0.f, u1 = t + 32 < np ? part[2 * t + 65] : 0.f;
     float dn_sum = 0.f, u_sum = 0.f;
-    for (int i = 0; i < p.nx / 16; i++) {
-      dn_sum += part[2 * i];
-      u_sum += part[2 * i + 1];
+    for (int i = 0; i < np; i++) {
+      dn_sum += __shfl_sync(0xffffffffu, i < 32 ? d0 : d1, i & 31);
+      u_sum += __shfl_sync(0xffffffffu, i < 32 ? u0 : u1, i & 31);
     }
-    const float dn0 = dn_sum / u_sum;  // mult_dn_mean_buff, bpm_3d_kernels.cl:117
-    s_n = p.n00f + dn0;                // mult_propagator_buff, bpm_3d_kernels.cl:482
-    if (blockIdx.x == 0) p.dn0_field[gl] = dn0;
+    if (t == 0) {
+      const float dn0 = dn_sum / u_sum;  // mult_dn_mean_buff, bpm_3d_kernels.cl:117
+      s_n = p.n00f + dn0;                // mult_propagator_buff, bpm_3d_kernels.cl:482
+      if (blockIdx.x == 0) p.dn0_field[gl] = dn0;
+    }
   }
 #pragma unroll
-  for (int i = 0; i < PER; i++) {
-    const int e = threadIdx.x + i * T;
-    tile[tile_idx(e >> 4, e & 15)] = ld[i];
-  }
+  for (int i = 0; i < PER; i++) tile[ts + 512 * i] = ld[i];
   if (threadIdx.x < WarpFft<N>::TW) tw[threadIdx.x] = twv;
   if (stage_ky && threadIdx.x < N) sky2[threadIdx.x] = kyv;
   __syncthreads();
   float2 v[E];
 #pragma unroll
-  for (int m = 0; m < E; m++) v[m] = tile[tile_idx(t + 32 * m, warp)];
+  for (int m = 0; m < E; m++) v[m] = tile[tc + 512 * m];
   __syncthreads();
   float2* buf = tile + warp * WarpFft<N>::BUF;
   if (WHICH != 2) warp_fft<N, false>(v, buf, tw, t);
   if (WHICH != 1) {
     const float n_eff = WHICH == 2 ? s_n : (p.prop_mode == 1 ? p.slice_n[p.z + 1] : p.n00f);
     const float nk = prop_nk(p, n_eff);
-    const float2 plain = (p.scat && x == 0) ? plain_wave(p) : make_float2(0.f, 0.f);
-    float S = 0.f, G = 0.f;
+    if (!p.scat && p.prop_mode == 0) {
+      // table H, transposed so the column is contiguous; conj(H) for the adjoint
+      const float2* hp = p.Ht + (size_t)x * p.ny + t;
+      const bool cj = p.conj_h;
 #pragma unroll
-    for (int m = 0; m < E; m++) v[m] = prop_point<true>(p, v[m], x, t + 32 * m, nk, plain, S, G, sky2);
-    if (p.scat) scat_partials_store<T>(p, S, G, gl, red);
+      for (int m = 0; m < E; m++) {
+        float2 h = __ldg(hp + 32 * m);
+        if (cj) h.y = -h.y;
+        v[m] = cscale(cmul(v[m], h), p.scale);
+      }
+    } else if (!p.scat) {
+      // FP32 recipe of bpm_3d_kernels.cl:408-432 on the staged ky^2 column
+      const float nkx = __fsub_rn(nk, __ldg(p.kx2 + x));
+#pragma unroll
+      for (int m = 0; m < E; m++) {
+        const float tmp = __fsub_rn(nkx, sky2[t + 32 * m]);
+        float2 h = make_float2(0.f, 0.f);
+        if (tmp >= 0.f) {
+          const float ph = __fmul_rn(-p.dzf, __fsqrt_rn(tmp));
+          sincosf(ph, &h.y, &h.x);
+        }
+        v[m] = cscale(cmul(v[m], h), p.scale);
+      }
+    } else {
+      const float2 plain = x == 0 ? plain_wave(p) : make_float2(0.f, 0.f);
+      float S = 0.f, G = 0.f;
+#pragma unroll
+      for (int m = 0; m < E; m++) v[m] = prop_point<true>(p, v[m], x, t + 32 * m, nk, plain, S, G, sky2);
+      scat_partials_store<T>(p, S, G, gl, red);
+    }
     warp_fft<N, true>(v, buf, tw, t);
   }
   __syncthreads();
 #pragma unroll
-  for (int m = 0; m < E; m++) tile[tile_idx(t + 32 * m, warp)] = v[m];
+  for (int m = 0; m < E; m++) tile[tc + 512 * m] = v[m];
   if (WHICH == 1 && dn_stage) cp_async_wait<0>();  // this thread's dn pieces have landed
   __syncthreads();
+  const unsigned gofs = (unsigned)(threadIdx.x >> 4) * (unsigned)p.nx + (unsigned)(x0 + (threadIdx.x & 15));
   if (WHICH == 1) {
     // weighted mode: sum |u_hat| and |u_hat|*dn over the tile while storing it, with the
     // coalesced tile mapping (dn slice 0 read 16 columns at a time)
     float sdn = 0.f, su = 0.f;
+    if (dn_stage && p.dn_dtype != BPM_DN_F16) {
+      const float* ds = reinterpret_cast<const float*>(dn_stage) + threadIdx.x;
+#pragma unroll
+      for (int i = 0; i < PER; i++) {
+        const float2 u = tile[ts + 512 * i];
+        Wp[gofs + i * gstep] = u;
+        const float a = __fsqrt_rn(cabs2(u));
+        su += a;
+        sdn = fmaf(a, ds[T * i], sdn);
+      }
+    } else if (dn_stage) {
+      const __half* ds = reinterpret_cast<const __half*>(dn_stage) + threadIdx.x;
+#pragma unroll
+      for (int i = 0; i < PER; i++) {
+        const float2 u = tile[ts + 512 * i];
+        Wp[gofs + i * gstep] = u;
+        const float a = __fsqrt_rn(cabs2(u));
+        su += a;
+        sdn = fmaf(a, __half2float(ds[T * i]), sdn);
+      }
+    } else {
 #pragma unroll 4
-    for (int i = 0; i < PER; i++) {
-      const int e = threadIdx.x + i * T;
-      const int n = e >> 4, c = e & 15;
-      const float2 u = tile[tile_idx(n, c)];
-      const size_t k = (size_t)n * p.nx + x0 + c;
-      Wp[k] = u;
-      const float a = __fsqrt_rn(cabs2(u));
-      su += a;
-      if (p.dn) {
-        float d;
-        if (dn_stage)
-          d = p.dn_dtype == BPM_DN_F16 ? __half2float(reinterpret_cast<const __half*>(dn_stage)[e])
-                                       : reinterpret_cast<const float*>(dn_stage)[e];
-        else
-          d = load_dn_real(p.dn, p.dn_dtype, gl * p.dn_bstride + k);
-        sdn = fmaf(a, d, sdn);
+      for (int i = 0; i < PER; i++) {
+        const float2 u = tile[ts + 512 * i];
+        const unsigned k = gofs + i * gstep;
+        Wp[k] = u;
+        const float a = __fsqrt_rn(cabs2(u));
+        su += a;
+        if (p.dn) sdn = fmaf(a, load_dn_real(p.dn, p.dn_dtype, gl * p.dn_bstride + k), sdn);
       }
     }
     block_sum2<T>(sdn, su, red);
@@ -932,7 +987,193 @@ col_warp_kernel(ColParams p) {
       o[1] = su;
     }
   } else {
-    col_store<N, T>(tile, Wp, p.nx, x0);
+#pragma unroll
+    for (int i = 0; i < PER; i++) Wp[gofs + i * gstep] = tile[ts + 512 * i];
+  }
+}
+
+// Column pass without the tile transposition (128 <= N <= 512, no scattering sums). The
+// block's 512 threads load 16 columns in the coalesced tile mapping — thread (r0, cc) holds
+// rows r0 + 32 i of column x0 + cc — and keep that mapping for every pointwise step (the
+// propagator from the row-major table or the FP32 recipe, the weighted partial sums, the
+// loads and stores); the first and last FFT stages run in it as well (colsplit_first /
+// colsplit_last) and only the middle stages per warp, on the column's exchange buffer. WHICH
+// as col_warp_kernel, whose results it reproduces bit for bit.
+template <int N>
+struct ColSplitCfg {
+  static constexpr int TW_F2 = (WarpFft<N>::TW + 1) & ~1;
+  static constexpr int DN_F2 = (TW_F2 + kColWarps * ColSplit<N>::STRIDE + 1) & ~1;  // 16-byte aligned
+  static constexpr size_t SMEM = (size_t)DN_F2 * sizeof(float2);
+  static constexpr size_t SMEM_DN = SMEM + (size_t)16 * N * sizeof(float);  // + dn slice 0 of the tile
+  static constexpr size_t SMEM_KY = SMEM + (size_t)N * sizeof(float);       // + the ky^2 column
+};
+
+// the propagator on the thread's rows r0 + 32 i of column x (prop_point's arithmetic without
+// the scattering sums): the row-major table H (conj(H) for the adjoint) or the FP32 recipe
+// with kx^2 of the column and the ky^2 table staged in shared memory
+template <int N>
+__device__ __forceinline__ void propagate_rows(const ColParams& p, float2 (&v)[N / 32], int x, int r0,
+                                               float n_eff, float kx2, const float* sky2) {
+  const unsigned step = 32u * (unsigned)p.nx;
+  if (p.prop_mode == 0) {
+    const float2* hp = p.H + ((unsigned)r0 * (unsigned)p.nx + (unsigned)x);
+    const bool cj = p.conj_h;
+#pragma unroll
+    for (int i = 0; i < N / 32; i++) {
+      float2 h = __ldg(hp + i * step);
+      if (cj) h.y = -h.y;
+      v[i] = cscale(cmul(v[i], h), p.scale);
+    }
+  } else {
+    const float nkx = __fsub_rn(prop_nk(p, n_eff), kx2);
+#pragma unroll
+    for (int i = 0; i < N / 32; i++) {
+      const float tmp = __fsub_rn(nkx, sky2[r0 + 32 * i]);
+      float2 h = make_float2(0.f, 0.f);
+      if (tmp >= 0.f) {
+        const float ph = __fmul_rn(-p.dzf, __fsqrt_rn(tmp));
+        sincosf(ph, &h.y, &h.x);
+      }
+      v[i] = cscale(cmul(v[i], h), p.scale);
+    }
+  }
+}
+
+template <int N, int WHICH>
+__global__ void __launch_bounds__(kColWarps * 32, 2)
+col_split_kernel(ColParams p) {
+  constexpr int E = N / 32;
+  constexpr int T = kColWarps * 32;
+  static_assert(T == 512, "32 threads per column");
+  extern __shared__ __align__(16) float2 smem[];
+  float2* tw = smem;
+  float2* bufs = smem + ColSplitCfg<N>::TW_F2;
+  __shared__ float red[64];
+  __shared__ float s_n;
+  const int warp = threadIdx.x >> 5, t = threadIdx.x & 31;
+  const int r0 = threadIdx.x >> 4, cc = threadIdx.x & 15;
+  const int gl = blockIdx.y;
+  const int x0 = blockIdx.x * kColWarps;
+  float2* Wp = p.W + (size_t)gl * p.nx * N;
+  const unsigned gstep = 32u * (unsigned)p.nx;
+  float2* colbuf = bufs + cc * ColSplit<N>::STRIDE;  // column x0 + cc: the tile-mapping stages
+  float2* wbuf = bufs + warp * ColSplit<N>::STRIDE;  // column x0 + warp: the middle stages
+  static_assert(WarpFft<N>::TW <= T && N <= T, "one twiddle and one ky^2 entry per thread");
+  // plan constants before the wait for the previous pass: the twiddles, and for the FP32
+  // recipe kx^2 of the thread's column and one ky^2 entry per thread (staged after it, in the
+  // region the weighted reduction uses for dn)
+  const float2 twv = threadIdx.x < WarpFft<N>::TW ? p.wtw[threadIdx.x] : make_float2(0.f, 0.f);
+  const bool recipe = WHICH != 1 && p.prop_mode != 0;
+  const float kx2v = recipe ? __ldg(p.kx2 + x0 + cc) : 0.f;
+  const float kyv = (recipe && threadIdx.x < N) ? __ldg(p.ky2 + threadIdx.x) : 0.f;
+  float* sky2 = reinterpret_cast<float*>(smem + ColSplitCfg<N>::DN_F2);
+  dep_wait();
+  dep_release();
+  // weighted reduction: dn slice 0 of this tile goes to shared memory with cp.async now and
+  // is read after the transform; a 16-value row is 2^lg 16-byte pieces
+  const char* dn_stage = nullptr;
+  if (WHICH == 1 && p.dn && p.dn_stage) {
+    const int lg = p.dn_dtype == BPM_DN_F16 ? 1 : 2;
+    const int es = 1 << lg;
+    char* dst = reinterpret_cast<char*>(smem + ColSplitCfg<N>::DN_F2);
+    const char* srcb = static_cast<const char*>(p.dn) + ((size_t)gl * p.dn_bstride + x0) * es;
+    const size_t rowb = (size_t)p.nx * es;
+    for (int ch = threadIdx.x; ch < (N << lg); ch += T)
+      cp_async16(dst + (size_t)ch * 16, srcb + (size_t)(ch >> lg) * rowb + (ch & (es - 1)) * 16);
+    cp_async_commit();
+    dn_stage = dst;
+  }
+  float2 v[E];
+  {
+    const unsigned gofs = (unsigned)r0 * (unsigned)p.nx + (unsigned)(x0 + cc);
+#pragma unroll
+    for (int i = 0; i < E; i++) v[i] = Wp[gofs + i * gstep];
+  }
+  if (WHICH == 2 && warp == 0) {
+    // as col_warp_kernel: the partials summed in index order, fetched at once by the lanes
+    const int np = p.nx / 16;
+    const float* part = p.red_part + (size_t)gl * np * 2;
+    const float d0 = t < np ? part[2 * t] : 0.f, u0 = t < np ? part[2 * t + 1] : 0.f;
+    const float d1 = t + 32 < np ? part[2 * t + 64] : 0.f, u1 = t + 32 < np ? part[2 * t + 65] : 0.f;
+    float dn_sum = 0.f, u_sum = 0.f;
+    for (int i = 0; i < np; i++) {
+      dn_sum += __shfl_sync(0xffffffffu, i < 32 ? d0 : d1, i & 31);
+      u_sum += __shfl_sync(0xffffffffu, i < 32 ? u0 : u1, i & 31);
+    }
+    if (t == 0) {
+      const float dn0 = dn_sum / u_sum;  // mult_dn_mean_buff, bpm_3d_kernels.cl:117
+      s_n = p.n00f + dn0;                // mult_propagator_buff, bpm_3d_kernels.cl:482
+      if (blockIdx.x == 0) p.dn0_field[gl] = dn0;
+    }
+  }
+  if (threadIdx.x < WarpFft<N>::TW) tw[threadIdx.x] = twv;
+  if (recipe && threadIdx.x < N) sky2[threadIdx.x] = kyv;
+  if (WHICH == 2) {
+    __syncthreads();  // s_n, ky^2
+    propagate_rows<N>(p, v, x0 + cc, r0, s_n, kx2v, sky2);
+  } else {
+    // forward column FFT
+    colsplit_first<N, false>(v, colbuf, r0);
+    __syncthreads();
+    colsplit_middle<N, false>(wbuf, tw, t);
+    __syncthreads();
+    colsplit_last<N, false>(v, colbuf, tw, r0);
+  }
+  if (WHICH == 0) {
+    propagate_rows<N>(p, v, x0 + cc, r0, p.prop_mode == 1 ? p.slice_n[p.z + 1] : p.n00f, kx2v, sky2);
+    __syncthreads();  // every thread has read its last-stage inputs before the buffers are reused
+  }
+  if (WHICH != 1) {
+    // inverse column FFT, then the coalesced store
+    colsplit_first<N, true>(v, colbuf, r0);
+    __syncthreads();
+    colsplit_middle<N, true>(wbuf, tw, t);
+    __syncthreads();
+    colsplit_last<N, true>(v, colbuf, tw, r0);
+    const unsigned gofs = (unsigned)r0 * (unsigned)p.nx + (unsigned)(x0 + cc);
+#pragma unroll
+    for (int i = 0; i < E; i++) Wp[gofs + i * gstep] = v[i];
+  } else {
+    // weighted mode: store k-space and sum |u_hat| and |u_hat|*dn over the tile, each thread
+    // over its rows in order (col_warp_kernel's order)
+    if (dn_stage) cp_async_wait<0>();
+    __syncthreads();  // the dn pieces other threads copied
+    const unsigned gofs = (unsigned)r0 * (unsigned)p.nx + (unsigned)(x0 + cc);
+    float sdn = 0.f, su = 0.f;
+    if (dn_stage && p.dn_dtype != BPM_DN_F16) {
+      const float* ds = reinterpret_cast<const float*>(dn_stage) + threadIdx.x;
+#pragma unroll
+      for (int i = 0; i < E; i++) {
+        Wp[gofs + i * gstep] = v[i];
+        const float a = __fsqrt_rn(cabs2(v[i]));
+        su += a;
+        sdn = fmaf(a, ds[T * i], sdn);
+      }
+    } else if (dn_stage) {
+      const __half* ds = reinterpret_cast<const __half*>(dn_stage) + threadIdx.x;
+#pragma unroll
+      for (int i = 0; i < E; i++) {
+        Wp[gofs + i * gstep] = v[i];
+        const float a = __fsqrt_rn(cabs2(v[i]));
+        su += a;
+        sdn = fmaf(a, __half2float(ds[T * i]), sdn);
+      }
+    } else {
+#pragma unroll
+      for (int i = 0; i < E; i++) {
+        const unsigned k = gofs + i * gstep;
+        Wp[k] = v[i];
+        const float a = __fsqrt_rn(cabs2(v[i]));
+        su += a;
+        if (p.dn) sdn = fmaf(a, load_dn_real(p.dn, p.dn_dtype, gl * p.dn_bstride + k), sdn);
+      }
+    }
+    block_sum2<T>(sdn, su, red);
+    if (threadIdx.x == 0) {
+      float* o = p.red_part + ((size_t)gl * (p.nx / 16) + blockIdx.x) * 2;
+      o[0] = sdn;
+      o[1] = su;
+    }
   }
 }
 
@@ -943,8 +1184,7 @@ col_warp_kernel(ColParams p) {
 // cp.async while it transforms the current one, so the global-memory latency of one item
 // hides behind the arithmetic of the previous one instead of stalling every block of a
 // single wave at the same time. Same arithmetic, in the same order, as the warp kernels
-// above; the two agree to FP32 rounding (the compiler is free to contract their complex
-// products into FMAs differently), and each is deterministic on its own.
+// above, and the same bits (every multiply-add of the shared arithmetic is an explicit fmaf).
 // ---------------------------------------------------------------------------------------
 template <int N>
 struct PipeCfg {
@@ -1460,6 +1700,16 @@ struct SizeDispatch;
 // BPM_GB300_KERNELS=warp / =pipe forces one family.
 thread_local bool t_single_group = false;
 
+// column passes of 128..512 without scattering sums run col_split_kernel;
+// BPM_GB300_COLSPLIT=0 selects col_warp_kernel instead (the same bits)
+bool colsplit_enabled() {
+  static const bool on = [] {
+    const char* e = getenv("BPM_GB300_COLSPLIT");
+    return !(e && strcmp(e, "0") == 0);
+  }();
+  return on;
+}
+
 bool pipe_enabled() {
   static const int forced = [] {
     const char* e = getenv("BPM_GB300_KERNELS");
@@ -1592,6 +1842,9 @@ struct ColK {
     static int cap = 0;
     return cap;
   }
+  static constexpr size_t split_smem() {
+    return WHICH == 1 ? ColSplitCfg<N>::SMEM_DN : ColSplitCfg<N>::SMEM_KY;
+  }
   static void prepare() {
     static bool attr = false;
     if (!attr) {
@@ -1600,6 +1853,8 @@ struct ColK {
         cudaFuncSetAttribute(col_pipe_kernel<N, WHICH>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                              (int)PipeCfg<N>::COL_SMEM);
         pipe_cap() = resident_blocks(col_pipe_kernel<N, WHICH>, kColWarps * 32, PipeCfg<N>::COL_SMEM);
+        cudaFuncSetAttribute(col_split_kernel<N, WHICH>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                             (int)split_smem());
       }
       attr = true;
     }
@@ -1612,6 +1867,11 @@ struct ColK {
         BPM_CUDA_TRY(launch_dep(col_pipe_kernel<N, WHICH>, dim3(balanced_workers(ntiles, pipe_cap())),
                                 dim3(kColWarps * 32), PipeCfg<N>::COL_SMEM, s, p, ntiles));
         BPM_LAUNCH_CHECK("col_pipe_kernel");
+        return BPM_OK;
+      }
+      if (!p.scat && colsplit_enabled()) {
+        BPM_CUDA_TRY(launch_dep(col_split_kernel<N, WHICH>, g, dim3(kColWarps * 32), split_smem(), s, p));
+        BPM_LAUNCH_CHECK("col_split_kernel");
         return BPM_OK;
       }
     }
@@ -2031,7 +2291,7 @@ int enqueue_march(bpm_plan* pl, const bpm_request* r, void* ws, size_t ws_bytes,
   const int ngroups = (r->batch + G - 1) / G;
   const size_t slot = ws_layout(pl, G).total;
   const int conc = std::max(
-      1, (int)std::min<size_t>({(size_t)ngroups, ws_bytes / slot, (size_t)kMaxConcurrentGroups}));
+      1, (int)std::min<size_t>({(size_t)ngroups, ws_bytes / slot, (size_t)conc_limit()}));
   struct SingleGroupScope {  // kernel family of this march (pipe_enabled)
     explicit SingleGroupScope(bool v) { t_single_group = v; }
     ~SingleGroupScope() { t_single_group = false; }
@@ -2407,7 +2667,7 @@ extern "C" size_t bpm_workspace_bytes(const bpm_plan* pl, int batch, int group) 
   if (!pl || batch < 1) return 0;
   const int G = group > 0 ? std::min(group, batch) : default_group(pl, batch);
   const int ngroups = (batch + G - 1) / G;
-  return (size_t)std::min(ngroups, kMaxConcurrentGroups) * ws_layout(pl, G).total;
+  return (size_t)std::min(ngroups, conc_limit()) * ws_layout(pl, G).total;
 }
 
 extern "C" int bpm_propagate(bpm_plan* pl, const bpm_request* r, void* ws, size_t ws_bytes, void* stream) {

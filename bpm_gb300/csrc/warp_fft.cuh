@@ -148,4 +148,100 @@ __device__ __forceinline__ void warp_fft(float2 (&v)[N / 32], float2* buf, const
   warp_fft_from<N, 1, INV>(v, buf, tw, t);
 }
 
+// ---- column-split transform ------------------------------------------------------------
+// A block of 512 threads holding 16 length-N columns in the coalesced tile mapping — thread
+// (r0, cc) = (tid / 16, tid % 16) holds rows r0 + 32 i, i = 0 .. N/32-1, of column cc — can
+// run the first and the last Stockham stage without an exchange: the first stage's butterfly
+// j = r0 reads rows r0 + 32 r, and the last stage (stride NS_LAST >= 32, radix N/NS_LAST)
+// has butterflies j = r0 + 32 q writing rows j + NS_LAST r, which are rows r0 + 32 i again.
+// Only the middle stages run per warp (warp w on column w) through the column's exchange
+// buffer. Butterflies, twiddle entries and operation order are warp_fft's, so a column gets
+// the same bits as from warp_fft, while the tile transposition through shared memory (a
+// store and a load per element on each side of the transform) disappears.
+__host__ __device__ constexpr int colsplit_last_ns(int N) {
+  int ns = 1;
+  const int E = N / 32;
+  while (true) {
+    const int rs = (N / ns) < E ? (N / ns) : E;
+    if (ns * rs == N) return ns;
+    ns *= rs;
+  }
+}
+
+template <int N>
+struct ColSplit {
+  static constexpr int E = N / 32;
+  static constexpr int NS_LAST = colsplit_last_ns(N);
+  // column buffers are STRIDE float2 apart; an odd stride puts the 16 columns a half-warp
+  // touches in the tile mapping on 16 different bank pairs
+  static constexpr int STRIDE = WarpFft<N>::BUF | 1;
+  static_assert(NS_LAST >= 32 && NS_LAST < N, "last stage spans whole 32-row groups");
+};
+
+// first stage (radix E, stride 1) of column cc from the thread's rows r0 + 32 r, written to
+// positions r0*E + r of the column's buffer (padded index p + p/16; r0*E + r stays inside
+// one 16-element run, so the pad is that of r0*E)
+template <int N, bool INV>
+__device__ __forceinline__ void colsplit_first(const float2 (&v)[N / 32], float2* colbuf, int r0) {
+  constexpr int E = N / 32;
+  float2 a[E];
+#pragma unroll
+  for (int r = 0; r < E; r++) a[r] = v[r];
+  Dft<E, INV>::run(a);
+  float2* b = colbuf + r0 * E + ((r0 * E) >> 4);
+#pragma unroll
+  for (int r = 0; r < E; r++) b[r] = a[r];
+}
+
+// middle stages (stride E .. NS_LAST), warp-local on the warp's own column buffer; the
+// caller makes the first stage's stores visible before and synchronises the block after
+template <int N, int NS, bool INV>
+__device__ __forceinline__ void colsplit_middle_from(float2* buf, const float2* __restrict__ tw, int t) {
+  if constexpr (NS < ColSplit<N>::NS_LAST) {
+    constexpr int E = N / 32;
+    constexpr int REM = N / NS;
+    constexpr int RS = REM < E ? REM : E;
+    float2 unused[E];
+    warp_stage<N, RS, NS, INV, false, false>(unused, buf, tw, t);
+    colsplit_middle_from<N, NS * RS, INV>(buf, tw, t);
+  }
+}
+template <int N, bool INV>
+__device__ __forceinline__ void colsplit_middle(float2* buf, const float2* __restrict__ tw, int t) {
+  colsplit_middle_from<N, N / 32, INV>(buf, tw, t);
+}
+
+// last stage of column cc: butterflies j = r0 + 32 q read positions j + NS r (padded index:
+// (r0 + r0/16) + 34 q + (NS + NS/16) r), twiddle entries (r-1)*NS + j of the stage, and
+// leave row j + NS r in v[q + (NS/32) r]
+template <int N, bool INV>
+__device__ __forceinline__ void colsplit_last(float2 (&v)[N / 32], const float2* colbuf,
+                                              const float2* __restrict__ tw, int r0) {
+  constexpr int NS = ColSplit<N>::NS_LAST;
+  constexpr int RS = N / NS;
+  constexpr int Q = NS / 32;
+  constexpr int TWOFF = wtw_offset(N, NS);
+  float2 a[N / 32];
+  const float2* b = colbuf + r0 + (r0 >> 4);
+#pragma unroll
+  for (int q = 0; q < Q; q++)
+#pragma unroll
+    for (int r = 0; r < RS; r++) a[q * RS + r] = b[34 * q + (NS + NS / 16) * r];
+  const float2* twl = tw + TWOFF + r0;
+#pragma unroll
+  for (int q = 0; q < Q; q++)
+#pragma unroll
+    for (int r = 1; r < RS; r++) {
+      float2 w = twl[(r - 1) * NS + 32 * q];
+      if (INV) w.y = -w.y;
+      a[q * RS + r] = cmul(a[q * RS + r], w);
+    }
+#pragma unroll
+  for (int q = 0; q < Q; q++) Dft<RS, INV>::run(&a[q * RS]);
+#pragma unroll
+  for (int q = 0; q < Q; q++)
+#pragma unroll
+    for (int r = 0; r < RS; r++) v[q + r * Q] = a[q * RS + r];
+}
+
 }  // namespace bpmgb

@@ -1,5 +1,6 @@
-"""March cases shared by the kernel-path comparison test: run in-process (pipelined
-kernels) and in a child process with BPM_GB300_KERNELS=warp (single-wave warp kernels).
+"""March cases shared by the kernel-path comparison tests, each run in a child process
+whose environment picks the kernels (BPM_GB300_KERNELS, BPM_GB300_COLSPLIT,
+BPM_GB300_CLUSTER).
 
     python tests/_march_cases.py OUT.npz
 """
@@ -17,7 +18,8 @@ def cases():
     for (nx, ny, nz), mode, dtype, half, B in [((512, 256, 10), "weighted", np.float32, False, 3),
                                                ((256, 512, 8), "simple", np.float32, True, 2),
                                                ((128, 128, 12), "ignore", np.complex64, False, 3),
-                                               ((512, 512, 6), "weighted", np.float32, False, 5)]:
+                                               ((512, 512, 6), "weighted", np.float32, False, 5),
+                                               ((256, 128, 7), "weighted", np.float32, True, 2)]:
         dn = (.03 * rng.standard_normal((nz, ny, nx))).astype(np.float32)
         if dtype == np.complex64:
             dn = (dn - 1j * np.abs(.002 * rng.standard_normal((nz, ny, nx)))).astype(np.complex64)

@@ -2,6 +2,8 @@
 reference's own kernels) and with the CPU oracle, plus the reference's own physics
 checks. Tolerance: relative L2 <= 1e-4 against the FP64 oracle and against the
 reference-faithful FP32 oracle; evanescent mask and taper bit-exact."""
+import os
+
 import numpy as np
 import pytest
 
@@ -214,12 +216,17 @@ def test_batched_host_out_pipeline(bpm):
     assert bool(np.array_equal(got2, want2))
 
 
-def test_graph_replay_equals_direct(bpm):
+# (64, 32, 16) runs the pass kernels: one row pass, then two column passes and one row pass
+# per step. The square 64 grid runs the whole march as one cluster launch.
+@pytest.mark.parametrize("size,launches", [((64, 32, 16), 1 + 2 * 15 + 15), ((64, 64, 16), 1)])
+def test_graph_replay_equals_direct(bpm, size, launches):
     import torch
-    size = (64, 64, 16)
-    dn = random_spheres(64, 64, 16, 4, 9)
+    if launches == 1 and os.environ.get("BPM_GB300_CLUSTER", "") == "0":
+        pytest.skip("cluster kernel switched off")
+    Nx, Ny, Nz = size
+    dn = random_spheres(Nx, Ny, Nz, 4, 9)
     m = bpm.BatchedMarch(size, (.1, .1, .1), .5, 1.33, 3, dn=dn, out_kind="field")
-    m.u0.copy_(torch.from_numpy(np.exp(1j * np.linspace(0, 3, 64 * 64 * 3)).reshape(3, 64, 64)
+    m.u0.copy_(torch.from_numpy(np.exp(1j * np.linspace(0, 3, Nx * Ny * 3)).reshape(3, Ny, Nx)
                                 .astype(np.complex64)))
     m.run()
     torch.cuda.synchronize()
@@ -228,7 +235,7 @@ def test_graph_replay_equals_direct(bpm):
     n0 = bpm.launch_count()
     m.run()
     torch.cuda.synchronize()
-    assert bpm.launch_count() - n0 == 1 + 2 * 15 + 15  # row + (2 col + 1 row) per step
+    assert bpm.launch_count() - n0 == launches
 
 
 def test_plane_wave_analytic(bpm):
@@ -295,6 +302,28 @@ def test_pipelined_kernels_match_warp_kernels(bpm, tmp_path):
     assert sorted(A.files) == sorted(B.files)
     for k in A.files:
         assert np.array_equal(A[k], A2[k]), k
+        assert np.array_equal(A[k], B[k]), k
+
+
+def test_split_columns_match_warp_columns(bpm, tmp_path):
+    """The column passes without the tile transposition (col_split_kernel: first and last
+    FFT stages in the coalesced load/store mapping) against the warp-per-column kernels
+    (BPM_GB300_COLSPLIT=0), each in a child process with the single-wave kernel family and
+    the cluster kernel off: column lengths 128, 256 and 512, the three mean modes, f32 /
+    f16 / complex dn, weighted reductions with staged f32 and f16 dn. Same butterflies and
+    order, so the same bits."""
+    import subprocess
+    import sys
+    script = os.path.join(os.path.dirname(os.path.abspath(__file__)), "_march_cases.py")
+    paths = {}
+    for tag, split in (("split", "1"), ("warp", "0")):
+        paths[tag] = str(tmp_path / (tag + ".npz"))
+        subprocess.run([sys.executable, script, paths[tag]], check=True, timeout=600,
+                       env=dict(os.environ, BPM_GB300_KERNELS="warp", BPM_GB300_COLSPLIT=split,
+                                BPM_GB300_CLUSTER="0"))
+    A, B = (np.load(paths[t]) for t in ("split", "warp"))
+    assert sorted(A.files) == sorted(B.files)
+    for k in A.files:
         assert np.array_equal(A[k], B[k]), k
 
 
