@@ -671,7 +671,8 @@ constexpr int kColWarps = 16;  // columns per block (16 columns = one 128-byte s
 
 template <int N>
 struct WarpCfg {
-  static constexpr size_t ROW_SMEM = ((size_t)N + (size_t)kRowWarps * WarpFft<N>::BUF) * sizeof(float2);
+  static constexpr size_t row_smem(int rw) { return ((size_t)N + (size_t)rw * WarpFft<N>::BUF) * sizeof(float2); }
+  static constexpr size_t ROW_SMEM = row_smem(kRowWarps);
   static constexpr size_t ROW_SMEM_SHARED = ROW_SMEM + (size_t)N * sizeof(float2);  // + the staged row
   static constexpr size_t COL_F2 = (size_t)N + (size_t)kColWarps * WarpFft<N>::BUF;  // twiddles, tile/exchange
   static constexpr size_t COL_SMEM = COL_F2 * sizeof(float2);
@@ -684,17 +685,17 @@ struct WarpCfg {
 // Row pass, one warp per row: coalesced row load straight into registers, [inverse row
 // FFT], pointwise work, [forward row FFT], coalesced store. No block-level barrier after
 // the twiddle table is loaded.
-template <int N, bool ADJ, int PRE>
-__global__ void __launch_bounds__(kRowWarps * 32, PRE ? 4 : 3)
+template <int N, bool ADJ, int PRE, int RW = kRowWarps>
+__global__ void __launch_bounds__(RW * 32, (PRE ? 4 : 3) * (kRowWarps / RW))
 row_warp_kernel(RowParams p) {
   constexpr int E = N / 32;
-  constexpr int T = kRowWarps * 32;
+  constexpr int T = RW * 32;
   extern __shared__ float2 smem[];
   float2* tw = smem;
   const int warp = threadIdx.x >> 5, t = threadIdx.x & 31;
   float2* buf = smem + N + warp * WarpFft<N>::BUF;
   const int gl = blockIdx.y;
-  const int y = blockIdx.x * kRowWarps + warp;
+  const int y = blockIdx.x * RW + warp;
   const size_t plane = (size_t)N * p.ny;
   // the twiddle table (a plan constant) is fetched before the wait for the previous pass;
   // the row loads go out before the barrier, so their latency overlaps the table's
@@ -993,16 +994,22 @@ col_warp_kernel(ColParams p) {
 }
 
 // Column pass without the tile transposition (128 <= N <= 512, no scattering sums). The
-// block's 512 threads load 16 columns in the coalesced tile mapping — thread (r0, cc) holds
-// rows r0 + 32 i of column x0 + cc — and keep that mapping for every pointwise step (the
-// propagator from the row-major table or the FP32 recipe, the weighted partial sums, the
-// loads and stores); the first and last FFT stages run in it as well (colsplit_first /
-// colsplit_last) and only the middle stages per warp, on the column's exchange buffer. WHICH
-// as col_warp_kernel, whose results it reproduces bit for bit.
-template <int N>
+// block's 32*C threads load C columns (16, or 8 for small non-weighted passes) in the
+// coalesced tile mapping — thread (r0, cc) = (tid / C, tid % C) holds rows r0 + 32 i of column
+// x0 + cc — and keep that mapping for every pointwise step (the propagator from the
+// row-major table or the FP32 recipe, the weighted partial sums, the loads and stores); the
+// first and last FFT stages run in it as well (colsplit_first / colsplit_last) and only the
+// middle stages per warp, on the column's exchange buffer. WHICH as col_warp_kernel, whose
+// results it reproduces bit for bit. The weighted passes keep C = 16: their per-block
+// partial sums then group the same elements in the same order as every other kernel's.
+// Column buffers are STRIDE float2 apart: with 16 columns an odd stride puts a half-warp's
+// 16 columns on 16 different bank pairs; with 8 columns a half-warp spans two rows of 8
+// columns, conflict-free at N = 512 for stride 546, 2-way on some accesses at 128 and 256.
+template <int N, int C = kColWarps>
 struct ColSplitCfg {
+  static constexpr int STRIDE = (C == 8 && N == 512) ? 546 : (WarpFft<N>::BUF | 1);
   static constexpr int TW_F2 = (WarpFft<N>::TW + 1) & ~1;
-  static constexpr int DN_F2 = (TW_F2 + kColWarps * ColSplit<N>::STRIDE + 1) & ~1;  // 16-byte aligned
+  static constexpr int DN_F2 = (TW_F2 + C * STRIDE + 1) & ~1;  // 16-byte aligned
   static constexpr size_t SMEM = (size_t)DN_F2 * sizeof(float2);
   static constexpr size_t SMEM_DN = SMEM + (size_t)16 * N * sizeof(float);  // + dn slice 0 of the tile
   static constexpr size_t SMEM_KY = SMEM + (size_t)N * sizeof(float);       // + the ky^2 column
@@ -1039,34 +1046,46 @@ __device__ __forceinline__ void propagate_rows(const ColParams& p, float2 (&v)[N
   }
 }
 
-template <int N, int WHICH>
-__global__ void __launch_bounds__(kColWarps * 32, 2)
+template <int N, int WHICH, int C = kColWarps>
+__global__ void __launch_bounds__(C * 32, C == 16 ? 2 : 4)
 col_split_kernel(ColParams p) {
+  using Cfg = ColSplitCfg<N, C>;
   constexpr int E = N / 32;
-  constexpr int T = kColWarps * 32;
-  static_assert(T == 512, "32 threads per column");
+  constexpr int T = C * 32;
+  static_assert(C == 16 || (C == 8 && WHICH == 0), "weighted passes keep 16-column blocks");
   extern __shared__ __align__(16) float2 smem[];
   float2* tw = smem;
-  float2* bufs = smem + ColSplitCfg<N>::TW_F2;
+  float2* bufs = smem + Cfg::TW_F2;
   __shared__ float red[64];
   __shared__ float s_n;
   const int warp = threadIdx.x >> 5, t = threadIdx.x & 31;
-  const int r0 = threadIdx.x >> 4, cc = threadIdx.x & 15;
+  const int r0 = threadIdx.x / C, cc = threadIdx.x % C;
   const int gl = blockIdx.y;
-  const int x0 = blockIdx.x * kColWarps;
+  const int x0 = blockIdx.x * C;
   float2* Wp = p.W + (size_t)gl * p.nx * N;
   const unsigned gstep = 32u * (unsigned)p.nx;
-  float2* colbuf = bufs + cc * ColSplit<N>::STRIDE;  // column x0 + cc: the tile-mapping stages
-  float2* wbuf = bufs + warp * ColSplit<N>::STRIDE;  // column x0 + warp: the middle stages
-  static_assert(WarpFft<N>::TW <= T && N <= T, "one twiddle and one ky^2 entry per thread");
+  float2* colbuf = bufs + cc * Cfg::STRIDE;    // column x0 + cc: the tile-mapping stages
+  float2* wbuf = bufs + warp * Cfg::STRIDE;    // column x0 + warp: the middle stages
   // plan constants before the wait for the previous pass: the twiddles, and for the FP32
   // recipe kx^2 of the thread's column and one ky^2 entry per thread (staged after it, in the
   // region the weighted reduction uses for dn)
-  const float2 twv = threadIdx.x < WarpFft<N>::TW ? p.wtw[threadIdx.x] : make_float2(0.f, 0.f);
+  constexpr int TWR = (WarpFft<N>::TW + T - 1) / T;  // twiddles per thread (1, or 2 with 8 columns)
+  constexpr int KYR = (N + T - 1) / T;                // ky^2 entries per thread
+  float2 twv[TWR];
+#pragma unroll
+  for (int k = 0; k < TWR; k++) {
+    const int i = threadIdx.x + k * T;
+    twv[k] = i < WarpFft<N>::TW ? p.wtw[i] : make_float2(0.f, 0.f);
+  }
   const bool recipe = WHICH != 1 && p.prop_mode != 0;
   const float kx2v = recipe ? __ldg(p.kx2 + x0 + cc) : 0.f;
-  const float kyv = (recipe && threadIdx.x < N) ? __ldg(p.ky2 + threadIdx.x) : 0.f;
-  float* sky2 = reinterpret_cast<float*>(smem + ColSplitCfg<N>::DN_F2);
+  float kyv[KYR];
+#pragma unroll
+  for (int k = 0; k < KYR; k++) {
+    const int i = threadIdx.x + k * T;
+    kyv[k] = (recipe && i < N) ? __ldg(p.ky2 + i) : 0.f;
+  }
+  float* sky2 = reinterpret_cast<float*>(smem + Cfg::DN_F2);
   dep_wait();
   dep_release();
   // weighted reduction: dn slice 0 of this tile goes to shared memory with cp.async now and
@@ -1075,7 +1094,7 @@ col_split_kernel(ColParams p) {
   if (WHICH == 1 && p.dn && p.dn_stage) {
     const int lg = p.dn_dtype == BPM_DN_F16 ? 1 : 2;
     const int es = 1 << lg;
-    char* dst = reinterpret_cast<char*>(smem + ColSplitCfg<N>::DN_F2);
+    char* dst = reinterpret_cast<char*>(smem + Cfg::DN_F2);
     const char* srcb = static_cast<const char*>(p.dn) + ((size_t)gl * p.dn_bstride + x0) * es;
     const size_t rowb = (size_t)p.nx * es;
     for (int ch = threadIdx.x; ch < (N << lg); ch += T)
@@ -1106,8 +1125,12 @@ col_split_kernel(ColParams p) {
       if (blockIdx.x == 0) p.dn0_field[gl] = dn0;
     }
   }
-  if (threadIdx.x < WarpFft<N>::TW) tw[threadIdx.x] = twv;
-  if (recipe && threadIdx.x < N) sky2[threadIdx.x] = kyv;
+#pragma unroll
+  for (int k = 0; k < TWR; k++)
+    if (threadIdx.x + k * T < WarpFft<N>::TW) tw[threadIdx.x + k * T] = twv[k];
+#pragma unroll
+  for (int k = 0; k < KYR; k++)
+    if (recipe && threadIdx.x + k * T < N) sky2[threadIdx.x + k * T] = kyv[k];
   if (WHICH == 2) {
     __syncthreads();  // s_n, ky^2
     propagate_rows<N>(p, v, x0 + cc, r0, s_n, kx2v, sky2);
@@ -1691,14 +1714,14 @@ struct SizeDispatch;
 
 // Which row/column kernels a march uses for 128 <= N <= 512. The pipelined persistent
 // kernels hide each item's load latency behind the previous item but hold the whole device
-// at half the warps of the single-wave warp kernels; several field groups marching at once
-// on their own streams hide that latency better by overlapping each other's waves. So the
-// pipelined kernels serve marches of a single group, the warp kernels concurrent groups
-// (measured on GB300, 512x512: one field 8.0 vs 6.6 G voxel-updates/s; 64 fields in 4
-// concurrent groups of 8: 74 vs 57 ms). Both compute the same bits (explicit fmaf in all
-// shared arithmetic), so a field's result does not depend on the batch it marched in.
-// BPM_GB300_KERNELS=warp / =pipe forces one family.
-thread_local bool t_single_group = false;
+// at half the warps of the single-wave warp kernels, and their column pass keeps the tile
+// transposition that col_split_kernel drops. Measured on GB300 (512x512x256 weighted, one
+// group of B fields): B = 1 6.3 vs 6.1 ms, B = 2 6.6 vs 5.0, B = 8 11.9 vs 7.6 (pipelined vs
+// warp row + split column kernels; 256x256: equal at B = 1, 3.5 vs 2.6 ms at B = 2), and
+// concurrent groups favour the warp kernels further. So the warp kernels serve every march
+// and BPM_GB300_KERNELS=pipe selects the pipelined ones (=warp is the default). All compute
+// the same bits (explicit fmaf in all shared arithmetic), so a field's result does not
+// depend on the batch it marched in or the kernels that ran it.
 
 // column passes of 128..512 without scattering sums run col_split_kernel;
 // BPM_GB300_COLSPLIT=0 selects col_warp_kernel instead (the same bits)
@@ -1711,13 +1734,23 @@ bool colsplit_enabled() {
 }
 
 bool pipe_enabled() {
-  static const int forced = [] {
+  static const bool on = [] {
     const char* e = getenv("BPM_GB300_KERNELS");
-    if (e && strcmp(e, "warp") == 0) return 0;
-    if (e && strcmp(e, "pipe") == 0) return 1;
-    return -1;
+    return e && strcmp(e, "pipe") == 0;
   }();
-  return forced >= 0 ? forced == 1 : t_single_group;
+  return on;
+}
+
+// SMs of the current device (read once per process)
+int sm_count() {
+  static const int n = [] {
+    int dev = 0, v = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&v, cudaDevAttrMultiProcessorCount, dev);
+    cudaGetLastError();
+    return v > 0 ? v : 1;
+  }();
+  return n;
 }
 
 // blocks of `kernel` resident on the whole device at once
@@ -1812,6 +1845,17 @@ struct RowK {
         BPM_LAUNCH_CHECK("row_shared_kernel");
         return BPM_OK;
       }
+      // with fewer 8-row blocks than twice the SMs (a single field, small per-field-dn
+      // groups), blocks of 2 rows spread the pass over 4 times as many SMs
+      const int rows = (int)(g.x * 16) * (int)g.y;
+      if (rows / kRowWarps < 2 * sm_count()) {
+        const dim3 gw(g.x * 16 / 2, g.y);
+        auto fn = adj ? (p.mask ? row_warp_kernel<N, true, 1, 2> : row_warp_kernel<N, true, 0, 2>)
+                      : (p.mask ? row_warp_kernel<N, false, 1, 2> : row_warp_kernel<N, false, 0, 2>);
+        BPM_CUDA_TRY(launch_dep(fn, gw, dim3(2 * 32), WarpCfg<N>::row_smem(2), s, p));
+        BPM_LAUNCH_CHECK("row_warp_kernel");
+        return BPM_OK;
+      }
       const dim3 gw(g.x * 16 / kRowWarps, g.y);
       auto fn = adj ? (p.mask ? row_warp_kernel<N, true, 1> : row_warp_kernel<N, true, 0>)
                     : (p.mask ? row_warp_kernel<N, false, 1> : row_warp_kernel<N, false, 0>);
@@ -1845,6 +1889,7 @@ struct ColK {
   static constexpr size_t split_smem() {
     return WHICH == 1 ? ColSplitCfg<N>::SMEM_DN : ColSplitCfg<N>::SMEM_KY;
   }
+  static constexpr size_t split8_smem() { return ColSplitCfg<N, 8>::SMEM_KY; }
   static void prepare() {
     static bool attr = false;
     if (!attr) {
@@ -1855,6 +1900,9 @@ struct ColK {
         pipe_cap() = resident_blocks(col_pipe_kernel<N, WHICH>, kColWarps * 32, PipeCfg<N>::COL_SMEM);
         cudaFuncSetAttribute(col_split_kernel<N, WHICH>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                              (int)split_smem());
+        if constexpr (WHICH == 0)
+          cudaFuncSetAttribute(col_split_kernel<N, 0, 8>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                               (int)split8_smem());
       }
       attr = true;
     }
@@ -1870,6 +1918,16 @@ struct ColK {
         return BPM_OK;
       }
       if (!p.scat && colsplit_enabled()) {
+        // a non-weighted pass with fewer 16-column blocks than SMs runs 8-column blocks, so
+        // twice as many SMs share it (the columns' arithmetic is the same)
+        if constexpr (WHICH == 0) {
+          if ((int)(g.x * g.y) < sm_count()) {
+            BPM_CUDA_TRY(launch_dep(col_split_kernel<N, 0, 8>, dim3(g.x * 2, g.y), dim3(8 * 32), split8_smem(),
+                                    s, p));
+            BPM_LAUNCH_CHECK("col_split_kernel");
+            return BPM_OK;
+          }
+        }
         BPM_CUDA_TRY(launch_dep(col_split_kernel<N, WHICH>, g, dim3(kColWarps * 32), split_smem(), s, p));
         BPM_LAUNCH_CHECK("col_split_kernel");
         return BPM_OK;
@@ -2292,10 +2350,6 @@ int enqueue_march(bpm_plan* pl, const bpm_request* r, void* ws, size_t ws_bytes,
   const size_t slot = ws_layout(pl, G).total;
   const int conc = std::max(
       1, (int)std::min<size_t>({(size_t)ngroups, ws_bytes / slot, (size_t)conc_limit()}));
-  struct SingleGroupScope {  // kernel family of this march (pipe_enabled)
-    explicit SingleGroupScope(bool v) { t_single_group = v; }
-    ~SingleGroupScope() { t_single_group = false; }
-  } scope(conc == 1);
   cudaStream_t st[kMaxConcurrentGroups];
   for (int j = 0; j < conc; j++) st[j] = conc > 1 ? pl->aux[j] : s;
   if (conc > 1 || sink) BPM_CUDA_TRY(cudaEventRecord(pl->ev_fork, s));

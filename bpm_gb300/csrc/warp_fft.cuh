@@ -172,9 +172,6 @@ template <int N>
 struct ColSplit {
   static constexpr int E = N / 32;
   static constexpr int NS_LAST = colsplit_last_ns(N);
-  // column buffers are STRIDE float2 apart; an odd stride puts the 16 columns a half-warp
-  // touches in the tile mapping on 16 different bank pairs
-  static constexpr int STRIDE = WarpFft<N>::BUF | 1;
   static_assert(NS_LAST >= 32 && NS_LAST < N, "last stage spans whole 32-row groups");
 };
 
