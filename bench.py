@@ -500,12 +500,45 @@ def config1_dn(n=128):
     return (.05 * (((x - n / 2) ** 2 + (y - n / 2) ** 2 + (z - n / 2) ** 2) <= 20 ** 2)).astype(np.float32)
 
 
+def profile_kernels():
+    """One small invocation of every kernel family not in the batched march, for per-kernel
+    ncu captures: tile kernels (1024^2, 64x32), narrow single-field kernels (256^2), the
+    adjoint, the scattering column pass, the mask precompute, the coated-sphere fill and the
+    Debye-Wolf plane / free-point / Gaussian-pupil variants."""
+    import torch
+    import bpm_gb300
+    from bpm_gb300.adjoint import propagate_exit
+    rng = np.random.default_rng(SEED)
+    for (nx, ny, nz) in ((1024, 1024, 6), (64, 32, 6), (256, 256, 6)):
+        dn = torch.from_numpy((.02 * rng.standard_normal((nz, ny, nx)) - 1e-4j).astype(np.complex64)).cuda()
+        bpm_gb300.bpm_3d((nx, ny, nz), UNITS, lam=LAM, n0=N0, dn=dn, mean_mode="ignore", return_field=False)
+    dn = torch.from_numpy((.02 * rng.standard_normal((6, 256, 256))).astype(np.float32)).cuda()
+    bpm_gb300.bpm_3d((256, 256, 6), UNITS, lam=LAM, n0=N0, dn=dn, return_scattering=True)
+    bpm_gb300.bpm_3d_batched((256, 128, 6), UNITS, lam=LAM, n0=N0, u0=make_u0(2, 256, 128, 1), dn=dn[:, :128].contiguous(),
+                             return_field=False)
+    dng = dn.clone().requires_grad_(True)
+    out = propagate_exit(dng, torch.from_numpy(make_u0(2, 256, 256, 2)).cuda(), (256, 256, 6), UNITS, LAM, N0,
+                         ckpt_every=2)
+    (out.abs() ** 2).sum().backward()
+    bpm_gb300.bpm_3d_spheres((256, 256, 64), UNITS, points=[[12.8, 12.8, 3.2], [6.4, 19.2, 2.]], dn_outer=.05,
+                             rad_outer=2.)
+    bpm_gb300.focus_field_debye_plane((256, 256), (.1, .1), z=1., lam=LAM, NA=.8)
+    pts = np.linspace(-2, 2, 4096).astype(np.float32)
+    bpm_gb300.focus_field_debye_at(pts, pts[::-1].copy(), .5 * pts, LAM, 1.1, n0=N0)
+    bpm_gb300.focus_field_debye_gauss((128, 128, 128), (.1, .1, .1), LAM, [0, .9])
+    torch.cuda.synchronize()
+    print(json.dumps({"profile_run": True, "case": "kernels", "launches": bpm_gb300.launch_count()}))
+
+
 def profile_run(args):
     """The device march alone (same buffers as the timed region), for ncu captures;
     --profile-case config1: one 128^3 weighted request through bpm_3d per step instead."""
     import torch
     import bpm_gb300
     torch.cuda.set_device(0)
+    if args.profile_case == "kernels":
+        profile_kernels()
+        return
     if args.profile_case == "config1":
         dn1 = torch.from_numpy(config1_dn()).cuda()
         for _ in range(args.warmup + args.steps):
@@ -594,8 +627,9 @@ def main():
     ap.add_argument("--nz", type=int, default=NZ, help="z planes (smaller for profiling)")
     ap.add_argument("--profile", action="store_true",
                     help="only the device march (warm-up + steps), for ncu launch lists")
-    ap.add_argument("--profile-case", default="batched", choices=["batched", "config1"],
-                    help="with --profile: the batched march, or one 128^3 weighted request per step")
+    ap.add_argument("--profile-case", default="batched", choices=["batched", "config1", "kernels"],
+                    help="with --profile: the batched march, one 128^3 weighted request per step, or one "
+                         "small call of every other kernel family")
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3
