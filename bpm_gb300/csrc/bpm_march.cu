@@ -686,7 +686,7 @@ struct WarpCfg {
 // FFT], pointwise work, [forward row FFT], coalesced store. No block-level barrier after
 // the twiddle table is loaded.
 template <int N, bool ADJ, int PRE, int RW = kRowWarps>
-__global__ void __launch_bounds__(RW * 32, (PRE ? 4 : 3) * (kRowWarps / RW))
+__global__ void __launch_bounds__(RW * 32, (N > 512 ? 2 : (PRE ? 4 : 3)) * (kRowWarps / RW))
 row_warp_kernel(RowParams p) {
   constexpr int E = N / 32;
   constexpr int T = RW * 32;
@@ -745,22 +745,24 @@ __device__ __forceinline__ float2 staged_mask(const RowParams& p, const void* ml
 }
 
 // Forward row pass when the fields of the group share one mask (precomputed, or one dn
-// volume): block (y, b) takes row y of fields 8b .. 8b+7, one field per warp, so the mask
-// row (or dn row) of slice z is staged once per block into shared memory with cp.async at
-// block start and is ready when the warps finish their inverse row FFTs. The arithmetic is
+// volume): block (y, b) takes row y of fields nw*b .. nw*b + nw-1, one field per warp (nw =
+// blockDim.x / 32 <= 8, chosen so no block holds idle warps' registers), so the mask row (or
+// dn row) of slice z is staged once per block into shared memory with cp.async at block
+// start and is ready when the warps finish their inverse row FFTs. The arithmetic is
 // row_warp_kernel's.
 template <int N, int PRE>
-__global__ void __launch_bounds__(kRowWarps * 32, 4)
+__global__ void __launch_bounds__(kRowWarps * 32, N > 512 ? 2 : 4)
 row_shared_kernel(RowParams p, int nfields) {
   constexpr int E = N / 32;
-  constexpr int T = kRowWarps * 32;
+  const int T = blockDim.x;
+  const int nw = T >> 5;
   extern __shared__ __align__(16) float2 smem[];
   float2* tw = smem;
   const int warp = threadIdx.x >> 5, t = threadIdx.x & 31;
   float2* buf = smem + N + warp * WarpFft<N>::BUF;
-  float2* mrow = smem + N + kRowWarps * WarpFft<N>::BUF;  // N float2: the staged mask or dn row
+  float2* mrow = smem + N + nw * WarpFft<N>::BUF;  // N float2: the staged mask or dn row
   const int y = blockIdx.x;
-  const int gl = blockIdx.y * kRowWarps + warp;
+  const int gl = blockIdx.y * nw + warp;
   const bool active = gl < nfields;
   const size_t plane = (size_t)N * p.ny;
   const size_t zoff = (size_t)p.z * plane;
@@ -1004,10 +1006,11 @@ col_warp_kernel(ColParams p) {
 // partial sums then group the same elements in the same order as every other kernel's.
 // Column buffers are STRIDE float2 apart: with 16 columns an odd stride puts a half-warp's
 // 16 columns on 16 different bank pairs; with 8 columns a half-warp spans two rows of 8
-// columns, conflict-free at N = 512 for stride 546, 2-way on some accesses at 128 and 256.
+// columns, conflict-free at N = 512 and 1024 for stride BUF + 2, 2-way on some accesses at
+// 128 and 256.
 template <int N, int C = kColWarps>
 struct ColSplitCfg {
-  static constexpr int STRIDE = (C == 8 && N == 512) ? 546 : (WarpFft<N>::BUF | 1);
+  static constexpr int STRIDE = (C == 8 && N >= 512) ? WarpFft<N>::BUF + 2 : (WarpFft<N>::BUF | 1);
   static constexpr int TW_F2 = (WarpFft<N>::TW + 1) & ~1;
   static constexpr int DN_F2 = (TW_F2 + C * STRIDE + 1) & ~1;  // 16-byte aligned
   static constexpr size_t SMEM = (size_t)DN_F2 * sizeof(float2);
@@ -1047,7 +1050,7 @@ __device__ __forceinline__ void propagate_rows(const ColParams& p, float2 (&v)[N
 }
 
 template <int N, int WHICH, int C = kColWarps>
-__global__ void __launch_bounds__(C * 32, C == 16 ? 2 : 4)
+__global__ void __launch_bounds__(C * 32, (C == 16 ? 2 : 4) / (N > 512 ? 2 : 1))
 col_split_kernel(ColParams p) {
   using Cfg = ColSplitCfg<N, C>;
   constexpr int E = N / 32;
@@ -1733,6 +1736,16 @@ bool colsplit_enabled() {
   return on;
 }
 
+// 1024-point rows and columns run the warp-FFT kernels (32 values per lane, one exchange
+// per transform); BPM_GB300_WARP1024=0 selects the shared-memory tile kernels instead
+bool warp1024_enabled() {
+  static const bool on = [] {
+    const char* e = getenv("BPM_GB300_WARP1024");
+    return !(e && strcmp(e, "0") == 0);
+  }();
+  return on;
+}
+
 bool pipe_enabled() {
   static const bool on = [] {
     const char* e = getenv("BPM_GB300_KERNELS");
@@ -1773,7 +1786,9 @@ inline int balanced_workers(int items, int cap) {
 
 template <int N>
 struct RowK {
-  static constexpr bool WARP = N >= 128 && N <= 512;
+  static constexpr bool WARP = N >= 128 && N <= 1024;  // warp-per-row kernels
+  static constexpr bool PIPE = N >= 128 && N <= 512;   // pipelined persistent kernels
+  static constexpr bool TILE = !WARP || N == 1024;     // shared-memory tile kernels
   static int& pipe_cap(int pre) {
     static int cap[2] = {0, 0};
     return cap[pre];
@@ -1786,12 +1801,14 @@ struct RowK {
                              (int)WarpCfg<N>::ROW_SMEM_SHARED);
         cudaFuncSetAttribute(row_shared_kernel<N, 1>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                              (int)WarpCfg<N>::ROW_SMEM_SHARED);
-        cudaFuncSetAttribute(row_pipe_kernel<N, 0>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                             (int)PipeCfg<N>::ROW_SMEM);
-        cudaFuncSetAttribute(row_pipe_kernel<N, 1>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                             (int)PipeCfg<N>::ROW_SMEM);
-        pipe_cap(0) = resident_blocks(row_pipe_kernel<N, 0>, kRowWarps * 32, PipeCfg<N>::ROW_SMEM);
-        pipe_cap(1) = resident_blocks(row_pipe_kernel<N, 1>, kRowWarps * 32, PipeCfg<N>::ROW_SMEM);
+        if constexpr (PIPE) {
+          cudaFuncSetAttribute(row_pipe_kernel<N, 0>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                               (int)PipeCfg<N>::ROW_SMEM);
+          cudaFuncSetAttribute(row_pipe_kernel<N, 1>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                               (int)PipeCfg<N>::ROW_SMEM);
+          pipe_cap(0) = resident_blocks(row_pipe_kernel<N, 0>, kRowWarps * 32, PipeCfg<N>::ROW_SMEM);
+          pipe_cap(1) = resident_blocks(row_pipe_kernel<N, 1>, kRowWarps * 32, PipeCfg<N>::ROW_SMEM);
+        }
         cudaFuncSetAttribute(row_warp_kernel<N, false, 0>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                              (int)WarpCfg<N>::ROW_SMEM);
         cudaFuncSetAttribute(row_warp_kernel<N, true, 0>, cudaFuncAttributeMaxDynamicSharedMemorySize,
@@ -1800,7 +1817,8 @@ struct RowK {
                              (int)WarpCfg<N>::ROW_SMEM);
         cudaFuncSetAttribute(row_warp_kernel<N, true, 1>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                              (int)WarpCfg<N>::ROW_SMEM);
-      } else {
+      }
+      if constexpr (TILE) {
         cudaFuncSetAttribute(row_pass_kernel<N, false>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                              (int)TileCfg<N>::SMEM);
         cudaFuncSetAttribute(row_pass_kernel<N, true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
@@ -1828,20 +1846,40 @@ struct RowK {
   static int launch(dim3 g, cudaStream_t s, const RowParams& p, bool adj) {
     prepare();
     if constexpr (WARP) {
-      if (!adj && pipe_ok(p)) {
-        const int pre = p.mask ? 1 : 0;
-        const int nrows = (int)g.y * p.ny;
-        const int warps = balanced_workers(nrows, pipe_cap(pre) * kRowWarps);
-        const int blocks = (warps + kRowWarps - 1) / kRowWarps;
-        auto fn = pre ? row_pipe_kernel<N, 1> : row_pipe_kernel<N, 0>;
-        BPM_CUDA_TRY(launch_dep(fn, dim3(blocks), dim3(kRowWarps * 32), PipeCfg<N>::ROW_SMEM, s, p, nrows));
-        BPM_LAUNCH_CHECK("row_pipe_kernel");
-        return BPM_OK;
+      if (N <= 512 || warp1024_enabled()) return launch_warp(g, s, p, adj);
+    }
+    if constexpr (TILE) {
+      if (adj)
+        BPM_CUDA_TRY(launch_dep(row_pass_kernel<N, true>, g, dim3(TileCfg<N>::THREADS), TileCfg<N>::SMEM, s, p));
+      else
+        BPM_CUDA_TRY(launch_dep(row_pass_kernel<N, false>, g, dim3(TileCfg<N>::THREADS), TileCfg<N>::SMEM, s, p));
+      BPM_LAUNCH_CHECK("row_pass_kernel");
+      return BPM_OK;
+    }
+    set_error("row pass: no kernel for this size");
+    return BPM_ERR_SHAPE;
+  }
+  static int launch_warp(dim3 g, cudaStream_t s, const RowParams& p, bool adj) {
+    if constexpr (WARP) {
+      if constexpr (PIPE) {
+        if (!adj && pipe_ok(p)) {
+          const int pre = p.mask ? 1 : 0;
+          const int nrows = (int)g.y * p.ny;
+          const int warps = balanced_workers(nrows, pipe_cap(pre) * kRowWarps);
+          const int blocks = (warps + kRowWarps - 1) / kRowWarps;
+          auto fn = pre ? row_pipe_kernel<N, 1> : row_pipe_kernel<N, 0>;
+          BPM_CUDA_TRY(launch_dep(fn, dim3(blocks), dim3(kRowWarps * 32), PipeCfg<N>::ROW_SMEM, s, p, nrows));
+          BPM_LAUNCH_CHECK("row_pipe_kernel");
+          return BPM_OK;
+        }
       }
       if (!adj && shared_ok(p) && g.y >= 2) {
-        const dim3 gs(p.ny, (g.y + kRowWarps - 1) / kRowWarps);
+        // fields per block: the group split evenly over ceil(G / 8) blocks per row
+        const int nb = ((int)g.y + kRowWarps - 1) / kRowWarps;
+        const int fw = ((int)g.y + nb - 1) / nb;
+        const size_t sm = ((size_t)2 * N + (size_t)fw * WarpFft<N>::BUF) * sizeof(float2);
         auto fn = p.mask ? row_shared_kernel<N, 1> : row_shared_kernel<N, 0>;
-        BPM_CUDA_TRY(launch_dep(fn, gs, dim3(kRowWarps * 32), WarpCfg<N>::ROW_SMEM_SHARED, s, p, (int)g.y));
+        BPM_CUDA_TRY(launch_dep(fn, dim3(p.ny, nb), dim3(fw * 32), sm, s, p, (int)g.y));
         BPM_LAUNCH_CHECK("row_shared_kernel");
         return BPM_OK;
       }
@@ -1860,20 +1898,17 @@ struct RowK {
       auto fn = adj ? (p.mask ? row_warp_kernel<N, true, 1> : row_warp_kernel<N, true, 0>)
                     : (p.mask ? row_warp_kernel<N, false, 1> : row_warp_kernel<N, false, 0>);
       BPM_CUDA_TRY(launch_dep(fn, gw, dim3(kRowWarps * 32), WarpCfg<N>::ROW_SMEM, s, p));
-    } else {
-      if (adj)
-        BPM_CUDA_TRY(launch_dep(row_pass_kernel<N, true>, g, dim3(TileCfg<N>::THREADS), TileCfg<N>::SMEM, s, p));
-      else
-        BPM_CUDA_TRY(launch_dep(row_pass_kernel<N, false>, g, dim3(TileCfg<N>::THREADS), TileCfg<N>::SMEM, s, p));
+      BPM_LAUNCH_CHECK("row_warp_kernel");
+      return BPM_OK;
     }
-    BPM_LAUNCH_CHECK("row_pass_kernel");
-    return BPM_OK;
+    return BPM_ERR_SHAPE;
   }
 };
 
 template <int N, int WHICH>
 struct ColK {
-  static constexpr bool WARP = N >= 128 && N <= 512;
+  static constexpr bool WARP = N >= 128 && N <= 512;    // warp-per-column and pipelined kernels
+  static constexpr bool SPLIT = N >= 128 && N <= 1024;  // col_split_kernel
   static void (*fn())(ColParams) {
     if constexpr (WARP) return col_warp_kernel<N, WHICH>;
     return WHICH == 0 ? col_pass_kernel<N> : (WHICH == 1 ? col_fwd_reduce_kernel<N> : col_inv_kernel<N>);
@@ -1898,6 +1933,8 @@ struct ColK {
         cudaFuncSetAttribute(col_pipe_kernel<N, WHICH>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                              (int)PipeCfg<N>::COL_SMEM);
         pipe_cap() = resident_blocks(col_pipe_kernel<N, WHICH>, kColWarps * 32, PipeCfg<N>::COL_SMEM);
+      }
+      if constexpr (SPLIT) {
         cudaFuncSetAttribute(col_split_kernel<N, WHICH>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                              (int)split_smem());
         if constexpr (WHICH == 0)
@@ -1917,11 +1954,14 @@ struct ColK {
         BPM_LAUNCH_CHECK("col_pipe_kernel");
         return BPM_OK;
       }
-      if (!p.scat && colsplit_enabled()) {
+    }
+    if constexpr (SPLIT) {
+      if (!p.scat && colsplit_enabled() && (N <= 512 || warp1024_enabled())) {
         // a non-weighted pass with fewer 16-column blocks than SMs runs 8-column blocks, so
-        // twice as many SMs share it (the columns' arithmetic is the same)
+        // twice as many SMs share it (the columns' arithmetic is the same); so does every
+        // non-weighted 1024-point pass, whose 16-column blocks fill an SM alone
         if constexpr (WHICH == 0) {
-          if ((int)(g.x * g.y) < sm_count()) {
+          if ((int)(g.x * g.y) < sm_count() || N > 512) {
             BPM_CUDA_TRY(launch_dep(col_split_kernel<N, 0, 8>, dim3(g.x * 2, g.y), dim3(8 * 32), split8_smem(),
                                     s, p));
             BPM_LAUNCH_CHECK("col_split_kernel");
@@ -2642,7 +2682,7 @@ extern "C" int bpm_plan_create(const bpm_grid_desc* d, bpm_plan** out) {
     return fail(e, "cudaMemcpy");
   for (int axis = 0; axis < 2; axis++) {
     const int n = axis == 0 ? nx : ny;
-    if (n < 64 || n > 512) continue;  // the warp FFT's sizes (the cluster kernel uses 64 too)
+    if (n < 64 || n > 1024) continue;  // the warp FFT's sizes (the cluster kernel uses 64 too)
     std::vector<float2> w = warp_twiddles(n);
     float2** dst = axis == 0 ? &pl->wtw_x : &pl->wtw_y;
     if ((e = cudaMalloc(dst, w.size() * sizeof(float2)))) return fail(e, "cudaMalloc");

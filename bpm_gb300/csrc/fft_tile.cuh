@@ -109,6 +109,40 @@ struct Dft<16, INV> {
   }
 };
 
+// radix-32 by one even/odd split into two 16-point DFTs: X[k] = E[k] + W32^k O[k],
+// X[k+16] = E[k] - W32^k O[k]
+template <bool INV>
+struct Dft<32, INV> {
+  __device__ __forceinline__ static void run(float2* v) {
+    float2 e[16], o[16];
+#pragma unroll
+    for (int i = 0; i < 16; i++) {
+      e[i] = v[2 * i];
+      o[i] = v[2 * i + 1];
+    }
+    Dft<16, INV>::run(e);
+    Dft<16, INV>::run(o);
+    // W32^k = cos(2 pi k/32) -/+ i sin(2 pi k/32), k = 0..15
+    constexpr float C[16] = {1.f, 0.98078528040323044913f, 0.92387953251128675613f, 0.83146961230254523708f,
+                             0.70710678118654752440f, 0.55557023301960222474f, 0.38268343236508977173f,
+                             0.19509032201612826785f, 0.f, -0.19509032201612826785f, -0.38268343236508977173f,
+                             -0.55557023301960222474f, -0.70710678118654752440f, -0.83146961230254523708f,
+                             -0.92387953251128675613f, -0.98078528040323044913f};
+    constexpr float S[16] = {0.f, 0.19509032201612826785f, 0.38268343236508977173f, 0.55557023301960222474f,
+                             0.70710678118654752440f, 0.83146961230254523708f, 0.92387953251128675613f,
+                             0.98078528040323044913f, 1.f, 0.98078528040323044913f, 0.92387953251128675613f,
+                             0.83146961230254523708f, 0.70710678118654752440f, 0.55557023301960222474f,
+                             0.38268343236508977173f, 0.19509032201612826785f};
+#pragma unroll
+    for (int k = 0; k < 16; k++) {
+      const float2 w = make_float2(C[k], INV ? S[k] : -S[k]);
+      const float2 t = (k == 0) ? o[0] : (k == 8 ? mul_mi<INV>(o[8]) : cmul(o[k], w));
+      v[k] = cadd(e[k], t);
+      v[k + 16] = csub(e[k], t);
+    }
+  }
+};
+
 // One Stockham stage of radix RS with stride NS over the 16-sequence tile.
 // Thread (c, jt): c = sequence, jt = 0 .. N/R-1.
 template <int N, int R, int RS, int NS, bool INV>

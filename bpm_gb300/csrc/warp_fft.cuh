@@ -1,5 +1,5 @@
-// Warp-level FFT: one warp transforms one complex sequence of length N (64 <= N <= 512)
-// held in registers, 16 = N/32 values per lane for N = 512.
+// Warp-level FFT: one warp transforms one complex sequence of length N (64 <= N <= 1024)
+// held in registers, N/32 values per lane (16 for N = 512, 32 for N = 1024).
 //
 // Distribution. On entry and on exit lane t holds elements t + 32*m, m = 0 .. N/32-1, in
 // v[m]: natural order, consecutive elements on consecutive lanes. So a row of an image is
@@ -14,15 +14,16 @@
 // from the lane's own registers and the last stage writes its outputs back to them (both
 // fall on the lane's t + 32*m elements); the stages in between exchange through a
 // private per-warp shared-memory buffer synchronised with __syncwarp, with one pad
-// element every 16 (index p + p/16), which keeps every exchange at the minimum number of
-// shared-memory wavefronts for N = 256 and 512.
+// element every 2^S (index p + p >> S; S = 4 up to N = 512, 5 for N = 1024, whose lanes
+// write runs of 32), which keeps every exchange at the minimum number of shared-memory
+// wavefronts for N = 256, 512 and 1024.
 #pragma once
 
 #include "fft_tile.cuh"
 
 namespace bpmgb {
 
-__device__ __forceinline__ int wpad(int p) { return p + (p >> 4); }
+__host__ __device__ constexpr int pad_shift(int N) { return N >= 1024 ? 5 : 4; }
 
 // Twiddles are stored per stage, entry (r-1)*NS + jm of stage (RS, NS) holding
 // W_N^{jm*r*N/(NS*RS)} for r = 1..RS-1, jm = 0..NS-1, stages in march order, stages with
@@ -42,37 +43,39 @@ __host__ __device__ constexpr int wtw_size(int N) { return wtw_offset(N, N); }
 template <int N>
 struct WarpFft {
   static constexpr int E = N / 32;          // values per lane
-  static constexpr int BUF = N + N / 16;    // padded per-warp exchange buffer (float2)
+  static constexpr int BUF = N + (N >> pad_shift(N));  // padded per-warp exchange buffer (float2)
   static constexpr int TW = wtw_size(N);    // stage-ordered twiddle entries
 };
 
 // Exchange-buffer addressing. Every index a stage touches splits exactly into a per-lane
 // part (computed once) and a compile-time offset, so each shared-memory access is one
-// instruction with an immediate offset instead of recomputing p + p/16 per access.
-//   loads:  wpad(q*32 + t + r*(N/RS))              = (t + t/16) + wpad(q*32 + r*N/RS)
+// instruction with an immediate offset instead of recomputing p + (p >> S) per access.
+//   loads:  wpad(q*32 + t + r*(N/RS))              = (t + t>>S) + wpad(q*32 + r*N/RS)
 //   stores: wpad((j/NS)*NS*RS + j%NS + r*NS), j = q*32 + t
-//           NS >= 32: (t + t/16) + wpad((q*32/NS)*NS*RS + (q*32)%NS + r*NS)
-//           NS <  32: B + (((t/NS)*NS*RS) >> 4) + wpad(q*32*RS) + r*NS + ((r*NS) >> 4),
+//           NS >= 32: (t + t>>S) + wpad((q*32/NS)*NS*RS + (q*32)%NS + r*NS)
+//           NS <  32: B + (((t/NS)*NS*RS) >> S) + wpad(q*32*RS) + r*NS + ((r*NS) >> S),
 //                     B = (t/NS)*NS*RS + t%NS
 // (warp_index_check verifies both against the direct formula for every lane at compile time.)
-__host__ __device__ constexpr int wpad_c(int p) { return p + (p >> 4); }
-__host__ __device__ constexpr int ld_lane(int t) { return t + (t >> 4); }
-__host__ __device__ constexpr int ld_off(int N, int RS, int q, int r) { return wpad_c(q * 32 + r * (N / RS)); }
-__host__ __device__ constexpr int st_lane(int RS, int NS, int t) {
-  return NS >= 32 ? t + (t >> 4) : (t / NS) * NS * RS + t % NS + (((t / NS) * NS * RS) >> 4);
+__host__ __device__ constexpr int wpad_c(int N, int p) { return p + (p >> pad_shift(N)); }
+__host__ __device__ constexpr int ld_lane(int N, int t) { return t + (t >> pad_shift(N)); }
+__host__ __device__ constexpr int ld_off(int N, int RS, int q, int r) { return wpad_c(N, q * 32 + r * (N / RS)); }
+__host__ __device__ constexpr int st_lane(int N, int RS, int NS, int t) {
+  return NS >= 32 ? t + (t >> pad_shift(N))
+                  : (t / NS) * NS * RS + t % NS + (((t / NS) * NS * RS) >> pad_shift(N));
 }
-__host__ __device__ constexpr int st_off(int RS, int NS, int q, int r) {
-  return NS >= 32 ? wpad_c((q * 32 / NS) * NS * RS + (q * 32) % NS + r * NS)
-                  : wpad_c(q * 32 * RS) + r * NS + ((r * NS) >> 4);
+__host__ __device__ constexpr int st_off(int N, int RS, int NS, int q, int r) {
+  return NS >= 32 ? wpad_c(N, (q * 32 / NS) * NS * RS + (q * 32) % NS + r * NS)
+                  : wpad_c(N, q * 32 * RS) + r * NS + ((r * NS) >> pad_shift(N));
 }
 __host__ __device__ constexpr bool warp_index_check(int N, int RS, int NS) {
   const int Q = (N / 32) / RS;
   for (int t = 0; t < 32; t++)
     for (int q = 0; q < Q; q++)
       for (int r = 0; r < RS; r++) {
-        if (ld_lane(t) + ld_off(N, RS, q, r) != wpad_c(q * 32 + t + r * (N / RS))) return false;
+        if (ld_lane(N, t) + ld_off(N, RS, q, r) != wpad_c(N, q * 32 + t + r * (N / RS))) return false;
         const int j = q * 32 + t;
-        if (st_lane(RS, NS, t) + st_off(RS, NS, q, r) != wpad_c((j / NS) * NS * RS + j % NS + r * NS)) return false;
+        if (st_lane(N, RS, NS, t) + st_off(N, RS, NS, q, r) != wpad_c(N, (j / NS) * NS * RS + j % NS + r * NS))
+          return false;
       }
   return true;
 }
@@ -91,7 +94,7 @@ __device__ __forceinline__ void warp_stage(float2 (&v)[N / 32], float2* buf, con
 #pragma unroll
       for (int r = 0; r < RS; r++) a[q * RS + r] = v[q + r * Q];
   } else {
-    const float2* bl = buf + ld_lane(t);
+    const float2* bl = buf + ld_lane(N, t);
 #pragma unroll
     for (int q = 0; q < Q; q++)
 #pragma unroll
@@ -118,11 +121,11 @@ __device__ __forceinline__ void warp_stage(float2 (&v)[N / 32], float2* buf, con
       for (int r = 0; r < RS; r++) v[q + r * (NS / 32)] = a[q * RS + r];
   } else {
     __syncwarp();  // every lane is done reading the buffer (previous stage or transform)
-    float2* bs = buf + st_lane(RS, NS, t);
+    float2* bs = buf + st_lane(N, RS, NS, t);
 #pragma unroll
     for (int q = 0; q < Q; q++)
 #pragma unroll
-      for (int r = 0; r < RS; r++) bs[st_off(RS, NS, q, r)] = a[q * RS + r];
+      for (int r = 0; r < RS; r++) bs[st_off(N, RS, NS, q, r)] = a[q * RS + r];
     __syncwarp();
   }
 }
@@ -144,7 +147,7 @@ __device__ __forceinline__ void warp_fft_from(float2 (&v)[N / 32], float2* buf, 
 // tw: the stage-ordered twiddle table (WarpFft<N>::TW entries, see wtw_offset).
 template <int N, bool INV>
 __device__ __forceinline__ void warp_fft(float2 (&v)[N / 32], float2* buf, const float2* __restrict__ tw, int t) {
-  static_assert(N >= 64 && N <= 512, "warp FFT covers 64..512 points");
+  static_assert(N >= 64 && N <= 1024, "warp FFT covers 64..1024 points");
   warp_fft_from<N, 1, INV>(v, buf, tw, t);
 }
 
@@ -175,17 +178,33 @@ struct ColSplit {
   static_assert(NS_LAST >= 32 && NS_LAST < N, "last stage spans whole 32-row groups");
 };
 
+// padded positions the tile-mapping stages use, split as in colsplit_first / colsplit_last
+// (checked against the direct formula for every thread at compile time)
+__host__ __device__ constexpr bool colsplit_index_check(int N) {
+  const int E = N / 32, S = pad_shift(N), NS = colsplit_last_ns(N), RS = N / NS;
+  for (int r0 = 0; r0 < 32; r0++) {
+    for (int r = 0; r < E; r++)
+      if (r0 * E + ((r0 * E) >> S) + r != wpad_c(N, r0 * E + r)) return false;
+    for (int q = 0; q < NS / 32; q++)
+      for (int r = 0; r < RS; r++)
+        if (r0 + (r0 >> S) + (32 + (32 >> S)) * q + (NS + (NS >> S)) * r != wpad_c(N, r0 + 32 * q + NS * r))
+          return false;
+  }
+  return true;
+}
+
 // first stage (radix E, stride 1) of column cc from the thread's rows r0 + 32 r, written to
-// positions r0*E + r of the column's buffer (padded index p + p/16; r0*E + r stays inside
-// one 16-element run, so the pad is that of r0*E)
+// positions r0*E + r of the column's buffer (padded index p + (p >> S); r0*E + r stays
+// inside one 2^S-element run, so the pad is that of r0*E)
 template <int N, bool INV>
 __device__ __forceinline__ void colsplit_first(const float2 (&v)[N / 32], float2* colbuf, int r0) {
   constexpr int E = N / 32;
+  static_assert(colsplit_index_check(N), "column-split index split");
   float2 a[E];
 #pragma unroll
   for (int r = 0; r < E; r++) a[r] = v[r];
   Dft<E, INV>::run(a);
-  float2* b = colbuf + r0 * E + ((r0 * E) >> 4);
+  float2* b = colbuf + r0 * E + ((r0 * E) >> pad_shift(N));
 #pragma unroll
   for (int r = 0; r < E; r++) b[r] = a[r];
 }
@@ -209,8 +228,8 @@ __device__ __forceinline__ void colsplit_middle(float2* buf, const float2* __res
 }
 
 // last stage of column cc: butterflies j = r0 + 32 q read positions j + NS r (padded index:
-// (r0 + r0/16) + 34 q + (NS + NS/16) r), twiddle entries (r-1)*NS + j of the stage, and
-// leave row j + NS r in v[q + (NS/32) r]
+// (r0 + r0>>S) + (32 + 32>>S) q + (NS + NS>>S) r), twiddle entries (r-1)*NS + j of the stage,
+// and leave row j + NS r in v[q + (NS/32) r]
 template <int N, bool INV>
 __device__ __forceinline__ void colsplit_last(float2 (&v)[N / 32], const float2* colbuf,
                                               const float2* __restrict__ tw, int r0) {
@@ -219,11 +238,12 @@ __device__ __forceinline__ void colsplit_last(float2 (&v)[N / 32], const float2*
   constexpr int Q = NS / 32;
   constexpr int TWOFF = wtw_offset(N, NS);
   float2 a[N / 32];
-  const float2* b = colbuf + r0 + (r0 >> 4);
+  constexpr int S = pad_shift(N);
+  const float2* b = colbuf + r0 + (r0 >> S);
 #pragma unroll
   for (int q = 0; q < Q; q++)
 #pragma unroll
-    for (int r = 0; r < RS; r++) a[q * RS + r] = b[34 * q + (NS + NS / 16) * r];
+    for (int r = 0; r < RS; r++) a[q * RS + r] = b[(32 + (32 >> S)) * q + (NS + (NS >> S)) * r];
   const float2* twl = tw + TWOFF + r0;
 #pragma unroll
   for (int q = 0; q < Q; q++)

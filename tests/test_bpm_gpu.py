@@ -63,7 +63,8 @@ def test_golden_class_path(bpm, golden):
 @pytest.mark.parametrize("size,mode", [
     ((128, 128, 64), "weighted"), ((128, 128, 64), "simple"), ((128, 128, 64), "ignore"),
     ((256, 128, 24), "weighted"), ((16, 16, 8), "weighted"), ((32, 1024, 6), "ignore"),
-    ((1024, 32, 6), "simple"), ((512, 512, 12), "weighted"),
+    ((1024, 32, 6), "simple"), ((512, 512, 12), "weighted"), ((1024, 64, 6), "weighted"),
+    ((64, 1024, 6), "weighted"),
 ])
 def test_oracle_parity(bpm, size, mode):
     Nx, Ny, Nz = size
@@ -78,6 +79,25 @@ def test_oracle_parity(bpm, size, mode):
     assert rel_l2(u, o64) < TOL
     assert rel_l2(u, o32) < TOL
     del rng
+
+
+@pytest.mark.parametrize("size,mode", [((1024, 256, 5), "weighted"), ((256, 1024, 5), "ignore")])
+def test_batched_1024_matches_single_and_oracle(bpm, size, mode):
+    """1024-point rows and columns in the warp-FFT family (32 values per lane, one exchange
+    per transform): a batch of 3 fields with a shared dn (shared-mask row kernel, 16-column
+    split kernels) equals each field marched alone (narrow single-field kernels) bit for
+    bit, and matches the FP64 oracle."""
+    Nx, Ny, Nz = size
+    dn = sphere_dn(Nx, Ny, Nz, 40, .05)
+    x = .1 * np.arange(Nx)
+    u0 = np.stack([np.exp(2j * np.pi * f * x)[None, :].repeat(Ny, 0) for f in (0, .2, -.35)]).astype(np.complex64)
+    kw = dict(lam=.5, n0=1.33, dn=dn, mean_mode=mode, absorbing_width=4)
+    batch = bpm.bpm_3d_batched(size, (.1, .1, .1), u0=u0, return_field=True, **kw)
+    for b in range(3):
+        single = bpm.bpm_3d(size, (.1, .1, .1), u0=u0[b], **kw)
+        assert bool(np.array_equal(batch[b], single)), b
+        o64 = bpm_ref.bpm_3d(size, (.1, .1, .1), u0=u0[b], precision="fp64", **kw)
+        assert rel_l2(single, o64) < TOL
 
 
 def test_config1_plain(bpm):
