@@ -674,12 +674,6 @@ struct WarpCfg {
   static constexpr size_t row_smem(int rw) { return ((size_t)N + (size_t)rw * WarpFft<N>::BUF) * sizeof(float2); }
   static constexpr size_t ROW_SMEM = row_smem(kRowWarps);
   static constexpr size_t ROW_SMEM_SHARED = ROW_SMEM + (size_t)N * sizeof(float2);  // + the staged row
-  static constexpr size_t COL_F2 = (size_t)N + (size_t)kColWarps * WarpFft<N>::BUF;  // twiddles, tile/exchange
-  static constexpr size_t COL_SMEM = COL_F2 * sizeof(float2);
-  // the weighted-reduction pass also stages the tile's dn slice-0 values (up to 4 bytes each)
-  static constexpr size_t COL_SMEM_DN = COL_SMEM + (size_t)16 * N * sizeof(float);
-  // the propagating passes also stage the ky^2 table
-  static constexpr size_t COL_SMEM_KY = COL_SMEM + (size_t)N * sizeof(float);
 };
 
 // Row pass, one warp per row: coalesced row load straight into registers, [inverse row
@@ -817,193 +811,17 @@ row_shared_kernel(RowParams p, int nfields) {
   for (int m = 0; m < E; m++) dst[t + 32 * m] = v[m];
 }
 
-// Column pass, one warp per column of a 16-column tile: coalesced tile load into shared
-// memory, then every warp takes its column into registers. WHICH: 0 = forward FFT,
-// propagator, inverse FFT; 1 = forward FFT + weighted-mode partial sums (k-space stored
-// back); 2 = n from the partial sums, propagator, inverse FFT.
-// Addressing: in the coalesced mapping thread (r0, cc) = (tid / 16, tid % 16) handles rows
-// r0 + 32 i of column x0 + cc, so its tile slots are tile_idx(r0, cc) + 512 i and its plane
-// elements gofs + 32 nx i (32-bit: a plane has at most 2^19 elements here); warp w's column
-// slots are tile_idx(t, w) + 512 m. The common cases (table propagator, FP32 recipe without
-// scattering sums, staged dn) run loops free of per-element branches with the arithmetic
-// of the general path in the same order, so they give the same bits.
-template <int N, int WHICH>
-__global__ void __launch_bounds__(kColWarps * 32, 2)
-col_warp_kernel(ColParams p) {
-  constexpr int E = N / 32;
-  constexpr int T = kColWarps * 32;
-  static_assert(T == 512, "the coalesced mapping steps 32 rows at a time");
-  extern __shared__ float2 smem[];
-  float2* tw = smem;
-  float2* tile = smem + N;  // the 16 x N tile, then the warps' exchange buffers
-  __shared__ float red[64];
-  __shared__ float s_n;
-  const int warp = threadIdx.x >> 5, t = threadIdx.x & 31;
-  const int gl = blockIdx.y;
-  const int x0 = blockIdx.x * kColWarps;
-  const int x = x0 + warp;
-  float2* Wp = p.W + (size_t)gl * p.nx * N;
-  constexpr int PER = 16 * N / T;
-  const int r0 = threadIdx.x >> 4, cc = threadIdx.x & 15;
-  const unsigned gstep = 32u * (unsigned)p.nx;
-  const int ts = (r0 << 4) + (cc ^ (r0 & 15));  // tile_idx(r0 + 32 i, cc) - 512 i
-  const int tc = (t << 4) + (warp ^ (t & 15));  // tile_idx(t + 32 m, warp) - 512 m
-  static_assert(WarpFft<N>::TW <= T && N <= T, "one twiddle and one ky^2 entry per thread");
-  // plan constants first (the twiddle table; the propagator recipe's ky^2 column, staged
-  // next to the tile), then the wait for the previous pass
-  const float2 twv = threadIdx.x < WarpFft<N>::TW ? p.wtw[threadIdx.x] : make_float2(0.f, 0.f);
-  float* sky2 = reinterpret_cast<float*>(smem + WarpCfg<N>::COL_F2);
-  const bool stage_ky = WHICH != 1 && p.prop_mode != 0;
-  const float kyv = (stage_ky && threadIdx.x < N) ? p.ky2[threadIdx.x] : 0.f;
-  dep_wait();
-  dep_release();
-  // weighted reduction: dn slice 0 of this tile goes to shared memory with cp.async now and
-  // is read only after the transform; a 16-value row is 2^lg 16-byte pieces
-  const char* dn_stage = nullptr;
-  if (WHICH == 1 && p.dn && p.dn_stage) {
-    const int lg = p.dn_dtype == BPM_DN_F16 ? 1 : 2;
-    const int es = 1 << lg;
-    char* dst = reinterpret_cast<char*>(smem + WarpCfg<N>::COL_F2);
-    const char* srcb = static_cast<const char*>(p.dn) + ((size_t)gl * p.dn_bstride + x0) * es;
-    const size_t rowb = (size_t)p.nx * es;
-    for (int ch = threadIdx.x; ch < (N << lg); ch += T)
-      cp_async16(dst + (size_t)ch * 16, srcb + (size_t)(ch >> lg) * rowb + (ch & (es - 1)) * 16);
-    cp_async_commit();
-    dn_stage = dst;
-  }
-  // the tile loads go out before any shared-memory store waits on them
-  float2 ld[PER];
-  {
-    const unsigned gofs = (unsigned)r0 * (unsigned)p.nx + (unsigned)(x0 + cc);
-#pragma unroll
-    for (int i = 0; i < PER; i++) ld[i] = Wp[gofs + i * gstep];
-  }
-  if (WHICH == 2 && warp == 0) {
-    // every block of the field sums the partials in index order, so all get the same n; the
-    // lanes fetch them at once (at most 64: nx <= 1024) and pass them on by shuffles
-    const int np = p.nx / 16;
-    const float* part = p.red_part + (size_t)gl * np * 2;
-    const float d0 = t < np ? part[2 * t] : 0.f, u0 = t < np ? part[2 * t + 1] : 0.f;
-    const float d1 = t + 32 < np ? part[2 * t + 64] : 0.f, u1 = t + 32 < np ? part[2 * t + 65] : 0.f;
-    float dn_sum = 0.f, u_sum = 0.f;
-    for (int i = 0; i < np; i++) {
-      dn_sum += __shfl_sync(0xffffffffu, i < 32 ? d0 : d1, i & 31);
-      u_sum += __shfl_sync(0xffffffffu, i < 32 ? u0 : u1, i & 31);
-    }
-    if (t == 0) {
-      const float dn0 = dn_sum / u_sum;  // mult_dn_mean_buff, bpm_3d_kernels.cl:117
-      s_n = p.n00f + dn0;                // mult_propagator_buff, bpm_3d_kernels.cl:482
-      if (blockIdx.x == 0) p.dn0_field[gl] = dn0;
-    }
-  }
-#pragma unroll
-  for (int i = 0; i < PER; i++) tile[ts + 512 * i] = ld[i];
-  if (threadIdx.x < WarpFft<N>::TW) tw[threadIdx.x] = twv;
-  if (stage_ky && threadIdx.x < N) sky2[threadIdx.x] = kyv;
-  __syncthreads();
-  float2 v[E];
-#pragma unroll
-  for (int m = 0; m < E; m++) v[m] = tile[tc + 512 * m];
-  __syncthreads();
-  float2* buf = tile + warp * WarpFft<N>::BUF;
-  if (WHICH != 2) warp_fft<N, false>(v, buf, tw, t);
-  if (WHICH != 1) {
-    const float n_eff = WHICH == 2 ? s_n : (p.prop_mode == 1 ? p.slice_n[p.z + 1] : p.n00f);
-    const float nk = prop_nk(p, n_eff);
-    if (!p.scat && p.prop_mode == 0) {
-      // table H, transposed so the column is contiguous; conj(H) for the adjoint
-      const float2* hp = p.Ht + (size_t)x * p.ny + t;
-      const bool cj = p.conj_h;
-#pragma unroll
-      for (int m = 0; m < E; m++) {
-        float2 h = __ldg(hp + 32 * m);
-        if (cj) h.y = -h.y;
-        v[m] = cscale(cmul(v[m], h), p.scale);
-      }
-    } else if (!p.scat) {
-      // FP32 recipe of bpm_3d_kernels.cl:408-432 on the staged ky^2 column
-      const float nkx = __fsub_rn(nk, __ldg(p.kx2 + x));
-#pragma unroll
-      for (int m = 0; m < E; m++) {
-        const float tmp = __fsub_rn(nkx, sky2[t + 32 * m]);
-        float2 h = make_float2(0.f, 0.f);
-        if (tmp >= 0.f) {
-          const float ph = __fmul_rn(-p.dzf, __fsqrt_rn(tmp));
-          sincosf(ph, &h.y, &h.x);
-        }
-        v[m] = cscale(cmul(v[m], h), p.scale);
-      }
-    } else {
-      const float2 plain = x == 0 ? plain_wave(p) : make_float2(0.f, 0.f);
-      float S = 0.f, G = 0.f;
-#pragma unroll
-      for (int m = 0; m < E; m++) v[m] = prop_point<true>(p, v[m], x, t + 32 * m, nk, plain, S, G, sky2);
-      scat_partials_store<T>(p, S, G, gl, red);
-    }
-    warp_fft<N, true>(v, buf, tw, t);
-  }
-  __syncthreads();
-#pragma unroll
-  for (int m = 0; m < E; m++) tile[tc + 512 * m] = v[m];
-  if (WHICH == 1 && dn_stage) cp_async_wait<0>();  // this thread's dn pieces have landed
-  __syncthreads();
-  const unsigned gofs = (unsigned)(threadIdx.x >> 4) * (unsigned)p.nx + (unsigned)(x0 + (threadIdx.x & 15));
-  if (WHICH == 1) {
-    // weighted mode: sum |u_hat| and |u_hat|*dn over the tile while storing it, with the
-    // coalesced tile mapping (dn slice 0 read 16 columns at a time)
-    float sdn = 0.f, su = 0.f;
-    if (dn_stage && p.dn_dtype != BPM_DN_F16) {
-      const float* ds = reinterpret_cast<const float*>(dn_stage) + threadIdx.x;
-#pragma unroll
-      for (int i = 0; i < PER; i++) {
-        const float2 u = tile[ts + 512 * i];
-        Wp[gofs + i * gstep] = u;
-        const float a = __fsqrt_rn(cabs2(u));
-        su += a;
-        sdn = fmaf(a, ds[T * i], sdn);
-      }
-    } else if (dn_stage) {
-      const __half* ds = reinterpret_cast<const __half*>(dn_stage) + threadIdx.x;
-#pragma unroll
-      for (int i = 0; i < PER; i++) {
-        const float2 u = tile[ts + 512 * i];
-        Wp[gofs + i * gstep] = u;
-        const float a = __fsqrt_rn(cabs2(u));
-        su += a;
-        sdn = fmaf(a, __half2float(ds[T * i]), sdn);
-      }
-    } else {
-#pragma unroll 4
-      for (int i = 0; i < PER; i++) {
-        const float2 u = tile[ts + 512 * i];
-        const unsigned k = gofs + i * gstep;
-        Wp[k] = u;
-        const float a = __fsqrt_rn(cabs2(u));
-        su += a;
-        if (p.dn) sdn = fmaf(a, load_dn_real(p.dn, p.dn_dtype, gl * p.dn_bstride + k), sdn);
-      }
-    }
-    block_sum2<T>(sdn, su, red);
-    if (threadIdx.x == 0) {
-      float* o = p.red_part + ((size_t)gl * (p.nx / 16) + blockIdx.x) * 2;
-      o[0] = sdn;
-      o[1] = su;
-    }
-  } else {
-#pragma unroll
-    for (int i = 0; i < PER; i++) Wp[gofs + i * gstep] = tile[ts + 512 * i];
-  }
-}
-
 // Column pass without the tile transposition (128 <= N <= 512, no scattering sums). The
 // block's 32*C threads load C columns (16, or 8 for small non-weighted passes) in the
 // coalesced tile mapping — thread (r0, cc) = (tid / C, tid % C) holds rows r0 + 32 i of column
 // x0 + cc — and keep that mapping for every pointwise step (the propagator from the
 // row-major table or the FP32 recipe, the weighted partial sums, the loads and stores); the
 // first and last FFT stages run in it as well (colsplit_first / colsplit_last) and only the
-// middle stages per warp, on the column's exchange buffer. WHICH as col_warp_kernel, whose
-// results it reproduces bit for bit. The weighted passes keep C = 16: their per-block
-// partial sums then group the same elements in the same order as every other kernel's.
+// middle stages per warp, on the column's exchange buffer. WHICH: 0 = forward FFT,
+// propagator, inverse FFT; 1 = forward FFT + weighted-mode partial sums (k-space stored back);
+// 2 = n from the partial sums, propagator, inverse FFT. The weighted passes keep C = 16: their
+// per-block partial sums then group the same elements in the same order as the cluster
+// kernel's.
 // Column buffers are STRIDE float2 apart: with 16 columns an odd stride puts a half-warp's
 // 16 columns on 16 different bank pairs; with 8 columns a half-warp spans two rows of 8
 // columns, conflict-free at N = 512 and 1024 for stride BUF + 2, 2-way on some accesses at
@@ -1018,44 +836,66 @@ struct ColSplitCfg {
   static constexpr size_t SMEM_KY = SMEM + (size_t)N * sizeof(float);       // + the ky^2 column
 };
 
-// the propagator on the thread's rows r0 + 32 i of column x (prop_point's arithmetic without
-// the scattering sums): the row-major table H (conj(H) for the adjoint) or the FP32 recipe
-// with kx^2 of the column and the ky^2 table staged in shared memory
-template <int N>
-__device__ __forceinline__ void propagate_rows(const ColParams& p, float2 (&v)[N / 32], int x, int r0,
-                                               float n_eff, float kx2, const float* sky2) {
+// the propagator on the thread's rows r0 + 32 i of column x (prop_point's arithmetic): the
+// row-major table H (conj(H) for the adjoint; TABLE) or the FP32 recipe with kx^2 of the
+// column and the ky^2 table staged in shared memory; with scattering sums
+// (bpm_3d.py:335-341) the thread's partials S, G over its rows
+template <int N, bool TABLE, bool SCAT>
+__device__ __forceinline__ void propagate_rows_t(const ColParams& p, float2 (&v)[N / 32], int x, int r0,
+                                                 float n_eff, float kx2, const float* sky2, float& S, float& G) {
   const unsigned step = 32u * (unsigned)p.nx;
-  if (p.prop_mode == 0) {
-    const float2* hp = p.H + ((unsigned)r0 * (unsigned)p.nx + (unsigned)x);
-    const bool cj = p.conj_h;
-#pragma unroll
-    for (int i = 0; i < N / 32; i++) {
-      float2 h = __ldg(hp + i * step);
+  const unsigned off = (unsigned)r0 * (unsigned)p.nx + (unsigned)x;
+  const bool cj = p.conj_h;
+  const float nkx = TABLE ? 0.f : __fsub_rn(prop_nk(p, n_eff), kx2);
+  auto hval = [&](int i) {
+    float2 h;
+    if constexpr (TABLE) {
+      h = __ldg(p.H + off + i * step);
       if (cj) h.y = -h.y;
-      v[i] = cscale(cmul(v[i], h), p.scale);
-    }
-  } else {
-    const float nkx = __fsub_rn(prop_nk(p, n_eff), kx2);
-#pragma unroll
-    for (int i = 0; i < N / 32; i++) {
+    } else {
       const float tmp = __fsub_rn(nkx, sky2[r0 + 32 * i]);
-      float2 h = make_float2(0.f, 0.f);
+      h = make_float2(0.f, 0.f);
       if (tmp >= 0.f) {
         const float ph = __fmul_rn(-p.dzf, __fsqrt_rn(tmp));
         sincosf(ph, &h.y, &h.x);
       }
-      v[i] = cscale(cmul(v[i], h), p.scale);
     }
+    return h;
+  };
+  if constexpr (!SCAT) {
+#pragma unroll
+    for (int i = 0; i < N / 32; i++) v[i] = cscale(cmul(v[i], hval(i)), p.scale);
+    return;
+  }
+  const float2 plain = (x == 0 && r0 == 0) ? plain_wave(p) : make_float2(0.f, 0.f);
+#pragma unroll
+  for (int i = 0; i < N / 32; i++) {
+    const float2 u = cmul(v[i], hval(i));
+    float2 d = u;
+    if (x == 0 && r0 == 0 && i == 0) d = csub(d, plain);
+    const float a2 = cabs2(d);
+    S = fmaf(__ldg(p.sw + off + i * step), a2, S);
+    G = fmaf(__ldg(p.gw + off + i * step), a2, G);
+    v[i] = cscale(u, p.scale);
   }
 }
+template <int N, bool SCAT>
+__device__ __forceinline__ void propagate_rows(const ColParams& p, float2 (&v)[N / 32], int x, int r0,
+                                               float n_eff, float kx2, const float* sky2, float& S, float& G) {
+  if (p.prop_mode == 0)
+    propagate_rows_t<N, true, SCAT>(p, v, x, r0, n_eff, kx2, sky2, S, G);
+  else
+    propagate_rows_t<N, false, SCAT>(p, v, x, r0, n_eff, kx2, sky2, S, G);
+}
 
-template <int N, int WHICH, int C = kColWarps>
+template <int N, int WHICH, int C = kColWarps, bool SCAT = false>
 __global__ void __launch_bounds__(C * 32, (C == 16 ? 2 : 4) / (N > 512 ? 2 : 1))
 col_split_kernel(ColParams p) {
   using Cfg = ColSplitCfg<N, C>;
   constexpr int E = N / 32;
   constexpr int T = C * 32;
   static_assert(C == 16 || (C == 8 && WHICH == 0), "weighted passes keep 16-column blocks");
+  static_assert(!SCAT || (C == 16 && WHICH != 1), "scattering partials per 16-column tile");
   extern __shared__ __align__(16) float2 smem[];
   float2* tw = smem;
   float2* bufs = smem + Cfg::TW_F2;
@@ -1112,7 +952,8 @@ col_split_kernel(ColParams p) {
     for (int i = 0; i < E; i++) v[i] = Wp[gofs + i * gstep];
   }
   if (WHICH == 2 && warp == 0) {
-    // as col_warp_kernel: the partials summed in index order, fetched at once by the lanes
+    // every block of the field sums the partials in index order, so all get the same n; the
+    // lanes fetch them at once (at most 64: nx <= 1024) and pass them on by shuffles
     const int np = p.nx / 16;
     const float* part = p.red_part + (size_t)gl * np * 2;
     const float d0 = t < np ? part[2 * t] : 0.f, u0 = t < np ? part[2 * t + 1] : 0.f;
@@ -1134,9 +975,10 @@ col_split_kernel(ColParams p) {
 #pragma unroll
   for (int k = 0; k < KYR; k++)
     if (recipe && threadIdx.x + k * T < N) sky2[threadIdx.x + k * T] = kyv[k];
+  float S = 0.f, G = 0.f;  // scattering partials
   if (WHICH == 2) {
     __syncthreads();  // s_n, ky^2
-    propagate_rows<N>(p, v, x0 + cc, r0, s_n, kx2v, sky2);
+    propagate_rows<N, SCAT>(p, v, x0 + cc, r0, s_n, kx2v, sky2, S, G);
   } else {
     // forward column FFT
     colsplit_first<N, false>(v, colbuf, r0);
@@ -1146,10 +988,12 @@ col_split_kernel(ColParams p) {
     colsplit_last<N, false>(v, colbuf, tw, r0);
   }
   if (WHICH == 0) {
-    propagate_rows<N>(p, v, x0 + cc, r0, p.prop_mode == 1 ? p.slice_n[p.z + 1] : p.n00f, kx2v, sky2);
+    propagate_rows<N, SCAT>(p, v, x0 + cc, r0, p.prop_mode == 1 ? p.slice_n[p.z + 1] : p.n00f, kx2v, sky2, S,
+                            G);
     __syncthreads();  // every thread has read its last-stage inputs before the buffers are reused
   }
   if (WHICH != 1) {
+    if constexpr (SCAT) scat_partials_store<T>(p, S, G, gl, red);
     // inverse column FFT, then the coalesced store
     colsplit_first<N, true>(v, colbuf, r0);
     __syncthreads();
@@ -1161,7 +1005,7 @@ col_split_kernel(ColParams p) {
     for (int i = 0; i < E; i++) Wp[gofs + i * gstep] = v[i];
   } else {
     // weighted mode: store k-space and sum |u_hat| and |u_hat|*dn over the tile, each thread
-    // over its rows in order (col_warp_kernel's order)
+    // over its rows in order
     if (dn_stage) cp_async_wait<0>();
     __syncthreads();  // the dn pieces other threads copied
     const unsigned gofs = (unsigned)r0 * (unsigned)p.nx + (unsigned)(x0 + cc);
@@ -1204,257 +1048,23 @@ col_split_kernel(ColParams p) {
 }
 
 // ---------------------------------------------------------------------------------------
-// Pipelined persistent kernels (128 <= N <= 512). A launch holds as many blocks as fit on
-// the device at once; each warp (row pass) or block (column pass) walks a strided list of
-// rows or 16-column tiles and copies the next item's inputs into shared memory with
-// cp.async while it transforms the current one, so the global-memory latency of one item
-// hides behind the arithmetic of the previous one instead of stalling every block of a
-// single wave at the same time. Same arithmetic, in the same order, as the warp kernels
-// above, and the same bits (every multiply-add of the shared arithmetic is an explicit fmaf).
-// ---------------------------------------------------------------------------------------
-template <int N>
-struct PipeCfg {
-  static constexpr int TWPAD = (WarpFft<N>::TW + 1) & ~1;  // keeps the regions after it 16-byte aligned
-  static constexpr int ROW_WARP_F2 = WarpFft<N>::BUF + 2 * N;  // exchange buffer, row landing, mask landing
-  static constexpr size_t ROW_SMEM = ((size_t)TWPAD + (size_t)kRowWarps * ROW_WARP_F2) * sizeof(float2);
-  static constexpr size_t COL_SMEM =
-      ((size_t)TWPAD + 2 * 16 * (size_t)N + (size_t)kColWarps * WarpFft<N>::BUF) * sizeof(float2);
-  static_assert(WarpFft<N>::BUF % 2 == 0 && TWPAD % 2 == 0, "16-byte aligned regions");
-};
-
-// the warp copies bytes [src, src + bytes) into dst in 16-byte pieces (bytes % 16 == 0,
-// both addresses 16-byte aligned)
-__device__ __forceinline__ void warp_copy_async(void* dst, const void* src, int bytes, int t) {
-  const char* s = static_cast<const char*>(src);
-  char* d = static_cast<char*>(dst);
-  for (int o = t * 16; o < bytes; o += 32 * 16) cp_async16(d + o, s + o);
-}
-
-// Forward row pass over rows r = gw, gw + nw, ... of the group (r = field * ny + y).
-template <int N, int PRE>
-__global__ void __launch_bounds__(kRowWarps * 32, 2)
-row_pipe_kernel(RowParams p, int nrows) {
-  constexpr int E = N / 32;
-  constexpr int T = kRowWarps * 32;
-  extern __shared__ __align__(16) float2 smem[];
-  float2* tw = smem;
-  const int warp = threadIdx.x >> 5, t = threadIdx.x & 31;
-  float2* buf = smem + PipeCfg<N>::TWPAD + warp * PipeCfg<N>::ROW_WARP_F2;
-  float2* land = buf + WarpFft<N>::BUF;
-  float2* mland = land + N;
-  if (p.do_inv || p.do_fwd) {
-    for (int k = threadIdx.x; k < WarpFft<N>::TW; k += T) tw[k] = p.wtw[k];
-    __syncthreads();
-  }
-  dep_wait();
-  dep_release();
-  const size_t plane = (size_t)N * p.ny;
-  const int dn_es = p.dn_dtype == BPM_DN_C64 ? 8 : (p.dn_dtype == BPM_DN_F16 ? 2 : 4);
-  const size_t zoff = (size_t)p.z * plane;
-  const size_t ooff = (size_t)(p.z - p.zout0) * plane;
-  const bool last = (p.z == p.nz - 1);
-  const int nw = gridDim.x * kRowWarps;
-
-  auto issue_row = [&](int rr) {
-    const int gl = rr / p.ny, y = rr - gl * p.ny;
-    warp_copy_async(land, p.src + gl * p.src_bstride + (size_t)y * N, N * 8, t);
-  };
-  auto issue_mask = [&](int rr) {
-    if (!p.do_mask) return;
-    const int gl = rr / p.ny, y = rr - gl * p.ny;
-    if (PRE)
-      warp_copy_async(mland, p.mask + zoff + (size_t)y * N, N * 8, t);
-    else
-      warp_copy_async(mland,
-                      static_cast<const char*>(p.dn) + ((size_t)gl * p.dn_bstride + zoff + (size_t)y * N) * dn_es,
-                      N * dn_es, t);
-  };
-
-  // commit groups alternate row, mask, row, mask, ...: waiting until one group is pending
-  // completes the older of the two
-  int r = blockIdx.x * kRowWarps + warp;
-  if (r < nrows) issue_row(r);
-  cp_async_commit();
-  if (r < nrows) issue_mask(r);
-  cp_async_commit();
-  for (; r < nrows; r += nw) {
-    const int gl = r / p.ny, y = r - gl * p.ny;
-    cp_async_wait<1>();  // row r
-    __syncwarp();
-    float2 v[E];
-#pragma unroll
-    for (int m = 0; m < E; m++) v[m] = land[t + 32 * m];
-    __syncwarp();
-    const int rn = r + nw;
-    if (rn < nrows) issue_row(rn);
-    cp_async_commit();
-    if (p.do_inv) warp_fft<N, true>(v, buf, tw, t);
-
-    const float dn0 = row_dn0(p, gl);
-    const float2 rot = row_rot(p, dn0);
-    float2* ckp = nullptr;
-    if (p.ckpt && p.z % p.ckpt_every == 0) ckp = p.ckpt + ((size_t)gl * p.n_ckpt + p.z / p.ckpt_every) * plane;
-    cp_async_wait<1>();  // mask row r
-    __syncwarp();
-#pragma unroll
-    for (int m = 0; m < E; m++) {
-      const int x = t + 32 * m;
-      const size_t pix = (size_t)y * N + x;
-      float2 u = v[m];
-      if (p.do_mask) {
-        u = cmul(u, staged_mask<PRE>(p, mland, x, y));
-        if (dn0 != 0.f) u = cmul(u, rot);
-      }
-      if (p.out_kind == BPM_OUT_FIELD)
-        __stcs(reinterpret_cast<float2*>(p.out) + gl * p.out_bstride + ooff + pix, u);
-      else if (p.out_kind == BPM_OUT_INTENSITY)
-        __stcs(reinterpret_cast<float*>(p.out) + gl * p.out_bstride + ooff + pix, cabs2(u));
-      if (last && p.last_plane) p.last_plane[gl * plane + pix] = u;
-      if (ckp) ckp[pix] = u;
-      v[m] = u;
-    }
-    __syncwarp();
-    if (rn < nrows) issue_mask(rn);
-    cp_async_commit();
-    if (p.scat_p && y == 0 && t == 0) row_scatter_finish(p, gl);
-    if (p.do_fwd) {
-      warp_fft<N, false>(v, buf, tw, t);
-      float2* dst = p.W + gl * plane + (size_t)y * N;
-#pragma unroll
-      for (int m = 0; m < E; m++) dst[t + 32 * m] = v[m];
-    }
-  }
-  cp_async_wait<0>();
-}
-
-// Column pass over 16-column tiles it = blockIdx.x, + gridDim.x, ... of the group
-// (it = field * (nx/16) + tile), double-buffered in shared memory. WHICH as col_warp_kernel.
-template <int N, int WHICH>
-__global__ void __launch_bounds__(kColWarps * 32, 1)
-col_pipe_kernel(ColParams p, int ntiles) {
-  constexpr int E = N / 32;
-  constexpr int T = kColWarps * 32;
-  constexpr int PER = 16 * N / T;
-  extern __shared__ __align__(16) float2 smem[];
-  float2* tw = smem;
-  float2* tiles = smem + PipeCfg<N>::TWPAD;
-  __shared__ float red[64];
-  __shared__ float s_n;
-  const int warp = threadIdx.x >> 5, t = threadIdx.x & 31;
-  float2* buf = tiles + 2 * 16 * N + warp * WarpFft<N>::BUF;
-  const int tpf = p.nx / 16;
-  for (int k = threadIdx.x; k < WarpFft<N>::TW; k += T) tw[k] = p.wtw[k];
-  auto issue_tile = [&](float2* dst, int it) {
-    const int gl = it / tpf, x0 = (it - gl * tpf) * 16;
-    const float2* Wp = p.W + (size_t)gl * p.nx * N;
-#pragma unroll
-    for (int i = 0; i < PER; i++) {
-      const int e = threadIdx.x + i * T;
-      cp_async8(dst + tile_idx(e >> 4, e & 15), Wp + (size_t)(e >> 4) * p.nx + x0 + (e & 15));
-    }
-  };
-  dep_wait();
-  dep_release();
-  int it = blockIdx.x;
-  if (it < ntiles) issue_tile(tiles, it);
-  cp_async_commit();
-  for (int k = 0; it < ntiles; it += gridDim.x, k++) {
-    float2* cur = tiles + (k & 1) * 16 * N;
-    const int nxt = it + gridDim.x;
-    if (nxt < ntiles) issue_tile(tiles + ((k + 1) & 1) * 16 * N, nxt);
-    cp_async_commit();
-    const int gl = it / tpf, ti = it - gl * tpf, x0 = ti * 16, x = x0 + warp;
-    float2* Wp = p.W + (size_t)gl * p.nx * N;
-    if (WHICH == 2 && threadIdx.x == 0) {
-      // every block of the field sums the partials in the same order: identical results
-      const float* part = p.red_part + (size_t)gl * tpf * 2;
-      float dn_sum = 0.f, u_sum = 0.f;
-      for (int i = 0; i < tpf; i++) {
-        dn_sum += part[2 * i];
-        u_sum += part[2 * i + 1];
-      }
-      const float dn0 = dn_sum / u_sum;  // mult_dn_mean_buff, bpm_3d_kernels.cl:117
-      s_n = p.n00f + dn0;                // mult_propagator_buff, bpm_3d_kernels.cl:482
-      if (ti == 0) p.dn0_field[gl] = dn0;
-    }
-    float dnv[WHICH == 1 ? PER : 1];
-    if (WHICH == 1) {
-      // dn slice 0 of this tile, fetched now so the loads overlap the transform
-#pragma unroll
-      for (int i = 0; i < PER; i++) {
-        const int e = threadIdx.x + i * T;
-        dnv[i] = p.dn ? load_dn_real(p.dn, p.dn_dtype, gl * p.dn_bstride + (size_t)(e >> 4) * p.nx + x0 + (e & 15))
-                      : 0.f;
-      }
-    }
-    cp_async_wait<1>();  // tile it
-    __syncthreads();
-    float2 v[E];
-#pragma unroll
-    for (int m = 0; m < E; m++) v[m] = cur[tile_idx(t + 32 * m, warp)];
-    if (WHICH != 2) warp_fft<N, false>(v, buf, tw, t);
-    if (WHICH != 1) {
-      const float n_eff = WHICH == 2 ? s_n : (p.prop_mode == 1 ? p.slice_n[p.z + 1] : p.n00f);
-      const float nk = prop_nk(p, n_eff);
-      const float2 plain = (p.scat && x == 0) ? plain_wave(p) : make_float2(0.f, 0.f);
-      float S = 0.f, G = 0.f;
-#pragma unroll
-      for (int m = 0; m < E; m++) v[m] = prop_point<true>(p, v[m], x, t + 32 * m, nk, plain, S, G, p.ky2);
-      if (p.scat) {
-        block_sum2<T>(S, G, red);
-        if (threadIdx.x == 0) {
-          float* o = p.scat_part + ((size_t)gl * tpf + ti) * 2;
-          o[0] = S;
-          o[1] = G;
-        }
-      }
-      warp_fft<N, true>(v, buf, tw, t);
-    }
-    // each warp writes back the column it read: no other warp touches those slots
-#pragma unroll
-    for (int m = 0; m < E; m++) cur[tile_idx(t + 32 * m, warp)] = v[m];
-    __syncthreads();
-    if (WHICH == 1) {
-      float sdn = 0.f, su = 0.f;
-#pragma unroll
-      for (int i = 0; i < PER; i++) {
-        const int e = threadIdx.x + i * T;
-        const int n = e >> 4, c = e & 15;
-        const float2 u = cur[tile_idx(n, c)];
-        Wp[(size_t)n * p.nx + x0 + c] = u;
-        const float a = __fsqrt_rn(cabs2(u));
-        su += a;
-        if (p.dn) sdn = fmaf(a, dnv[i], sdn);
-      }
-      block_sum2<T>(sdn, su, red);
-      if (threadIdx.x == 0) {
-        float* o = p.red_part + ((size_t)gl * tpf + ti) * 2;
-        o[0] = sdn;
-        o[1] = su;
-      }
-    } else {
-      col_store<N, T>(cur, Wp, p.nx, x0);
-    }
-    __syncthreads();  // cur is refilled by the next iteration's prefetch
-  }
-  cp_async_wait<0>();
-}
-
-// ---------------------------------------------------------------------------------------
 // Whole-march cluster kernel for square grids N = 64, 128, 256: one thread-block cluster of
-// C = N/32 blocks per field holds the field in distributed shared memory for all nz steps.
-// Block c owns rows [32c, 32c+32) (row slab R, 32 x N) and columns [32c, 32c+32) (column
-// slab K, N x 33 with one pad column). A step: cluster barrier (row slabs ready) -> every
-// block gathers its column slab from the other blocks' row slabs through DSMEM -> column
-// FFT, [weighted: per-16-column-tile partial sums, exchanged through DSMEM after a cluster
-// barrier], propagator, inverse column FFT -> cluster barrier (column slabs ready) -> every
-// block gathers its row slab back -> inverse row FFT, phase mask, plane output, forward row
-// FFT. The field never leaves the chip; one launch runs the whole march of every field of
-// the request. The FFTs, pointwise helpers and the weighted partial sums (same 16-column
-// tiles, same 512-thread element order, same fixed-order total) are those of the warp
-// kernels, so the results are the same bits. Cluster barriers are hardware barriers over
-// blocks the launch co-schedules; a final barrier keeps every block's shared memory alive
-// until the others have finished reading it.
+// C = N/16 blocks per field (16 at 256, a non-portable cluster size) holds the field in
+// distributed shared memory for all nz steps. Block c owns rows [16c, 16c+16) (row slab R,
+// 16 x N) and columns [16c, 16c+16) (column slab K, N x 17 with one pad column). A step:
+// cluster barrier (row slabs ready) -> every block gathers its column slab from the other
+// blocks' row slabs through DSMEM (all remote loads of a batch issued before any store) ->
+// column FFT, [weighted: per-16-column-tile partial sums, exchanged through DSMEM after a
+// cluster barrier], propagator (the block's table columns and ky^2 staged once) -> inverse
+// column FFT -> cluster barrier (column slabs ready) -> every block gathers its row slab back
+// -> inverse row FFT, phase mask (the next plane's mask rows prefetched by cp.async during
+// the column pass), plane output, forward row FFT. The field never leaves the chip; one
+// launch runs the whole march of every field of the request. The FFTs, pointwise helpers and
+// the weighted partial sums (same 16-column tiles, same 512-thread element order, same
+// fixed-order total) are those of the pass kernels, so the results are the same bits (at
+// 64, where the pass kernels use the tile FFT, the same to FP32 rounding). Cluster barriers
+// are hardware barriers over blocks the launch co-schedules; a final barrier keeps every
+// block's shared memory alive until the others have finished reading it.
 // ---------------------------------------------------------------------------------------
 constexpr int kClusterThreads = 512;  // 16 warps
 
@@ -1715,26 +1325,14 @@ __global__ void __launch_bounds__(kClusterThreads, 1) cluster_march_kernel(Clust
 template <template <int> class K>
 struct SizeDispatch;
 
-// Which row/column kernels a march uses for 128 <= N <= 512. The pipelined persistent
-// kernels hide each item's load latency behind the previous item but hold the whole device
-// at half the warps of the single-wave warp kernels, and their column pass keeps the tile
-// transposition that col_split_kernel drops. Measured on GB300 (512x512x256 weighted, one
-// group of B fields): B = 1 6.3 vs 6.1 ms, B = 2 6.6 vs 5.0, B = 8 11.9 vs 7.6 (pipelined vs
-// warp row + split column kernels; 256x256: equal at B = 1, 3.5 vs 2.6 ms at B = 2), and
-// concurrent groups favour the warp kernels further. So the warp kernels serve every march
-// and BPM_GB300_KERNELS=pipe selects the pipelined ones (=warp is the default). All compute
-// the same bits (explicit fmaf in all shared arithmetic), so a field's result does not
-// depend on the batch it marched in or the kernels that ran it.
-
-// column passes of 128..512 without scattering sums run col_split_kernel;
-// BPM_GB300_COLSPLIT=0 selects col_warp_kernel instead (the same bits)
-bool colsplit_enabled() {
-  static const bool on = [] {
-    const char* e = getenv("BPM_GB300_COLSPLIT");
-    return !(e && strcmp(e, "0") == 0);
-  }();
-  return on;
-}
+// Row and column kernels for 128 <= N <= 1024: warp-per-row kernels and the
+// transposition-free column kernel. A pipelined persistent family (each warp or block
+// walking a strided item list and prefetching the next item with cp.async) was measured
+// against them on GB300 (512x512x256 weighted, one group of B fields: B = 1 6.3 vs 6.1 ms,
+// B = 2 6.6 vs 5.0, B = 8 11.9 vs 7.6; concurrent groups favoured the warp kernels further)
+// and removed. Every kernel computes the same bits for a sequence whatever the launch shape
+// (explicit fmaf in all shared arithmetic), so a field's result does not depend on the
+// batch it marched in.
 
 // 1024-point rows and columns run the warp-FFT kernels (32 values per lane, one exchange
 // per transform); BPM_GB300_WARP1024=0 selects the shared-memory tile kernels instead
@@ -1742,14 +1340,6 @@ bool warp1024_enabled() {
   static const bool on = [] {
     const char* e = getenv("BPM_GB300_WARP1024");
     return !(e && strcmp(e, "0") == 0);
-  }();
-  return on;
-}
-
-bool pipe_enabled() {
-  static const bool on = [] {
-    const char* e = getenv("BPM_GB300_KERNELS");
-    return e && strcmp(e, "pipe") == 0;
   }();
   return on;
 }
@@ -1787,12 +1377,7 @@ inline int balanced_workers(int items, int cap) {
 template <int N>
 struct RowK {
   static constexpr bool WARP = N >= 128 && N <= 1024;  // warp-per-row kernels
-  static constexpr bool PIPE = N >= 128 && N <= 512;   // pipelined persistent kernels
   static constexpr bool TILE = !WARP || N == 1024;     // shared-memory tile kernels
-  static int& pipe_cap(int pre) {
-    static int cap[2] = {0, 0};
-    return cap[pre];
-  }
   static void prepare() {
     static bool attr = false;
     if (!attr) {
@@ -1801,14 +1386,6 @@ struct RowK {
                              (int)WarpCfg<N>::ROW_SMEM_SHARED);
         cudaFuncSetAttribute(row_shared_kernel<N, 1>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                              (int)WarpCfg<N>::ROW_SMEM_SHARED);
-        if constexpr (PIPE) {
-          cudaFuncSetAttribute(row_pipe_kernel<N, 0>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                               (int)PipeCfg<N>::ROW_SMEM);
-          cudaFuncSetAttribute(row_pipe_kernel<N, 1>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                               (int)PipeCfg<N>::ROW_SMEM);
-          pipe_cap(0) = resident_blocks(row_pipe_kernel<N, 0>, kRowWarps * 32, PipeCfg<N>::ROW_SMEM);
-          pipe_cap(1) = resident_blocks(row_pipe_kernel<N, 1>, kRowWarps * 32, PipeCfg<N>::ROW_SMEM);
-        }
         cudaFuncSetAttribute(row_warp_kernel<N, false, 0>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                              (int)WarpCfg<N>::ROW_SMEM);
         cudaFuncSetAttribute(row_warp_kernel<N, true, 0>, cudaFuncAttributeMaxDynamicSharedMemorySize,
@@ -1826,14 +1403,6 @@ struct RowK {
       }
       attr = true;
     }
-  }
-  // the pipelined kernel copies rows of src and of the mask (or dn) with 16-byte cp.async
-  static bool pipe_ok(const RowParams& p) {
-    if (!pipe_enabled() || !aligned16(p.src) || ((size_t)p.src_bstride * 8) % 16) return false;
-    if (!p.do_mask) return true;
-    if (p.mask) return aligned16(p.mask);
-    const int es = p.dn_dtype == BPM_DN_C64 ? 8 : (p.dn_dtype == BPM_DN_F16 ? 2 : 4);
-    return aligned16(p.dn) && ((size_t)p.dn_bstride * es) % 16 == 0;
   }
   // all fields of the group share the slice-z mask row: the precomputed mask, or one dn
   // volume (dn_batch_stride 0); the row is staged with 16-byte cp.async
@@ -1861,18 +1430,6 @@ struct RowK {
   }
   static int launch_warp(dim3 g, cudaStream_t s, const RowParams& p, bool adj) {
     if constexpr (WARP) {
-      if constexpr (PIPE) {
-        if (!adj && pipe_ok(p)) {
-          const int pre = p.mask ? 1 : 0;
-          const int nrows = (int)g.y * p.ny;
-          const int warps = balanced_workers(nrows, pipe_cap(pre) * kRowWarps);
-          const int blocks = (warps + kRowWarps - 1) / kRowWarps;
-          auto fn = pre ? row_pipe_kernel<N, 1> : row_pipe_kernel<N, 0>;
-          BPM_CUDA_TRY(launch_dep(fn, dim3(blocks), dim3(kRowWarps * 32), PipeCfg<N>::ROW_SMEM, s, p, nrows));
-          BPM_LAUNCH_CHECK("row_pipe_kernel");
-          return BPM_OK;
-        }
-      }
       if (!adj && shared_ok(p) && g.y >= 2) {
         // fields per block: the group split evenly over ceil(G / 8) blocks per row
         const int nb = ((int)g.y + kRowWarps - 1) / kRowWarps;
@@ -1907,20 +1464,15 @@ struct RowK {
 
 template <int N, int WHICH>
 struct ColK {
-  static constexpr bool WARP = N >= 128 && N <= 512;    // warp-per-column and pipelined kernels
   static constexpr bool SPLIT = N >= 128 && N <= 1024;  // col_split_kernel
+  static constexpr bool TILE = !SPLIT || N == 1024;     // shared-memory tile kernels
   static void (*fn())(ColParams) {
-    if constexpr (WARP) return col_warp_kernel<N, WHICH>;
-    return WHICH == 0 ? col_pass_kernel<N> : (WHICH == 1 ? col_fwd_reduce_kernel<N> : col_inv_kernel<N>);
+    if constexpr (TILE)
+      return WHICH == 0 ? col_pass_kernel<N> : (WHICH == 1 ? col_fwd_reduce_kernel<N> : col_inv_kernel<N>);
+    return nullptr;
   }
-  static constexpr int threads() { return WARP ? kColWarps * 32 : TileCfg<N>::THREADS; }
-  static constexpr size_t smem() {
-    return WARP ? (WHICH == 1 ? WarpCfg<N>::COL_SMEM_DN : WarpCfg<N>::COL_SMEM_KY) : TileCfg<N>::SMEM;
-  }
-  static int& pipe_cap() {
-    static int cap = 0;
-    return cap;
-  }
+  static constexpr int threads() { return TileCfg<N>::THREADS; }
+  static constexpr size_t smem() { return TileCfg<N>::SMEM; }
   static constexpr size_t split_smem() {
     return WHICH == 1 ? ColSplitCfg<N>::SMEM_DN : ColSplitCfg<N>::SMEM_KY;
   }
@@ -1928,42 +1480,39 @@ struct ColK {
   static void prepare() {
     static bool attr = false;
     if (!attr) {
-      cudaFuncSetAttribute(fn(), cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem());
-      if constexpr (WARP) {
-        cudaFuncSetAttribute(col_pipe_kernel<N, WHICH>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                             (int)PipeCfg<N>::COL_SMEM);
-        pipe_cap() = resident_blocks(col_pipe_kernel<N, WHICH>, kColWarps * 32, PipeCfg<N>::COL_SMEM);
-      }
+      if constexpr (TILE) cudaFuncSetAttribute(fn(), cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem());
       if constexpr (SPLIT) {
         cudaFuncSetAttribute(col_split_kernel<N, WHICH>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                              (int)split_smem());
         if constexpr (WHICH == 0)
           cudaFuncSetAttribute(col_split_kernel<N, 0, 8>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                (int)split8_smem());
+        if constexpr (WHICH != 1)
+          cudaFuncSetAttribute(col_split_kernel<N, WHICH, kColWarps, true>,
+                               cudaFuncAttributeMaxDynamicSharedMemorySize, (int)split_smem());
       }
       attr = true;
     }
   }
   static int launch(dim3 g, cudaStream_t s, const ColParams& p) {
     prepare();
-    if constexpr (WARP) {
-      if (pipe_enabled() && aligned16(p.W)) {
-        const int ntiles = (int)(g.x * g.y);
-        BPM_CUDA_TRY(launch_dep(col_pipe_kernel<N, WHICH>, dim3(balanced_workers(ntiles, pipe_cap())),
-                                dim3(kColWarps * 32), PipeCfg<N>::COL_SMEM, s, p, ntiles));
-        BPM_LAUNCH_CHECK("col_pipe_kernel");
-        return BPM_OK;
-      }
-    }
     if constexpr (SPLIT) {
-      if (!p.scat && colsplit_enabled() && (N <= 512 || warp1024_enabled())) {
+      if (N <= 512 || warp1024_enabled()) {
         // a non-weighted pass with fewer 16-column blocks than SMs runs 8-column blocks, so
         // twice as many SMs share it (the columns' arithmetic is the same); so does every
         // non-weighted 1024-point pass, whose 16-column blocks fill an SM alone
         if constexpr (WHICH == 0) {
-          if ((int)(g.x * g.y) < sm_count() || N > 512) {
+          if (!p.scat && ((int)(g.x * g.y) < sm_count() || N > 512)) {
             BPM_CUDA_TRY(launch_dep(col_split_kernel<N, 0, 8>, dim3(g.x * 2, g.y), dim3(8 * 32), split8_smem(),
                                     s, p));
+            BPM_LAUNCH_CHECK("col_split_kernel");
+            return BPM_OK;
+          }
+        }
+        if constexpr (WHICH != 1) {
+          if (p.scat) {
+            BPM_CUDA_TRY(launch_dep(col_split_kernel<N, WHICH, kColWarps, true>, g, dim3(kColWarps * 32),
+                                    split_smem(), s, p));
             BPM_LAUNCH_CHECK("col_split_kernel");
             return BPM_OK;
           }
@@ -1973,9 +1522,13 @@ struct ColK {
         return BPM_OK;
       }
     }
-    BPM_CUDA_TRY(launch_dep(fn(), g, dim3(threads()), smem(), s, p));
-    BPM_LAUNCH_CHECK("col_pass_kernel");
-    return BPM_OK;
+    if constexpr (TILE) {
+      BPM_CUDA_TRY(launch_dep(fn(), g, dim3(threads()), smem(), s, p));
+      BPM_LAUNCH_CHECK("col_pass_kernel");
+      return BPM_OK;
+    }
+    set_error("column pass: no kernel for this size");
+    return BPM_ERR_SHAPE;
   }
 };
 

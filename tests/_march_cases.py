@@ -1,6 +1,5 @@
-"""March cases shared by the kernel-path comparison tests, each run in a child process
-whose environment picks the kernels (BPM_GB300_KERNELS, BPM_GB300_COLSPLIT,
-BPM_GB300_CLUSTER).
+"""March cases for the tests that run them in child processes (cross-process determinism;
+the cluster kernel against the pass kernels, chosen by BPM_GB300_CLUSTER).
 
     python tests/_march_cases.py OUT.npz
 """
