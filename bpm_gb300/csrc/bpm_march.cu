@@ -56,7 +56,7 @@ struct bpm_plan {
   int device;
   float2* tw_x;     // W_nx^k
   float2* tw_y;     // W_ny^k
-  float2* wtw_x;    // stage-ordered twiddles of the warp FFT along x (128 <= nx <= 512)
+  float2* wtw_x;    // stage-ordered twiddles of the warp FFT along x (64 <= nx <= 1024)
   float2* wtw_y;    // ... along y
   float* kx2;       // (2.f*M_PI*FFTFREQ(i,nx,dx))^2, FP32 recipe
   float* ky2;
@@ -99,15 +99,16 @@ float fftfreq_f32(int i, int N, float d) {  // FFTFREQ, bpm_3d_kernels.cl:6
   return f;
 }
 
-// stage-ordered twiddle table of the warp FFT (layout documented at wtw_offset), FP64
-std::vector<float2> warp_twiddles(int N) {
-  std::vector<float2> w(wtw_size(N));
-  const int E = N / 32;
+// stage-ordered twiddle table of the warp FFT with L lanes per sequence (layout documented
+// at wtw_offset), FP64
+std::vector<float2> warp_twiddles(int N, int L = 32) {
+  std::vector<float2> w(wtw_size(N, L));
+  const int E = N / L;
   int ns = 1;
   while (ns < N) {
     const int rs = std::min(E, N / ns);
     if (ns > 1) {
-      const int off = wtw_offset(N, ns);
+      const int off = wtw_offset(N, ns, L);
       for (int r = 1; r < rs; r++)
         for (int jm = 0; jm < ns; jm++) {
           const double a = -2. * M_PI * (double)((long)jm * r * (N / (ns * rs))) / N;
@@ -663,47 +664,56 @@ col_inv_kernel(ColParams p) {
 }
 
 // ---------------------------------------------------------------------------------------
-// warp-per-sequence kernels (128 <= N <= 512): each warp transforms one row or one column
-// entirely in registers, exchanging only through its own shared-memory buffer
+// sequence-in-registers kernels (128 <= N <= 1024): L lanes (a warp, or a half-warp for
+// 512-point sequences) transform one row or one column entirely in registers, exchanging
+// only through the sequence's own shared-memory buffer
 // ---------------------------------------------------------------------------------------
 constexpr int kRowWarps = 8;   // rows per block
 constexpr int kColWarps = 16;  // columns per block (16 columns = one 128-byte segment per row)
 
-template <int N>
+template <int N, int L = 32>
 struct WarpCfg {
-  static constexpr size_t row_smem(int rw) { return ((size_t)N + (size_t)rw * WarpFft<N>::BUF) * sizeof(float2); }
+  static constexpr size_t row_smem(int rw) {
+    return ((size_t)N + (size_t)rw * WarpFft<N, L>::BUF) * sizeof(float2);
+  }
   static constexpr size_t ROW_SMEM = row_smem(kRowWarps);
   static constexpr size_t ROW_SMEM_SHARED = ROW_SMEM + (size_t)N * sizeof(float2);  // + the staged row
 };
 
-// Row pass, one warp per row: coalesced row load straight into registers, [inverse row
+// blocks per SM a row kernel of RW sequences of L lanes must fit: 32 values per lane need
+// up to 128 registers a thread, fewer 64 (85 for the on-the-fly mask)
+__host__ __device__ constexpr int row_min_blocks(int N, int L, int PRE, int RW) {
+  return N / L >= 32 ? 65536 / (128 * RW * L) : (PRE ? 4 : 3) * (kRowWarps / RW);
+}
+
+// Row pass, L lanes per row: coalesced row load straight into registers, [inverse row
 // FFT], pointwise work, [forward row FFT], coalesced store. No block-level barrier after
 // the twiddle table is loaded.
-template <int N, bool ADJ, int PRE, int RW = kRowWarps>
-__global__ void __launch_bounds__(RW * 32, (N > 512 ? 2 : (PRE ? 4 : 3)) * (kRowWarps / RW))
+template <int N, bool ADJ, int PRE, int RW = kRowWarps, int L = 32>
+__global__ void __launch_bounds__(RW * L, row_min_blocks(N, L, PRE, RW))
 row_warp_kernel(RowParams p) {
-  constexpr int E = N / 32;
-  constexpr int T = RW * 32;
+  constexpr int E = N / L;
+  constexpr int T = RW * L;
   extern __shared__ float2 smem[];
   float2* tw = smem;
-  const int warp = threadIdx.x >> 5, t = threadIdx.x & 31;
-  float2* buf = smem + N + warp * WarpFft<N>::BUF;
+  const int seq = threadIdx.x / L, t = threadIdx.x % L;
+  float2* buf = smem + N + seq * WarpFft<N, L>::BUF;
   const int gl = blockIdx.y;
-  const int y = blockIdx.x * RW + warp;
+  const int y = blockIdx.x * RW + seq;
   const size_t plane = (size_t)N * p.ny;
   // the twiddle table (a plan constant) is fetched before the wait for the previous pass;
   // the row loads go out before the barrier, so their latency overlaps the table's
   const bool fft = p.do_inv || p.do_fwd;
   if (fft)
-    for (int k = threadIdx.x; k < WarpFft<N>::TW; k += T) tw[k] = p.wtw[k];
+    for (int k = threadIdx.x; k < WarpFft<N, L>::TW; k += T) tw[k] = p.wtw[k];
   dep_wait();
   dep_release();
   float2 v[E];
   const float2* src = p.src + gl * p.src_bstride + (size_t)y * N;
 #pragma unroll
-  for (int m = 0; m < E; m++) v[m] = src[t + 32 * m];
+  for (int m = 0; m < E; m++) v[m] = src[t + L * m];
   if (fft) __syncthreads();
-  if (p.do_inv) warp_fft<N, true>(v, buf, tw, t);
+  if (p.do_inv) warp_fft<N, true, L>(v, buf, tw, t);
 
   const float dn0 = row_dn0(p, gl);
   const float2 rot = row_rot(p, dn0);
@@ -715,14 +725,14 @@ row_warp_kernel(RowParams p) {
     ckp = p.ckpt + ((size_t)gl * p.n_ckpt + p.z / p.ckpt_every) * plane;
 #pragma unroll
   for (int m = 0; m < E; m++)
-    v[m] = row_point<ADJ, PRE>(p, v[m], t + 32 * m, y, gl, plane, zoff, ooff, dn0, rot, last, ckp);
+    v[m] = row_point<ADJ, PRE>(p, v[m], t + L * m, y, gl, plane, zoff, ooff, dn0, rot, last, ckp);
   if (!ADJ && p.scat_p && blockIdx.x == 0 && threadIdx.x == 0) row_scatter_finish(p, gl);
 
   if (!p.do_fwd) return;
-  warp_fft<N, false>(v, buf, tw, t);
+  warp_fft<N, false, L>(v, buf, tw, t);
   float2* dst = p.W + gl * plane + (size_t)y * N;
 #pragma unroll
-  for (int m = 0; m < E; m++) dst[t + 32 * m] = v[m];
+  for (int m = 0; m < E; m++) dst[t + L * m] = v[m];
 }
 
 // the phase mask at (x, y) from the staged row: the precomputed mask or the dn value
@@ -739,28 +749,28 @@ __device__ __forceinline__ float2 staged_mask(const RowParams& p, const void* ml
 }
 
 // Forward row pass when the fields of the group share one mask (precomputed, or one dn
-// volume): block (y, b) takes row y of fields nw*b .. nw*b + nw-1, one field per warp (nw =
-// blockDim.x / 32 <= 8, chosen so no block holds idle warps' registers), so the mask row (or
-// dn row) of slice z is staged once per block into shared memory with cp.async at block
-// start and is ready when the warps finish their inverse row FFTs. The arithmetic is
-// row_warp_kernel's.
-template <int N, int PRE>
-__global__ void __launch_bounds__(kRowWarps * 32, N > 512 ? 2 : 4)
-row_shared_kernel(RowParams p, int nfields) {
-  constexpr int E = N / 32;
+// volume): block (y, b) takes row y of fields fw*b .. fw*b + fw-1, L lanes per field (fw <= 8,
+// chosen so no block holds idle sequences' registers; with half-warps an odd fw leaves one
+// idle slot), so the mask row (or dn row) of slice z is staged once per block into shared
+// memory with cp.async at block start and is ready when the sequences finish their inverse
+// row FFTs. The arithmetic is row_warp_kernel's.
+template <int N, int PRE, int L = 32>
+__global__ void __launch_bounds__(kRowWarps * 32, N / L >= 32 ? 2 : 4)
+row_shared_kernel(RowParams p, int nfields, int fw) {
+  constexpr int E = N / L;
   const int T = blockDim.x;
-  const int nw = T >> 5;
+  const int slots = T / L;
   extern __shared__ __align__(16) float2 smem[];
   float2* tw = smem;
-  const int warp = threadIdx.x >> 5, t = threadIdx.x & 31;
-  float2* buf = smem + N + warp * WarpFft<N>::BUF;
-  float2* mrow = smem + N + nw * WarpFft<N>::BUF;  // N float2: the staged mask or dn row
+  const int seq = threadIdx.x / L, t = threadIdx.x % L;
+  float2* buf = smem + N + seq * WarpFft<N, L>::BUF;
+  float2* mrow = smem + N + slots * WarpFft<N, L>::BUF;  // N float2: the staged mask or dn row
   const int y = blockIdx.x;
-  const int gl = blockIdx.y * nw + warp;
-  const bool active = gl < nfields;
+  const int gl = blockIdx.y * fw + seq;
+  const bool active = seq < fw && gl < nfields;
   const size_t plane = (size_t)N * p.ny;
   const size_t zoff = (size_t)p.z * plane;
-  for (int k = threadIdx.x; k < WarpFft<N>::TW; k += T) tw[k] = p.wtw[k];  // plan constant
+  for (int k = threadIdx.x; k < WarpFft<N, L>::TW; k += T) tw[k] = p.wtw[k];  // plan constant
   dep_wait();
   dep_release();
   {
@@ -775,10 +785,10 @@ row_shared_kernel(RowParams p, int nfields) {
   if (active) {
     const float2* src = p.src + gl * p.src_bstride + (size_t)y * N;
 #pragma unroll
-    for (int m = 0; m < E; m++) v[m] = src[t + 32 * m];
+    for (int m = 0; m < E; m++) v[m] = src[t + L * m];
   }
   __syncthreads();
-  if (active && p.do_inv) warp_fft<N, true>(v, buf, tw, t);
+  if (active && p.do_inv) warp_fft<N, true, L>(v, buf, tw, t);
   cp_async_wait<0>();
   __syncthreads();  // the staged row is visible to every warp
   if (!active) return;
@@ -791,7 +801,7 @@ row_shared_kernel(RowParams p, int nfields) {
   if (p.ckpt && p.z % p.ckpt_every == 0) ckp = p.ckpt + ((size_t)gl * p.n_ckpt + p.z / p.ckpt_every) * plane;
 #pragma unroll
   for (int m = 0; m < E; m++) {
-    const int x = t + 32 * m;
+    const int x = t + L * m;
     const size_t pix = (size_t)y * N + x;
     float2 u = cmul(v[m], staged_mask<PRE>(p, mrow, x, y));
     if (dn0 != 0.f) u = cmul(u, rot);
@@ -805,10 +815,10 @@ row_shared_kernel(RowParams p, int nfields) {
   }
   if (p.scat_p && y == 0 && t == 0) row_scatter_finish(p, gl);
   if (!p.do_fwd) return;
-  warp_fft<N, false>(v, buf, tw, t);
+  warp_fft<N, false, L>(v, buf, tw, t);
   float2* dst = p.W + gl * plane + (size_t)y * N;
 #pragma unroll
-  for (int m = 0; m < E; m++) dst[t + 32 * m] = v[m];
+  for (int m = 0; m < E; m++) dst[t + L * m] = v[m];
 }
 
 // Column pass without the tile transposition (128 <= N <= 512, no scattering sums). The
@@ -826,24 +836,25 @@ row_shared_kernel(RowParams p, int nfields) {
 // 16 columns on 16 different bank pairs; with 8 columns a half-warp spans two rows of 8
 // columns, conflict-free at N = 512 and 1024 for stride BUF + 2, 2-way on some accesses at
 // 128 and 256.
-template <int N, int C = kColWarps>
+template <int N, int C = kColWarps, int L = 32>
 struct ColSplitCfg {
-  static constexpr int STRIDE = (C == 8 && N >= 512) ? WarpFft<N>::BUF + 2 : (WarpFft<N>::BUF | 1);
-  static constexpr int TW_F2 = (WarpFft<N>::TW + 1) & ~1;
+  static constexpr int BUF = WarpFft<N, L>::BUF;
+  static constexpr int STRIDE = (C == 8 && N / L >= 16) ? BUF + 2 : (BUF | 1);
+  static constexpr int TW_F2 = (WarpFft<N, L>::TW + 1) & ~1;
   static constexpr int DN_F2 = (TW_F2 + C * STRIDE + 1) & ~1;  // 16-byte aligned
   static constexpr size_t SMEM = (size_t)DN_F2 * sizeof(float2);
   static constexpr size_t SMEM_DN = SMEM + (size_t)16 * N * sizeof(float);  // + dn slice 0 of the tile
   static constexpr size_t SMEM_KY = SMEM + (size_t)N * sizeof(float);       // + the ky^2 column
 };
 
-// the propagator on the thread's rows r0 + 32 i of column x (prop_point's arithmetic): the
+// the propagator on the thread's rows r0 + L i of column x (prop_point's arithmetic): the
 // row-major table H (conj(H) for the adjoint; TABLE) or the FP32 recipe with kx^2 of the
 // column and the ky^2 table staged in shared memory; with scattering sums
 // (bpm_3d.py:335-341) the thread's partials S, G over its rows
-template <int N, bool TABLE, bool SCAT>
-__device__ __forceinline__ void propagate_rows_t(const ColParams& p, float2 (&v)[N / 32], int x, int r0,
+template <int N, bool TABLE, bool SCAT, int L>
+__device__ __forceinline__ void propagate_rows_t(const ColParams& p, float2 (&v)[N / L], int x, int r0,
                                                  float n_eff, float kx2, const float* sky2, float& S, float& G) {
-  const unsigned step = 32u * (unsigned)p.nx;
+  const unsigned step = (unsigned)L * (unsigned)p.nx;
   const unsigned off = (unsigned)r0 * (unsigned)p.nx + (unsigned)x;
   const bool cj = p.conj_h;
   const float nkx = TABLE ? 0.f : __fsub_rn(prop_nk(p, n_eff), kx2);
@@ -853,7 +864,7 @@ __device__ __forceinline__ void propagate_rows_t(const ColParams& p, float2 (&v)
       h = __ldg(p.H + off + i * step);
       if (cj) h.y = -h.y;
     } else {
-      const float tmp = __fsub_rn(nkx, sky2[r0 + 32 * i]);
+      const float tmp = __fsub_rn(nkx, sky2[r0 + L * i]);
       h = make_float2(0.f, 0.f);
       if (tmp >= 0.f) {
         const float ph = __fmul_rn(-p.dzf, __fsqrt_rn(tmp));
@@ -864,12 +875,12 @@ __device__ __forceinline__ void propagate_rows_t(const ColParams& p, float2 (&v)
   };
   if constexpr (!SCAT) {
 #pragma unroll
-    for (int i = 0; i < N / 32; i++) v[i] = cscale(cmul(v[i], hval(i)), p.scale);
+    for (int i = 0; i < N / L; i++) v[i] = cscale(cmul(v[i], hval(i)), p.scale);
     return;
   }
   const float2 plain = (x == 0 && r0 == 0) ? plain_wave(p) : make_float2(0.f, 0.f);
 #pragma unroll
-  for (int i = 0; i < N / 32; i++) {
+  for (int i = 0; i < N / L; i++) {
     const float2 u = cmul(v[i], hval(i));
     float2 d = u;
     if (x == 0 && r0 == 0 && i == 0) d = csub(d, plain);
@@ -879,21 +890,26 @@ __device__ __forceinline__ void propagate_rows_t(const ColParams& p, float2 (&v)
     v[i] = cscale(u, p.scale);
   }
 }
-template <int N, bool SCAT>
-__device__ __forceinline__ void propagate_rows(const ColParams& p, float2 (&v)[N / 32], int x, int r0,
+template <int N, bool SCAT, int L>
+__device__ __forceinline__ void propagate_rows(const ColParams& p, float2 (&v)[N / L], int x, int r0,
                                                float n_eff, float kx2, const float* sky2, float& S, float& G) {
   if (p.prop_mode == 0)
-    propagate_rows_t<N, true, SCAT>(p, v, x, r0, n_eff, kx2, sky2, S, G);
+    propagate_rows_t<N, true, SCAT, L>(p, v, x, r0, n_eff, kx2, sky2, S, G);
   else
-    propagate_rows_t<N, false, SCAT>(p, v, x, r0, n_eff, kx2, sky2, S, G);
+    propagate_rows_t<N, false, SCAT, L>(p, v, x, r0, n_eff, kx2, sky2, S, G);
 }
 
-template <int N, int WHICH, int C = kColWarps, bool SCAT = false>
-__global__ void __launch_bounds__(C * 32, (C == 16 ? 2 : 4) / (N > 512 ? 2 : 1))
+// blocks per SM a column kernel of C columns x L threads must fit (registers as row_min_blocks)
+__host__ __device__ constexpr int col_min_blocks(int N, int L, int C) {
+  return 65536 / ((N / L >= 32 ? 128 : 64) * C * L);
+}
+
+template <int N, int WHICH, int C = kColWarps, bool SCAT = false, int L = 32>
+__global__ void __launch_bounds__(C * L, col_min_blocks(N, L, C))
 col_split_kernel(ColParams p) {
-  using Cfg = ColSplitCfg<N, C>;
-  constexpr int E = N / 32;
-  constexpr int T = C * 32;
+  using Cfg = ColSplitCfg<N, C, L>;
+  constexpr int E = N / L;
+  constexpr int T = C * L;
   static_assert(C == 16 || (C == 8 && WHICH == 0), "weighted passes keep 16-column blocks");
   static_assert(!SCAT || (C == 16 && WHICH != 1), "scattering partials per 16-column tile");
   extern __shared__ __align__(16) float2 smem[];
@@ -906,19 +922,20 @@ col_split_kernel(ColParams p) {
   const int gl = blockIdx.y;
   const int x0 = blockIdx.x * C;
   float2* Wp = p.W + (size_t)gl * p.nx * N;
-  const unsigned gstep = 32u * (unsigned)p.nx;
-  float2* colbuf = bufs + cc * Cfg::STRIDE;    // column x0 + cc: the tile-mapping stages
-  float2* wbuf = bufs + warp * Cfg::STRIDE;    // column x0 + warp: the middle stages
+  const unsigned gstep = (unsigned)L * (unsigned)p.nx;
+  float2* colbuf = bufs + cc * Cfg::STRIDE;                 // column x0 + cc: the tile-mapping stages
+  float2* wbuf = bufs + (threadIdx.x / L) * Cfg::STRIDE;    // column x0 + tid/L: the middle stages
+  const int wt = threadIdx.x % L;
   // plan constants before the wait for the previous pass: the twiddles, and for the FP32
   // recipe kx^2 of the thread's column and one ky^2 entry per thread (staged after it, in the
   // region the weighted reduction uses for dn)
-  constexpr int TWR = (WarpFft<N>::TW + T - 1) / T;  // twiddles per thread (1, or 2 with 8 columns)
+  constexpr int TWR = (WarpFft<N, L>::TW + T - 1) / T;  // twiddles per thread
   constexpr int KYR = (N + T - 1) / T;                // ky^2 entries per thread
   float2 twv[TWR];
 #pragma unroll
   for (int k = 0; k < TWR; k++) {
     const int i = threadIdx.x + k * T;
-    twv[k] = i < WarpFft<N>::TW ? p.wtw[i] : make_float2(0.f, 0.f);
+    twv[k] = i < WarpFft<N, L>::TW ? p.wtw[i] : make_float2(0.f, 0.f);
   }
   const bool recipe = WHICH != 1 && p.prop_mode != 0;
   const float kx2v = recipe ? __ldg(p.kx2 + x0 + cc) : 0.f;
@@ -971,35 +988,35 @@ col_split_kernel(ColParams p) {
   }
 #pragma unroll
   for (int k = 0; k < TWR; k++)
-    if (threadIdx.x + k * T < WarpFft<N>::TW) tw[threadIdx.x + k * T] = twv[k];
+    if (threadIdx.x + k * T < WarpFft<N, L>::TW) tw[threadIdx.x + k * T] = twv[k];
 #pragma unroll
   for (int k = 0; k < KYR; k++)
     if (recipe && threadIdx.x + k * T < N) sky2[threadIdx.x + k * T] = kyv[k];
   float S = 0.f, G = 0.f;  // scattering partials
   if (WHICH == 2) {
     __syncthreads();  // s_n, ky^2
-    propagate_rows<N, SCAT>(p, v, x0 + cc, r0, s_n, kx2v, sky2, S, G);
+    propagate_rows<N, SCAT, L>(p, v, x0 + cc, r0, s_n, kx2v, sky2, S, G);
   } else {
     // forward column FFT
-    colsplit_first<N, false>(v, colbuf, r0);
+    colsplit_first<N, false, L>(v, colbuf, r0);
     __syncthreads();
-    colsplit_middle<N, false>(wbuf, tw, t);
+    colsplit_middle<N, false, L>(wbuf, tw, wt);
     __syncthreads();
-    colsplit_last<N, false>(v, colbuf, tw, r0);
+    colsplit_last<N, false, L>(v, colbuf, tw, r0);
   }
   if (WHICH == 0) {
-    propagate_rows<N, SCAT>(p, v, x0 + cc, r0, p.prop_mode == 1 ? p.slice_n[p.z + 1] : p.n00f, kx2v, sky2, S,
-                            G);
+    propagate_rows<N, SCAT, L>(p, v, x0 + cc, r0, p.prop_mode == 1 ? p.slice_n[p.z + 1] : p.n00f, kx2v, sky2,
+                               S, G);
     __syncthreads();  // every thread has read its last-stage inputs before the buffers are reused
   }
   if (WHICH != 1) {
     if constexpr (SCAT) scat_partials_store<T>(p, S, G, gl, red);
     // inverse column FFT, then the coalesced store
-    colsplit_first<N, true>(v, colbuf, r0);
+    colsplit_first<N, true, L>(v, colbuf, r0);
     __syncthreads();
-    colsplit_middle<N, true>(wbuf, tw, t);
+    colsplit_middle<N, true, L>(wbuf, tw, wt);
     __syncthreads();
-    colsplit_last<N, true>(v, colbuf, tw, r0);
+    colsplit_last<N, true, L>(v, colbuf, tw, r0);
     const unsigned gofs = (unsigned)r0 * (unsigned)p.nx + (unsigned)(x0 + cc);
 #pragma unroll
     for (int i = 0; i < E; i++) Wp[gofs + i * gstep] = v[i];
@@ -1376,24 +1393,29 @@ inline int balanced_workers(int items, int cap) {
 
 template <int N>
 struct RowK {
-  static constexpr bool WARP = N >= 128 && N <= 1024;  // warp-per-row kernels
+  static constexpr bool WARP = N >= 128 && N <= 1024;  // sequence-in-registers kernels
   static constexpr bool TILE = !WARP || N == 1024;     // shared-memory tile kernels
+  template <int L>
+  static void prepare_l() {
+    using W = WarpCfg<N, L>;
+    cudaFuncSetAttribute(row_shared_kernel<N, 0, L>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                         (int)W::ROW_SMEM_SHARED);
+    cudaFuncSetAttribute(row_shared_kernel<N, 1, L>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                         (int)W::ROW_SMEM_SHARED);
+    cudaFuncSetAttribute(row_warp_kernel<N, false, 0, kRowWarps, L>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                         (int)W::ROW_SMEM);
+    cudaFuncSetAttribute(row_warp_kernel<N, true, 0, kRowWarps, L>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                         (int)W::ROW_SMEM);
+    cudaFuncSetAttribute(row_warp_kernel<N, false, 1, kRowWarps, L>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                         (int)W::ROW_SMEM);
+    cudaFuncSetAttribute(row_warp_kernel<N, true, 1, kRowWarps, L>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                         (int)W::ROW_SMEM);
+  }
   static void prepare() {
     static bool attr = false;
     if (!attr) {
       if constexpr (WARP) {
-        cudaFuncSetAttribute(row_shared_kernel<N, 0>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                             (int)WarpCfg<N>::ROW_SMEM_SHARED);
-        cudaFuncSetAttribute(row_shared_kernel<N, 1>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                             (int)WarpCfg<N>::ROW_SMEM_SHARED);
-        cudaFuncSetAttribute(row_warp_kernel<N, false, 0>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                             (int)WarpCfg<N>::ROW_SMEM);
-        cudaFuncSetAttribute(row_warp_kernel<N, true, 0>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                             (int)WarpCfg<N>::ROW_SMEM);
-        cudaFuncSetAttribute(row_warp_kernel<N, false, 1>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                             (int)WarpCfg<N>::ROW_SMEM);
-        cudaFuncSetAttribute(row_warp_kernel<N, true, 1>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                             (int)WarpCfg<N>::ROW_SMEM);
+        prepare_l<32>();
       }
       if constexpr (TILE) {
         cudaFuncSetAttribute(row_pass_kernel<N, false>, cudaFuncAttributeMaxDynamicSharedMemorySize,
@@ -1411,11 +1433,13 @@ struct RowK {
     if (p.mask) return aligned16(p.mask);
     return p.dn_bstride == 0 && aligned16(p.dn);
   }
-  // g.x counts 16-row tiles; the warp kernel covers kRowWarps rows per block
+  // g.x counts 16-row tiles
   static int launch(dim3 g, cudaStream_t s, const RowParams& p, bool adj) {
     prepare();
     if constexpr (WARP) {
-      if (N <= 512 || warp1024_enabled()) return launch_warp(g, s, p, adj);
+      if (N <= 512 || warp1024_enabled()) {
+        return launch_warp<32>(g, s, p, adj);
+      }
     }
     if constexpr (TILE) {
       if (adj)
@@ -1428,15 +1452,18 @@ struct RowK {
     set_error("row pass: no kernel for this size");
     return BPM_ERR_SHAPE;
   }
+  template <int L>
   static int launch_warp(dim3 g, cudaStream_t s, const RowParams& p, bool adj) {
     if constexpr (WARP) {
+      constexpr int BUF = WarpFft<N, L>::BUF;
       if (!adj && shared_ok(p) && g.y >= 2) {
         // fields per block: the group split evenly over ceil(G / 8) blocks per row
         const int nb = ((int)g.y + kRowWarps - 1) / kRowWarps;
         const int fw = ((int)g.y + nb - 1) / nb;
-        const size_t sm = ((size_t)2 * N + (size_t)fw * WarpFft<N>::BUF) * sizeof(float2);
-        auto fn = p.mask ? row_shared_kernel<N, 1> : row_shared_kernel<N, 0>;
-        BPM_CUDA_TRY(launch_dep(fn, dim3(p.ny, nb), dim3(fw * 32), sm, s, p, (int)g.y));
+        const int threads = (fw * L + 31) / 32 * 32;
+        const size_t sm = ((size_t)2 * N + (size_t)(threads / L) * BUF) * sizeof(float2);
+        auto fn = p.mask ? row_shared_kernel<N, 1, L> : row_shared_kernel<N, 0, L>;
+        BPM_CUDA_TRY(launch_dep(fn, dim3(p.ny, nb), dim3(threads), sm, s, p, (int)g.y, fw));
         BPM_LAUNCH_CHECK("row_shared_kernel");
         return BPM_OK;
       }
@@ -1445,16 +1472,16 @@ struct RowK {
       const int rows = (int)(g.x * 16) * (int)g.y;
       if (rows / kRowWarps < 2 * sm_count()) {
         const dim3 gw(g.x * 16 / 2, g.y);
-        auto fn = adj ? (p.mask ? row_warp_kernel<N, true, 1, 2> : row_warp_kernel<N, true, 0, 2>)
-                      : (p.mask ? row_warp_kernel<N, false, 1, 2> : row_warp_kernel<N, false, 0, 2>);
-        BPM_CUDA_TRY(launch_dep(fn, gw, dim3(2 * 32), WarpCfg<N>::row_smem(2), s, p));
+        auto fn = adj ? (p.mask ? row_warp_kernel<N, true, 1, 2, L> : row_warp_kernel<N, true, 0, 2, L>)
+                      : (p.mask ? row_warp_kernel<N, false, 1, 2, L> : row_warp_kernel<N, false, 0, 2, L>);
+        BPM_CUDA_TRY(launch_dep(fn, gw, dim3(2 * L), WarpCfg<N, L>::row_smem(2), s, p));
         BPM_LAUNCH_CHECK("row_warp_kernel");
         return BPM_OK;
       }
       const dim3 gw(g.x * 16 / kRowWarps, g.y);
-      auto fn = adj ? (p.mask ? row_warp_kernel<N, true, 1> : row_warp_kernel<N, true, 0>)
-                    : (p.mask ? row_warp_kernel<N, false, 1> : row_warp_kernel<N, false, 0>);
-      BPM_CUDA_TRY(launch_dep(fn, gw, dim3(kRowWarps * 32), WarpCfg<N>::ROW_SMEM, s, p));
+      auto fn = adj ? (p.mask ? row_warp_kernel<N, true, 1, kRowWarps, L> : row_warp_kernel<N, true, 0, kRowWarps, L>)
+                    : (p.mask ? row_warp_kernel<N, false, 1, kRowWarps, L> : row_warp_kernel<N, false, 0, kRowWarps, L>);
+      BPM_CUDA_TRY(launch_dep(fn, gw, dim3(kRowWarps * L), WarpCfg<N, L>::ROW_SMEM, s, p));
       BPM_LAUNCH_CHECK("row_warp_kernel");
       return BPM_OK;
     }
@@ -1473,53 +1500,62 @@ struct ColK {
   }
   static constexpr int threads() { return TileCfg<N>::THREADS; }
   static constexpr size_t smem() { return TileCfg<N>::SMEM; }
+  template <int L>
   static constexpr size_t split_smem() {
-    return WHICH == 1 ? ColSplitCfg<N>::SMEM_DN : ColSplitCfg<N>::SMEM_KY;
+    return WHICH == 1 ? ColSplitCfg<N, kColWarps, L>::SMEM_DN : ColSplitCfg<N, kColWarps, L>::SMEM_KY;
   }
-  static constexpr size_t split8_smem() { return ColSplitCfg<N, 8>::SMEM_KY; }
+  template <int L>
+  static constexpr size_t split8_smem() { return ColSplitCfg<N, 8, L>::SMEM_KY; }
+  template <int L>
+  static void prepare_l() {
+    cudaFuncSetAttribute(col_split_kernel<N, WHICH, kColWarps, false, L>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                         (int)split_smem<L>());
+    if constexpr (WHICH == 0)
+      cudaFuncSetAttribute(col_split_kernel<N, 0, 8, false, L>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                           (int)split8_smem<L>());
+    if constexpr (WHICH != 1)
+      cudaFuncSetAttribute(col_split_kernel<N, WHICH, kColWarps, true, L>,
+                           cudaFuncAttributeMaxDynamicSharedMemorySize, (int)split_smem<L>());
+  }
   static void prepare() {
     static bool attr = false;
     if (!attr) {
       if constexpr (TILE) cudaFuncSetAttribute(fn(), cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem());
-      if constexpr (SPLIT) {
-        cudaFuncSetAttribute(col_split_kernel<N, WHICH>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                             (int)split_smem());
-        if constexpr (WHICH == 0)
-          cudaFuncSetAttribute(col_split_kernel<N, 0, 8>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                               (int)split8_smem());
-        if constexpr (WHICH != 1)
-          cudaFuncSetAttribute(col_split_kernel<N, WHICH, kColWarps, true>,
-                               cudaFuncAttributeMaxDynamicSharedMemorySize, (int)split_smem());
-      }
+      if constexpr (SPLIT) prepare_l<32>();
       attr = true;
     }
+  }
+  template <int L>
+  static int launch_split(dim3 g, cudaStream_t s, const ColParams& p) {
+    // a non-weighted pass with fewer 16-column blocks than SMs runs 8-column blocks, so twice
+    // as many SMs share it (the columns' arithmetic is the same); so does every non-weighted
+    // pass with 32 values per thread, whose 16-column blocks take half an SM's registers
+    if constexpr (WHICH == 0) {
+      if (!p.scat && ((int)(g.x * g.y) < sm_count() || N / L >= 32)) {
+        BPM_CUDA_TRY(launch_dep(col_split_kernel<N, 0, 8, false, L>, dim3(g.x * 2, g.y), dim3(8 * L),
+                                split8_smem<L>(), s, p));
+        BPM_LAUNCH_CHECK("col_split_kernel");
+        return BPM_OK;
+      }
+    }
+    if constexpr (WHICH != 1) {
+      if (p.scat) {
+        BPM_CUDA_TRY(launch_dep(col_split_kernel<N, WHICH, kColWarps, true, L>, g, dim3(kColWarps * L),
+                                split_smem<L>(), s, p));
+        BPM_LAUNCH_CHECK("col_split_kernel");
+        return BPM_OK;
+      }
+    }
+    BPM_CUDA_TRY(launch_dep(col_split_kernel<N, WHICH, kColWarps, false, L>, g, dim3(kColWarps * L),
+                            split_smem<L>(), s, p));
+    BPM_LAUNCH_CHECK("col_split_kernel");
+    return BPM_OK;
   }
   static int launch(dim3 g, cudaStream_t s, const ColParams& p) {
     prepare();
     if constexpr (SPLIT) {
       if (N <= 512 || warp1024_enabled()) {
-        // a non-weighted pass with fewer 16-column blocks than SMs runs 8-column blocks, so
-        // twice as many SMs share it (the columns' arithmetic is the same); so does every
-        // non-weighted 1024-point pass, whose 16-column blocks fill an SM alone
-        if constexpr (WHICH == 0) {
-          if (!p.scat && ((int)(g.x * g.y) < sm_count() || N > 512)) {
-            BPM_CUDA_TRY(launch_dep(col_split_kernel<N, 0, 8>, dim3(g.x * 2, g.y), dim3(8 * 32), split8_smem(),
-                                    s, p));
-            BPM_LAUNCH_CHECK("col_split_kernel");
-            return BPM_OK;
-          }
-        }
-        if constexpr (WHICH != 1) {
-          if (p.scat) {
-            BPM_CUDA_TRY(launch_dep(col_split_kernel<N, WHICH, kColWarps, true>, g, dim3(kColWarps * 32),
-                                    split_smem(), s, p));
-            BPM_LAUNCH_CHECK("col_split_kernel");
-            return BPM_OK;
-          }
-        }
-        BPM_CUDA_TRY(launch_dep(col_split_kernel<N, WHICH>, g, dim3(kColWarps * 32), split_smem(), s, p));
-        BPM_LAUNCH_CHECK("col_split_kernel");
-        return BPM_OK;
+        return launch_split<32>(g, s, p);
       }
     }
     if constexpr (TILE) {
