@@ -331,7 +331,7 @@ def bench_ours(args, rank, world, local_rank):
     return res
 
 
-def psf_timing(reps=3):
+def psf_timing(reps=3, cpu=False):
     """Config 2's vectorial Debye-Wolf PSF: 256^3, NA 1.1, n0 1.33, lambda 0.5, x-polarised,
     512 quadrature steps (513 nodes), all four output volumes on the device. The
     quadrature (debye_accum_kernel) executes 12 flops per octant voxel per node."""
@@ -351,10 +351,31 @@ def psf_timing(reps=3):
     octant = 129 ** 3
     flops = octant * 513 * 12
     out_bytes = 256 ** 3 * 28
-    return {"workload": "vectorial PSF 256^3, NA 1.1, n0 1.33, 513 nodes, u+ex+ey+ez",
-            "ms": t, "voxels_per_s": 256 ** 3 / (t * 1e-3),
-            "quadrature_tflops": flops / (t * 1e-3) / 1e12, "quadrature_flops": flops,
-            "output_gbs": out_bytes / (t * 1e-3) / 1e9}
+    res = {"workload": "vectorial PSF 256^3, NA 1.1, n0 1.33, 513 nodes, u+ex+ey+ez",
+           "ms": t, "voxels_per_s": 256 ** 3 / (t * 1e-3),
+           "quadrature_tflops": flops / (t * 1e-3) / 1e12, "quadrature_flops": flops,
+           "output_gbs": out_bytes / (t * 1e-3) / 1e9}
+    if cpu:
+        res["cpu_baseline"] = psf_cpu_sample(shape, units)
+    return res
+
+
+def psf_cpu_sample(shape, units, rows=16):
+    """The oracle's FP64 restatement of debye_wolf (numpy/scipy, factorised like the GPU
+    pipeline: node x radius Bessel tables times node x plane phases) on the first `rows` of
+    the octant's y rows, scaled to the full octant; output voxels/s of the full volume
+    (the mirroring into it excluded)."""
+    from oracle import debye_ref
+    prm = debye_ref.octant_params(shape, units, .5, 1.1, 1.33)
+    ny = prm["Ny"]
+    sub = dict(prm, Ny=rows, y2=np.float32(float(prm["y2"]) * (rows - 1) / (ny - 1)))
+    t0 = time.perf_counter()
+    debye_ref.debye_octant(sub, 512)
+    t = (time.perf_counter() - t0) * ny / rows
+    nvox = shape[0] * shape[1] * shape[2]
+    return {"value": nvox / t, "unit": "voxels/s", "cores": host_cores(), "kind": "port",
+            "sample": "octant rows 0..%d of %d (%d x %d x %d octant points, 513 nodes), %.1f s scaled to %.1f s" % (
+                rows - 1, ny, prm["Nx"], rows, prm["Nz"], t * rows / ny, t)}
 
 
 def single_request_timing(reps=5):
@@ -499,6 +520,61 @@ def serve_trace(n=2000, rate=200., seed=0):
             "wall_s": wall, "voxel_updates_per_s": st["voxel_updates"] / wall, "requests_per_s": n / wall,
             "peak_hbm_gb": st["peak_hbm_bytes"] / 1e9, "budget_gb": st["budget_bytes"] / 1e9,
             "workload": "config-5 trace, seeded Poisson arrivals, all requests latency-measured"}
+
+
+def mixed_batch_timing(n=48, seed=5):
+    """Config 3's second batch, the uneven-size path: n plane-wave requests over grids 128^2,
+    256^2 and 512^2 with Nz in {64, 128, 256} (weighted mean mode, one shared resident dn
+    volume per grid, |u|^2 volume kept on the device), submitted at once to the serving
+    loop, which merges same-grid requests into batched launches and overlaps the grids on
+    separate streams; against the same requests one after the other through bpm_3d."""
+    import torch
+    import bpm_gb300
+    from bpm_gb300.serve import BpmRequest, Server
+    rng = np.random.default_rng(seed)
+    dns = {side: make_dn_device(side, side, 256, seed + side) for side in (128, 256, 512)}
+    reqs = []
+    for i in range(n):
+        side = (128, 256, 512)[i % 3]
+        nz = int(rng.choice([64, 128, 256]))
+        u0 = torch.from_numpy(make_u0(1, side, side, seed + i)[0]).cuda()
+        reqs.append((side, nz, u0))
+    vu = sum(side * side * (nz - 1) for side, nz, _ in reqs)
+
+    def alone(side, nz, u0):
+        return bpm_gb300.bpm_3d((side, side, nz), UNITS, lam=LAM, n0=N0, u0=u0, dn=dns[side][:nz],
+                                return_field=False)
+
+    for key in sorted({(side, nz) for side, nz, _ in reqs}):   # plans and kernels, untimed
+        alone(key[0], key[1], next(u for sd, z, u in reqs if (sd, z) == key))
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    ref = [alone(*r) for r in reqs]
+    torch.cuda.synchronize()
+    t_seq = time.perf_counter() - t0
+
+    def served():
+        srv = Server(max_inflight=8, max_batch=16)
+        t1 = time.perf_counter()
+        futs = [srv.submit(BpmRequest((side, side, nz), UNITS, lam=LAM, n0=N0, u0=u0, dn=dns[side][:nz],
+                                      return_field=False)) for side, nz, u0 in reqs]
+        out = [f.result() for f in futs]
+        torch.cuda.synchronize()
+        t = time.perf_counter() - t1
+        srv.close(wait=True)
+        return out, t, srv.stats()
+
+    served()                                                    # warm-up of the serving path
+    out, t_mix, st = served()
+    same = all(bool(torch.equal(out[i], ref[i])) for i in range(0, n, 7))
+    del dns, reqs, ref, out
+    torch.cuda.empty_cache()
+    return {"requests": n, "grids": "128^2, 256^2, 512^2; Nz in {64, 128, 256}; weighted; shared dn per grid",
+            "voxel_updates": vu, "mixed_ms": t_mix * 1e3, "mixed_voxel_updates_per_s": vu / t_mix,
+            "sequential_ms": t_seq * 1e3, "sequential_voxel_updates_per_s": vu / t_seq,
+            "speedup": t_seq / t_mix, "p50_ms": st["p50_ms"], "p99_ms": st["p99_ms"],
+            "same_result_as_alone": same,
+            "api": "bpm_gb300.serve.Server (all submitted at once) vs bpm_gb300.bpm_3d per request"}
 
 
 def config1_dn(n=128):
@@ -664,7 +740,8 @@ def main():
     if rank == 0:
         if not args.no_serve:
             res["serve"] = serve_trace()
-        res["psf"] = psf_timing()
+        res["psf"] = psf_timing(cpu=not args.no_cpu_baseline)
+        res["mixed_batch"] = mixed_batch_timing()
         res["single_requests"] = single_request_timing()
         res["adjoint"] = adjoint_timing()
         if not args.no_cpu_baseline:

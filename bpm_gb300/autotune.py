@@ -5,8 +5,9 @@ time on separate streams (see bpm_workspace_bytes in include/bpm_gb300.h). The b
 depends on the grid, the batch, the mean mode and the device: larger groups fill more of
 the GPU per launch, smaller ones keep every concurrent group's planes inside L2. The tuner
 times a short probe march (the same kernels on the first few dn slices, captured as a CUDA
-graph) for each candidate group and keeps the fastest; results are cached per device and
-shape in a JSON file (BPM_GB300_TUNE_CACHE, default ~/.cache/bpm_gb300/autotune.json).
+graph) for each candidate group, best of three trials, and keeps the largest group within
+3 % of the fastest (pick_group); results are cached per device and shape in a JSON file
+(BPM_GB300_TUNE_CACHE, default ~/.cache/bpm_gb300/autotune.json).
 """
 import json
 import os
@@ -15,7 +16,7 @@ import torch
 
 from . import _native as N
 
-__all__ = ["tune_group", "cache_path"]
+__all__ = ["tune_group", "pick_group", "cache_path"]
 
 _cache = None
 
@@ -53,8 +54,16 @@ def _candidates(batch):
     return sorted(c)
 
 
+def pick_group(times, tol=.03):
+    """The largest group whose probe time is within `tol` of the fastest: near-equal
+    candidates differ by noise, and a larger group launches fewer kernels and reads a shared
+    mask once for more fields."""
+    tmin = min(times.values())
+    return max(g for g, t in times.items() if t <= (1. + tol) * tmin)
+
+
 def tune_group(size, units, lam, n0, batch, dn, mean_mode="weighted", out_kind="intensity",
-               absorbing_width=0, nz_probe=12, reps=3, force=False):
+               absorbing_width=0, nz_probe=12, reps=3, trials=3, force=False):
     """Fields per launch that march `batch` fields of grid `size` fastest on this device.
     dn: the (Nz, Ny, Nx) volume of the real run (its first slices drive the probe)."""
     from .bpm3d import BatchedMarch, _dn_kind
@@ -75,14 +84,17 @@ def tune_group(size, units, lam, n0, batch, dn, mean_mode="weighted", out_kind="
         m.run()
         torch.cuda.synchronize()
         a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-        a.record()
-        for _ in range(reps):
-            m.run()
-        b.record()
-        torch.cuda.synchronize()
-        times[g] = a.elapsed_time(b) / reps
+        t = float("inf")
+        for _ in range(trials):  # best of several short trials: robust to a stray slow one
+            a.record()
+            for _ in range(reps):
+                m.run()
+            b.record()
+            torch.cuda.synchronize()
+            t = min(t, a.elapsed_time(b) / reps)
+        times[g] = t
         del m
-    best = min(times, key=times.get)
+    best = pick_group(times)
     cache[key] = {"group": int(best), "ms_probe": times, "nz_probe": nzp}
     _save()
     return int(best)

@@ -91,3 +91,12 @@ def test_null_plan_calls(native):
     assert L.bpm_propagate(None, None, None, 0, None) == native.BPM_ERR_ARG
     assert L.bpm_plan_destroy(None) == 0
     assert L.bpm_exec_destroy(None) == 0
+
+
+def test_autotune_pick_group():
+    """The tuner keeps the largest group within 3 % of the fastest probe time."""
+    from bpm_gb300.autotune import pick_group
+    assert pick_group({1: 10., 2: 8., 4: 7.9, 8: 7.95, 16: 9.}) == 8
+    assert pick_group({4: 7.0, 8: 7.5, 16: 7.6}) == 4
+    assert pick_group({8: 5.}) == 8
+    assert pick_group({2: 3., 4: 3.09}, tol=.03) == 4
