@@ -188,9 +188,19 @@ def _slice_tables(dn, n0, dev):
             torch.from_numpy(np.ascontiguousarray(sd, np.float32)).to(dev))
 
 
+def mask_pays(batch, Nx, Ny):
+    """Whether a march of `batch` fields through one shared dn volume computes its phase
+    masks once up front (precompute_mask) instead of per element in every row pass. The
+    results are the same bits either way. It pays for several fields, and for one field
+    from 512x512 up, where the row pass is bound by its per-element exp/sincos (GB300, one
+    field, Nz 128, precompute included: 1024^2 5.9 -> 4.6 ms ignore / 8.1 -> 7.0 ms
+    weighted, 512^2 2.5 -> 2.3 / 3.7 -> 3.2 ms; at 256^2 the weighted march slows down)."""
+    return batch >= 2 or Nx * Ny >= 512 * 512
+
+
 def precompute_mask(plan, dn_t, dn_kind):
-    """Phase masks (Nz, Ny, Nx) complex64 of a shared dn volume (bpm_mask_precompute), for
-    batches: every field then reads them instead of re-evaluating exp(-i k0 dz dn)."""
+    """Phase masks (Nz, Ny, Nx) complex64 of a shared dn volume (bpm_mask_precompute): every
+    field then reads them instead of re-evaluating exp(-i k0 dz dn) (see mask_pays)."""
     Nx, Ny, Nz = plan.size
     mask = torch.empty((Nz, Ny, Nx), dtype=torch.complex64, device=dn_t.device)
     N.check(N.lib().bpm_mask_precompute(plan.handle, _ptr(dn_t), dn_kind, _ptr(mask), _stream_ptr()),
@@ -420,7 +430,7 @@ def bpm_3d_batched(size, units, lam=.5, u0=None, dn=None, n0=1., return_full=Tru
     else:
         tabs = (None, None)
     out_kind = (N.OUT_FIELD if return_field else N.OUT_INTENSITY) if return_full else N.OUT_NONE
-    mask = precompute_mask(plan, dn_t, kind) if (dn_t is not None and bstride == 0 and B >= 2) else None
+    mask = precompute_mask(plan, dn_t, kind) if (dn_t is not None and bstride == 0 and mask_pays(B, Nx, Ny)) else None
     if out is not None and return_full:
         host = torch.from_numpy(out) if isinstance(out, np.ndarray) else out
         vdt = torch.complex64 if return_field else torch.float32

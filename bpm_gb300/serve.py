@@ -32,7 +32,7 @@ import numpy as np
 import torch
 
 from . import _native as N
-from .bpm3d import _dn_kind, _ptr, get_plan, precompute_mask
+from .bpm3d import _dn_kind, _ptr, get_plan, mask_pays, precompute_mask
 from .psf import _debye
 
 __all__ = ["BpmRequest", "PsfRequest", "Server"]
@@ -73,6 +73,7 @@ class BpmRequest:
         if self.dn is not None:
             cplx = self.dn.is_complex() if torch.is_tensor(self.dn) else np.iscomplexobj(self.dn)
             b += Nz * plane * (8 if cplx else 4)
+            b += Nz * plane * 8  # phase masks, if the launch precomputes them (an upper bound)
         if self.return_full:
             b += Nz * plane * (8 if self.return_field else 4)
         return b
@@ -288,10 +289,10 @@ class Server:
             vols = [r.dn for r in reqs]
             if all(_device_volume(v, tdt, (Nz, Ny, Nx), dev) for v in vols) and \
                     all(v.data_ptr() == vols[0].data_ptr() for v in vols):
-                # every field reads the same resident volume: march it in place, no copy;
-                # several fields share its phase masks, computed once
+                # every field reads the same resident volume: march it in place, no copy; its
+                # phase masks are computed once where that pays (several fields, large grids)
                 dn = vols[0]
-                if B >= 2:
+                if mask_pays(B, Nx, Ny):
                     mask = precompute_mask(plan, dn, kind)
             else:
                 dn = torch.empty((B, Nz, Ny, Nx), dtype=tdt, device=dev)
