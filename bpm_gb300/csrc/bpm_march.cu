@@ -821,7 +821,7 @@ row_shared_kernel(RowParams p, int nfields, int fw) {
   for (int m = 0; m < E; m++) dst[t + L * m] = v[m];
 }
 
-// Column pass without the tile transposition (128 <= N <= 512, no scattering sums). The
+// Column pass without the tile transposition (128 <= N <= 1024, with or without scattering sums). The
 // block's 32*C threads load C columns (16, or 8 for small non-weighted passes) in the
 // coalesced tile mapping — thread (r0, cc) = (tid / C, tid % C) holds rows r0 + 32 i of column
 // x0 + cc — and keep that mapping for every pointwise step (the propagator from the
