@@ -145,9 +145,10 @@ int bpm_plan_destroy(bpm_plan* plan);
 int bpm_group_size(const bpm_plan* plan, int batch, int group);
 
 /* Bytes of scratch bpm_propagate needs for a request of `batch` fields (256-aligned): one
- * slot per group of fields that may march at the same time (up to 4, each on its own
- * stream forked from and joined back to the caller's stream). Any workspace of at least
- * one slot works; smaller ones march the groups one after another. */
+ * slot per group of fields that may march at the same time (4 by default, 1..8 through the
+ * environment variable BPM_GB300_CONC, each on its own stream forked from and joined back
+ * to the caller's stream). Any workspace of at least one slot works; smaller ones march
+ * the groups one after another. */
 size_t bpm_workspace_bytes(const bpm_plan* plan, int batch, int group);
 
 /* March every field of the request through all nz slices.
