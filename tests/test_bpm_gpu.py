@@ -128,9 +128,13 @@ def test_complex_dn_ignore_and_errors(bpm):
         bpm.bpm_3d(size, (.1, .1, .1), dn=np.zeros((3, 64, 64), np.float32))
 
 
-def test_scattering_outputs(bpm):
-    size = (64, 64, 24)
-    dn = sphere_dn(64, 64, 24, 8, .04)
+@pytest.mark.parametrize("size", [(64, 64, 24), (256, 128, 12), (64, 256, 10), (128, 512, 8), (32, 1024, 6)])
+def test_scattering_outputs(bpm, size):
+    """Scattered power p and g-factor (bpm_3d.py:335-341, 395-414) against the FP64 oracle:
+    column lengths 64 (tile kernels) and 128 .. 1024 (the column-split kernel's scattering
+    instances), both mean modes."""
+    Nx, Ny, Nz = size
+    dn = sphere_dn(Nx, Ny, Nz, min(Nx, Ny) / 8, .04)
     for mode in ("weighted", "ignore"):
         u, p, g = bpm.bpm_3d(size, (.1, .1, .1), lam=.5, n0=1.0, dn=dn, mean_mode=mode,
                              return_scattering=True, return_g=True)
@@ -142,7 +146,7 @@ def test_scattering_outputs(bpm):
         # g = G/p is 0/0 where nothing has scattered yet (p at rounding level): compare
         # where the scattered power is resolved in FP32
         sel = po > 1e-3 * po.max()
-        assert sel.sum() > 5
+        assert sel.sum() >= max(3, Nz // 2)
         assert rel_l2(g[sel], go[sel]) < 1e-3
 
 
