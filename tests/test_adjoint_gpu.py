@@ -100,9 +100,13 @@ def test_gradient_vs_fp64_finite_differences(torch_bpm):
         assert abs(grad[idx] - fd) <= 2e-3 * abs(fd) + 1e-4 * scale, (idx, grad[idx], fd)
 
 
-def test_gradient_vs_torch_fp64_autograd(torch_bpm):
+@pytest.mark.parametrize("size", [(64, 32, 24), (256, 128, 10), (128, 512, 6), (1024, 64, 5)])
+def test_gradient_vs_torch_fp64_autograd(torch_bpm, size):
+    """Forward exit field, d(loss)/d(dn) and d(loss)/d(u0) against FP64 torch autograd of
+    the restated march: tile kernels (64, 32), warp row / column-split kernels (128 .. 512),
+    1024-point rows; with and without the absorbing taper."""
     torch, bpm, propagate_exit = torch_bpm
-    size, units, lam, n0 = (64, 32, 24), (.1, .1, .1), .5, 1.33
+    units, lam, n0 = (.1, .1, .1), .5, 1.33
     Nx, Ny, Nz = size
     u0 = tilted_waves(4, Nx, Ny, .1, lam, .6, 5)
     dn = spheres(Nx, Ny, Nz, 3, 6)
