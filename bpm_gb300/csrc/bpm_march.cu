@@ -2003,9 +2003,14 @@ int enqueue_march(bpm_plan* pl, const bpm_request* r, void* ws, size_t ws_bytes,
           if ((rc = launch_row_z(pl, r, c[j], i + 1, st[j]))) return rc;
         }
         const int z1 = std::min(i + 2, nz);  // planes [0, z1) of the group are written
-        if (sink && (z1 - zdone[j] >= sink->chunk || z1 == nz) && z1 > zdone[j]) {
-          if ((rc = sink_copy(pl, r, *sink, b0[j], Gc[j], zdone[j], z1, st[j], pl->ev_ready[j]))) return rc;
-          zdone[j] = z1;
+        if (sink) {
+          // a group's first run goes out after 2 planes, so the host link, the slower side,
+          // starts early; later runs are sink->chunk planes
+          const int run = zdone[j] == 0 ? std::min(sink->chunk, 2) : sink->chunk;
+          if ((z1 - zdone[j] >= run || z1 == nz) && z1 > zdone[j]) {
+            if ((rc = sink_copy(pl, r, *sink, b0[j], Gc[j], zdone[j], z1, st[j], pl->ev_ready[j]))) return rc;
+            zdone[j] = z1;
+          }
         }
       }
     }
