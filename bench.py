@@ -529,7 +529,8 @@ def mixed_batch_timing(n=48, seed=5):
     256^2 and 512^2 with Nz in {64, 128, 256} (weighted mean mode, one shared resident dn
     volume per grid, |u|^2 volume kept on the device), submitted at once to the serving
     loop, which merges same-grid requests into batched launches and overlaps the grids on
-    separate streams; against the same requests one after the other through bpm_3d."""
+    separate streams, and replayed as one CUDA graph (MixedBatch); against the same
+    requests one after the other through bpm_3d."""
     import torch
     import bpm_gb300
     from bpm_gb300.serve import BpmRequest, Server
@@ -569,14 +570,33 @@ def mixed_batch_timing(n=48, seed=5):
     served()                                                    # warm-up of the serving path
     out, t_mix, st = served()
     same = all(bool(torch.equal(out[i], ref[i])) for i in range(0, n, 7))
+    # the same requests replayed as one CUDA graph (MixedBatch): groups of a grid and Nz march
+    # together, every group a parallel branch
+    mb = bpm_gb300.MixedBatch([BpmRequest((side, side, nz), UNITS, lam=LAM, n0=N0, u0=u0, dn=dns[side][:nz])
+                               for side, nz, u0 in reqs])
+    mb.run()
+    torch.cuda.synchronize()
+    a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    a.record()
+    for _ in range(3):
+        mb.run()
+    b.record()
+    torch.cuda.synchronize()
+    t_graph = a.elapsed_time(b) / 3 * 1e-3
+    same = same and all(bool(torch.equal(mb.result(i), ref[i])) for i in range(0, n, 5))
+    n_groups = len(mb.groups)
+    del mb
     del dns, reqs, ref, out
     torch.cuda.empty_cache()
     return {"requests": n, "grids": "128^2, 256^2, 512^2; Nz in {64, 128, 256}; weighted; shared dn per grid",
             "voxel_updates": vu, "mixed_ms": t_mix * 1e3, "mixed_voxel_updates_per_s": vu / t_mix,
             "sequential_ms": t_seq * 1e3, "sequential_voxel_updates_per_s": vu / t_seq,
             "speedup": t_seq / t_mix, "p50_ms": st["p50_ms"], "p99_ms": st["p99_ms"],
+            "one_graph_ms": t_graph * 1e3, "one_graph_voxel_updates_per_s": vu / t_graph,
+            "one_graph_groups": n_groups, "one_graph_speedup": t_seq / t_graph,
             "same_result_as_alone": same,
-            "api": "bpm_gb300.serve.Server (all submitted at once) vs bpm_gb300.bpm_3d per request"}
+            "api": "bpm_gb300.serve.Server (all submitted at once) and bpm_gb300.MixedBatch (one CUDA graph) "
+                   "vs bpm_gb300.bpm_3d per request"}
 
 
 def config1_dn(n=128):

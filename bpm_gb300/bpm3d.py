@@ -20,7 +20,7 @@ import torch
 
 from . import _native as N
 
-__all__ = ["bpm_3d", "bpm_3d_batched", "Bpm3d", "BatchedMarch", "Plan", "get_plan"]
+__all__ = ["bpm_3d", "bpm_3d_batched", "Bpm3d", "BatchedMarch", "MixedBatch", "Plan", "get_plan"]
 
 
 # ----------------------------------------------------------------------------------------
@@ -581,6 +581,97 @@ class BatchedMarch:
             except Exception:
                 pass
             self.exec = None
+
+
+class MixedBatch:
+    """Marches of different grids, wavelengths, refractive indices and illuminations replayed
+    as one CUDA graph (one launch). Requests (objects with the fields of
+    bpm_gb300.serve.BpmRequest: size, units, lam, n0, u0, dn, mean_mode, absorbing_width)
+    that share a grid, physics and dn volume march together as one batched group with
+    resident buffers (phase masks precomputed where mask_pays); every group runs on its own
+    stream, captured as a parallel branch of the graph, so run() launches them all at once.
+    Each request's |u|^2 volume (out_kind "intensity") or field volume ("field") is result(i);
+    its exit field last(i). A group is bit-identical to the same requests marched alone."""
+
+    def __init__(self, requests, out_kind="intensity", use_graph=True):
+        dev = _device()
+        ok = {"field": N.OUT_FIELD, "intensity": N.OUT_INTENSITY}[out_kind]
+        self.requests = list(requests)
+        groups = {}
+        for i, r in enumerate(self.requests):
+            if r.mean_mode == "simple":
+                raise NotImplementedError("MixedBatch: mean_mode 'simple' (per-request slice tables) is not batched")
+            # the same dn volume: the same device memory (views of one tensor alike), or the
+            # same host array object
+            dn_id = ((r.dn.data_ptr(), tuple(r.dn.shape), r.dn.dtype) if _is_tensor(r.dn) else id(r.dn))
+            key = (tuple(int(v) for v in r.size), tuple(float(u) for u in r.units), float(r.lam), float(r.n0),
+                   r.mean_mode, int(r.absorbing_width), dn_id)
+            groups.setdefault(key, []).append(i)
+        self.where = [None] * len(self.requests)  # request -> (group, index in group)
+        self.groups = []
+        for gi, (key, idx) in enumerate(groups.items()):
+            r0 = self.requests[idx[0]]
+            Nx, Ny, Nz = (int(v) for v in r0.size)
+            B = len(idx)
+            plan = get_plan((Nx, Ny, Nz), r0.units, r0.lam, r0.n0, r0.absorbing_width, r0.mean_mode,
+                            N.PROP_FUNCTIONAL)
+            u0 = torch.ones((B, Ny, Nx), dtype=torch.complex64, device=dev)
+            for k, i in enumerate(idx):
+                if self.requests[i].u0 is not None:
+                    u0[k].copy_(_h2d(self.requests[i].u0, torch.complex64, dev).reshape(Ny, Nx))
+            kind, tdt = _dn_kind(r0.dn, False)
+            if kind == N.DN_C64 and r0.mean_mode != "ignore":
+                raise NotImplementedError("complex dn is only defined for mean_mode='ignore'")
+            dn = _h2d(r0.dn, tdt, dev) if r0.dn is not None else None
+            if dn is not None:
+                _check_shapes((Nx, Ny, Nz), None, dn)
+            mask = precompute_mask(plan, dn, kind) if (dn is not None and mask_pays(B, Nx, Ny)) else None
+            shape = (B, Nz, Ny, Nx)
+            out = torch.empty(shape, dtype=torch.complex64 if ok == N.OUT_FIELD else torch.float32, device=dev)
+            last = torch.empty((B, Ny, Nx), dtype=torch.complex64, device=dev)
+            wsb = plan.workspace_bytes(B, 0)
+            ws = torch.empty(wsb, dtype=torch.uint8, device=dev)
+            req = N.Request(B, _ptr(u0), _ptr(dn), kind, 0, None, None, _ptr(out), ok, Nz * Ny * Nx, _ptr(last),
+                            None, None, 0, 0, None, 0, _ptr(mask))
+            self.groups.append(dict(plan=plan, u0=u0, dn=dn, mask=mask, out=out, last=last, ws=ws, wsb=wsb,
+                                    req=req, stream=torch.cuda.Stream(device=dev)))
+            for k, i in enumerate(idx):
+                self.where[i] = (gi, k)
+        torch.cuda.synchronize()
+        self.graph = None
+        if use_graph:
+            self._enqueue()  # first run eagerly: plans' kernels prepared outside the capture
+            torch.cuda.synchronize()
+            self.graph = torch.cuda.CUDAGraph()
+            cs = torch.cuda.Stream(device=dev)
+            with torch.cuda.graph(self.graph, stream=cs):
+                self._enqueue()
+
+    def _enqueue(self):
+        """Every group's march on its own stream, forked from and joined back to the current
+        stream."""
+        cur = torch.cuda.current_stream()
+        for g in self.groups:
+            g["stream"].wait_stream(cur)
+            N.check(N.lib().bpm_propagate(g["plan"].handle, ctypes.byref(g["req"]), _ptr(g["ws"]), g["wsb"],
+                                          ctypes.c_void_p(g["stream"].cuda_stream)), "bpm_propagate")
+        for g in self.groups:
+            cur.wait_stream(g["stream"])
+
+    def run(self):
+        """All marches once (one graph launch), ordered on the current stream."""
+        if self.graph is not None:
+            self.graph.replay()
+        else:
+            self._enqueue()
+
+    def result(self, i):
+        g, k = self.where[i]
+        return self.groups[g]["out"][k]
+
+    def last(self, i):
+        g, k = self.where[i]
+        return self.groups[g]["last"][k]
 
 
 # ----------------------------------------------------------------------------------------

@@ -100,6 +100,30 @@ def test_batched_1024_matches_single_and_oracle(bpm, size, mode):
         assert rel_l2(single, o64) < TOL
 
 
+def test_mixed_batch_one_graph(bpm):
+    """Grids 128x64, 256x128 and 64x64 (the cluster kernel) at two wavelengths, one shared
+    resident dn per grid, replayed as one CUDA graph: every request equals the same request
+    marched alone, bit for bit, on every replay."""
+    import torch
+    from bpm_gb300.serve import BpmRequest
+    sizes = [(128, 64, 9), (256, 128, 7), (64, 64, 6)]
+    dns = {sz: torch.from_numpy(random_spheres(*sz, 4, sz[0])).cuda() for sz in sizes}
+    reqs = []
+    for k in range(11):
+        sz = sizes[k % 3]
+        u0 = np.exp(1j * .05 * k * np.arange(sz[0]))[None].repeat(sz[1], 0).astype(np.complex64)
+        reqs.append(BpmRequest(sz, (.1, .1, .1), lam=(.5, .6)[k % 2], n0=1.33, u0=u0, dn=dns[sz]))
+    mb = bpm.MixedBatch(reqs)
+    assert len(mb.groups) == 6
+    for rep in range(2):
+        mb.run()
+        torch.cuda.synchronize()
+        for i, r in enumerate(reqs):
+            want = bpm.bpm_3d(r.size, r.units, lam=r.lam, n0=r.n0, u0=r.u0, dn=r.dn, return_field=False)
+            want = want.cpu().numpy() if torch.is_tensor(want) else want
+            assert np.array_equal(mb.result(i).cpu().numpy(), want), (rep, i)
+
+
 def test_config1_plain(bpm):
     """128^3, dx=dz=0.1, lam 0.5, n0 1.33, plane wave, one centred sphere r=20 px dn=0.05;
     exit field and |u|^2 volume."""
