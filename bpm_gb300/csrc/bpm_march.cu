@@ -754,11 +754,14 @@ __device__ __forceinline__ float2 staged_mask(const RowParams& p, const void* ml
 // idle slot), so the mask row (or dn row) of slice z is staged once per block into shared
 // memory with cp.async at block start and is ready when the sequences finish their inverse
 // row FFTs. The arithmetic is row_warp_kernel's.
-template <int N, int PRE, int L = 32>
+template <int N, int PRE, int L = 32, int FW = 0>
 __global__ void __launch_bounds__(kRowWarps * 32, N / L >= 32 ? 2 : 4)
-row_shared_kernel(RowParams p, int nfields, int fw) {
+row_shared_kernel(RowParams p, int nfields, int fw_rt) {
   constexpr int E = N / L;
-  const int T = blockDim.x;
+  // FW > 0: a compile-time block of FW fields (the full groups of batched marches), so the
+  // staging loops and slot offsets are constants; FW = 0: fw_rt fields per block
+  const int fw = FW > 0 ? FW : fw_rt;
+  const int T = FW > 0 ? (FW * L + 31) / 32 * 32 : (int)blockDim.x;
   const int slots = T / L;
   extern __shared__ __align__(16) float2 smem[];
   float2* tw = smem;
@@ -1402,6 +1405,10 @@ struct RowK {
                          (int)W::ROW_SMEM_SHARED);
     cudaFuncSetAttribute(row_shared_kernel<N, 1, L>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                          (int)W::ROW_SMEM_SHARED);
+    cudaFuncSetAttribute(row_shared_kernel<N, 0, L, kRowWarps>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                         (int)W::ROW_SMEM_SHARED);
+    cudaFuncSetAttribute(row_shared_kernel<N, 1, L, kRowWarps>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                         (int)W::ROW_SMEM_SHARED);
     cudaFuncSetAttribute(row_warp_kernel<N, false, 0, kRowWarps, L>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                          (int)W::ROW_SMEM);
     cudaFuncSetAttribute(row_warp_kernel<N, true, 0, kRowWarps, L>, cudaFuncAttributeMaxDynamicSharedMemorySize,
@@ -1462,7 +1469,8 @@ struct RowK {
         const int fw = ((int)g.y + nb - 1) / nb;
         const int threads = (fw * L + 31) / 32 * 32;
         const size_t sm = ((size_t)2 * N + (size_t)(threads / L) * BUF) * sizeof(float2);
-        auto fn = p.mask ? row_shared_kernel<N, 1, L> : row_shared_kernel<N, 0, L>;
+        auto fn = fw == kRowWarps ? (p.mask ? row_shared_kernel<N, 1, L, kRowWarps> : row_shared_kernel<N, 0, L, kRowWarps>)
+                                  : (p.mask ? row_shared_kernel<N, 1, L> : row_shared_kernel<N, 0, L>);
         BPM_CUDA_TRY(launch_dep(fn, dim3(p.ny, nb), dim3(threads), sm, s, p, (int)g.y, fw));
         BPM_LAUNCH_CHECK("row_shared_kernel");
         return BPM_OK;
