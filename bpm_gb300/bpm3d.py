@@ -305,8 +305,9 @@ def _bpm_3d(size, units, lam=.5, u0=None, dn=None, subsample=1, n0=1.,
     if mean_mode == "simple" and dn is None:
         tabs = (tabs[0].expand(Nz).contiguous(), tabs[1].expand(Nz).contiguous())
     out_kind = (N.OUT_FIELD if return_field else N.OUT_INTENSITY) if return_full else N.OUT_NONE
+    mask = precompute_mask(plan, dn_t, kind) if (dn_t is not None and mask_pays(1, Nx, Ny)) else None
     out, last, p, g = _run(plan, u0_t, dn_t, kind, 0, out_kind, True, return_scattering, return_g,
-                           scattering_plane_ind, tabs)
+                           scattering_plane_ind, tabs, mask=mask)
     conv = (lambda t: t) if as_tensor else _d2h
     if return_full:
         res = conv(out[0])
