@@ -81,6 +81,30 @@ def test_oracle_parity(bpm, size, mode):
     del rng
 
 
+@pytest.mark.parametrize("size", [(64, 32, 1), (64, 32, 2), (1024, 64, 1), (256, 512, 2)])
+def test_shortest_marches(bpm, size):
+    """Nz = 1 stores u0 alone (no z-step), Nz = 2 takes one step: every mean mode and output
+    form (volume or last plane, field or |u|^2) agrees with the FP64 oracle, and a batch of
+    two equals each field marched alone."""
+    Nx, Ny, Nz = size
+    rng = np.random.default_rng(4)
+    dn = (.03 * rng.standard_normal((Nz, Ny, Nx))).astype(np.float32)
+    x = .1 * np.arange(Nx)
+    u0 = np.exp(2j * np.pi * .25 * x)[None, :].repeat(Ny, 0).astype(np.complex64)
+    for mode in ("weighted", "simple", "ignore"):
+        for field, full in ((True, True), (False, True), (True, False), (False, False)):
+            kw = dict(lam=.5, n0=1.33, dn=dn, mean_mode=mode, absorbing_width=3, return_field=field,
+                      return_full=full)
+            u = bpm.bpm_3d(size, (.1, .1, .1), u0=u0, **kw)
+            o = bpm_ref.bpm_3d(size, (.1, .1, .1), u0=u0, precision="fp64", **kw)
+            assert u.shape == o.shape, (mode, field, full)
+            assert rel_l2(u, o) < TOL, (mode, field, full)
+        kw = dict(lam=.5, n0=1.33, dn=dn, mean_mode=mode, absorbing_width=3)
+        ub = bpm.bpm_3d_batched(size, (.1, .1, .1), u0=np.stack([u0, u0.conj()]), **kw)
+        assert ub.shape == (2, Nz, Ny, Nx)
+        assert np.array_equal(ub[1], bpm.bpm_3d(size, (.1, .1, .1), u0=u0.conj(), **kw)), mode
+
+
 @pytest.mark.parametrize("size,mode", [((1024, 256, 5), "weighted"), ((256, 1024, 5), "ignore")])
 def test_batched_1024_matches_single_and_oracle(bpm, size, mode):
     """1024-point rows and columns in the warp-FFT family (32 values per lane, one exchange
@@ -245,6 +269,27 @@ def test_batched_equals_single_and_deterministic(bpm):
         for b in range(5):
             us = bpm.bpm_3d(size, (.1, .1, .1), u0=u0s[b], dn=dn, mean_mode=mode, return_field=False)
             assert np.array_equal(ub[b], us)
+
+
+@pytest.mark.parametrize("kind,absorb", [("f16", 0), ("c64", 0), ("f32", 5), ("f16", 3)])
+def test_batched_masks_equal_single_for_every_dn_kind(bpm, kind, absorb):
+    """A batch over a shared dn reads phase masks precomputed once (bpm_mask_precompute);
+    a single 128x64 field forms them per element in its row passes. Both give the same bits
+    for half-precision and complex dn and with the absorbing taper (complex dn has none)."""
+    size = (128, 64, 14)
+    rng = np.random.default_rng(31)
+    dn = (.03 * rng.standard_normal((14, 64, 128))).astype(np.float32)
+    if kind == "c64":
+        dn = (dn - 1j * np.abs(.002 * rng.standard_normal(dn.shape))).astype(np.complex64)
+    u0s = np.exp(2j * np.pi * rng.uniform(-.2, .2, (3, 1, 1)) * np.arange(128)[None, None, :]
+                 ).repeat(64, 1).astype(np.complex64)
+    kw = dict(dn=dn, store_dn_as_half=kind == "f16", absorbing_width=absorb, return_field=True)
+    # complex dn is defined for mean_mode "ignore" only
+    for mode in ("ignore",) if kind == "c64" else ("weighted", "ignore"):
+        ub = bpm.bpm_3d_batched(size, (.1, .1, .1), u0=u0s, mean_mode=mode, **kw)
+        for b in range(3):
+            us = bpm.bpm_3d(size, (.1, .1, .1), u0=u0s[b], mean_mode=mode, **kw)
+            assert np.array_equal(ub[b], us), (mode, b)
 
 
 def test_batched_host_out_pipeline(bpm):
