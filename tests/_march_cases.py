@@ -1,7 +1,8 @@
 """March cases for the tests that run them in child processes (cross-process determinism;
-the cluster kernel against the pass kernels, chosen by BPM_GB300_CLUSTER).
+the cluster kernel against the pass kernels, chosen by BPM_GB300_CLUSTER; the 1024-point
+warp-FFT kernels against the tile kernels, chosen by BPM_GB300_WARP1024).
 
-    python tests/_march_cases.py OUT.npz
+    python tests/_march_cases.py OUT.npz [cluster|w1024]
 """
 import os
 import sys
@@ -64,6 +65,31 @@ def run_cluster(path):
     np.savez(path, **res)
 
 
+def w1024_cases():
+    """1024-point rows or columns (and both), every dn kind: the warp-FFT kernels
+    (BPM_GB300_WARP1024=1) against the shared-memory tile kernels (=0)."""
+    rng = np.random.default_rng(9)
+    out = []
+    for (nx, ny, nz), mode, kind, B in [((1024, 128, 6), "weighted", "f32", 3), ((128, 1024, 6), "ignore", "c64", 1),
+                                        ((1024, 1024, 4), "simple", "f16", 1), ((256, 1024, 5), "weighted", "f32", 2)]:
+        dn = (.03 * rng.standard_normal((nz, ny, nx))).astype(np.float32)
+        if kind == "c64":
+            dn = (dn - 1j * np.abs(.002 * rng.standard_normal((nz, ny, nx)))).astype(np.complex64)
+        x = np.arange(nx) * .1
+        u0 = np.exp(2j * np.pi * rng.uniform(-.3, .3, (B, 1, 1)) * x[None, None, :]).repeat(ny, 1)
+        out.append(dict(size=(nx, ny, nz), mode=mode, dn=dn, half=kind == "f16", u0=u0.astype(np.complex64)))
+    return out
+
+
+def run_w1024(path):
+    import bpm_gb300 as bpm
+    res = {}
+    for i, c in enumerate(w1024_cases()):
+        res["f%d" % i] = bpm.bpm_3d_batched(c["size"], (.1, .1, .1), u0=c["u0"], dn=c["dn"], mean_mode=c["mode"],
+                                            store_dn_as_half=c["half"], return_field=True, absorbing_width=4)
+    np.savez(path, **res)
+
+
 def run(path):
     import bpm_gb300 as bpm
     res = {}
@@ -78,5 +104,7 @@ def run(path):
 if __name__ == "__main__":
     if len(sys.argv) > 2 and sys.argv[2] == "cluster":
         run_cluster(sys.argv[1])
+    elif len(sys.argv) > 2 and sys.argv[2] == "w1024":
+        run_w1024(sys.argv[1])
     else:
         run(sys.argv[1])

@@ -378,18 +378,37 @@ def test_linearity_at_full_size(bpm):
 def test_march_deterministic_across_processes(bpm, tmp_path):
     """The same marches (three mean modes, f32 / f16 / complex dn, precomputed and
     on-the-fly masks, batched and single, rows and columns of 128..512 points) in two child
-    processes give the same bits: no kernel depends on timing, atomics or launch order."""
+    processes give the same bits: no kernel depends on timing, atomics or launch order, and
+    groups marched one at a time (BPM_GB300_CONC=1) or all at once (=8) give the same bits."""
     import subprocess
     import sys
     script = os.path.join(os.path.dirname(os.path.abspath(__file__)), "_march_cases.py")
     paths = [str(tmp_path / ("run%d.npz" % i)) for i in range(2)]
-    for path in paths:
+    for path, conc in zip(paths, ("1", "8")):
         subprocess.run([sys.executable, script, path], check=True, timeout=600,
-                       env=dict(os.environ, BPM_GB300_CLUSTER="0"))
+                       env=dict(os.environ, BPM_GB300_CLUSTER="0", BPM_GB300_CONC=conc))
     A, B = (np.load(x) for x in paths)
     assert sorted(A.files) == sorted(B.files)
     for k in A.files:
         assert np.array_equal(A[k], B[k]), k
+
+
+def test_warp1024_matches_tile_kernels(bpm, tmp_path):
+    """1024-point rows and columns: the warp-FFT kernels (default) against the shared-memory
+    tile kernels (BPM_GB300_WARP1024=0), each in a child process, for every dn kind and a
+    batch. The two FFTs run in different radix orders, so they agree to FP32 rounding."""
+    import subprocess
+    import sys
+    script = os.path.join(os.path.dirname(os.path.abspath(__file__)), "_march_cases.py")
+    paths = [str(tmp_path / ("w%s.npz" % v)) for v in ("1", "0")]
+    for path, v in zip(paths, ("1", "0")):
+        subprocess.run([sys.executable, script, path, "w1024"], check=True, timeout=600,
+                       env=dict(os.environ, BPM_GB300_WARP1024=v))
+    A, B = (np.load(x) for x in paths)
+    assert sorted(A.files) == sorted(B.files) and len(A.files) == 4
+    errs = {k: rel_l2(A[k], B[k]) for k in A.files}
+    print("warp vs tile 1024, relative L2:", errs)
+    assert all(e < 2e-6 for e in errs.values()), errs
 
 
 @pytest.mark.parametrize("nz,chunk,group,field", [(37, 16, 2, False), (1, 16, 3, True), (20, 1, 4, True),
