@@ -288,6 +288,78 @@ __global__ void __launch_bounds__(256, 2) debye_accum_kernel(int T, int M, int M
     }
 }
 
+// The last nrz (1..RZ) octant planes when they are all that is left after whole 32-plane
+// tiles. The octant of an even shape has Nz/2 + 1 planes (129 at 256^3): one more 32-plane
+// tile for a single plane would cost a full tile's arithmetic, and at 256^3 a fifth wave
+// of blocks. Here the product is a matrix-vector one over the nodes, bound by reading A:
+// a block takes 64 radii (16 lanes of 4) and splits the nodes over its 16 thread rows
+// (row r takes t = r, r + 16, ...); the 16 partial sums are then added in row order, so the
+// result does not depend on timing.
+constexpr int REM_ROWS = 16;
+
+template <int RZ>
+__global__ void __launch_bounds__(256) debye_accum_rem_kernel(int T, int M, int Mp, int Zo, int Zp, int nrz,
+                                                              const float* __restrict__ J,
+                                                              const float2* __restrict__ E,
+                                                              float2* __restrict__ I) {
+  __shared__ float2 red[REM_ROWS][AM];
+  const int tid = threadIdx.x;
+  const int tm = tid & 15, tr = tid >> 4;
+  const int m0 = blockIdx.x * AM;
+  const int ma = m0 + tm * 4;  // first of this lane's 4 radii; Mp is a multiple of 4
+  const int zb = Zo - nrz;
+  const size_t TM = (size_t)T * Mp;
+  float2 acc[3][4][RZ];
+#pragma unroll
+  for (int n = 0; n < 3; n++)
+#pragma unroll
+    for (int a = 0; a < 4; a++)
+#pragma unroll
+      for (int j = 0; j < RZ; j++) acc[n][a][j] = make_float2(0.f, 0.f);
+  if (ma < Mp) {
+#pragma unroll 4
+    for (int t = tr; t < T; t += REM_ROWS) {
+      float2 ev[RZ];
+#pragma unroll
+      for (int j = 0; j < RZ; j++)
+        ev[j] = j < nrz ? __ldg(E + (size_t)t * Zp + zb + j) : make_float2(0.f, 0.f);
+#pragma unroll
+      for (int n = 0; n < 3; n++) {
+        const float4 j4 = __ldg(reinterpret_cast<const float4*>(J + n * TM + (size_t)t * Mp + ma));
+        const float jv[4] = {j4.x, j4.y, j4.z, j4.w};
+#pragma unroll
+        for (int a = 0; a < 4; a++)
+#pragma unroll
+          for (int j = 0; j < RZ; j++) {
+            acc[n][a][j].x = fmaf(jv[a], ev[j].x, acc[n][a][j].x);
+            acc[n][a][j].y = fmaf(jv[a], ev[j].y, acc[n][a][j].y);
+          }
+      }
+    }
+  }
+  const size_t ZM = (size_t)Zo * M;
+#pragma unroll
+  for (int n = 0; n < 3; n++)
+#pragma unroll
+    for (int j = 0; j < RZ; j++) {
+      if (j >= nrz) break;
+#pragma unroll
+      for (int a = 0; a < 4; a++) red[tr][tm * 4 + a] = acc[n][a][j];
+      __syncthreads();
+      if (tid < AM) {
+        float2 s = red[0][tid];
+#pragma unroll
+        for (int r = 1; r < REM_ROWS; r++) {
+          s.x += red[r][tid].x;
+          s.y += red[r][tid].y;
+        }
+        const int m = m0 + tid;
+        if (m < M) I[n * ZM + (size_t)(zb + j) * M + m] = s;
+      }
+      __syncthreads();
+    }
+}
+
 __device__ __forceinline__ int mirror_gauss(int p, int N0, int N) {
   return p >= N0 - N ? p - (N0 - N) : N - 1 - p;
 }
@@ -536,9 +608,21 @@ int run_octant(const debye_desc* d, bool gauss, double sig, float* u, void* ex, 
     cudaFuncSetAttribute(debye_accum_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)ACC_SMEM);
     attr = true;
   }
-  debye_accum_kernel<<<dim3((L.M + AM - 1) / AM, (L.Zo + AZ - 1) / AZ), 256, ACC_SMEM, s>>>(L.T, L.M, L.Mp, L.Zo,
-                                                                                          L.Zp, J, E, I);
+  // whole 32-plane tiles in the tile kernel; a remainder of 1..4 planes past them (the
+  // octant's Nz/2 + 1 planes) in the matrix-vector kernel
+  const int rem = L.Zo % AZ;
+  const int nrz = (L.Zo > AZ && rem <= 4) ? rem : 0;
+  const int mtiles = (L.M + AM - 1) / AM;
+  debye_accum_kernel<<<dim3(mtiles, (L.Zo - nrz + AZ - 1) / AZ), 256, ACC_SMEM, s>>>(L.T, L.M, L.Mp, L.Zo, L.Zp, J,
+                                                                                   E, I);
   BPM_LAUNCH_CHECK("debye_accum_kernel");
+  if (nrz == 1) {
+    debye_accum_rem_kernel<1><<<mtiles, 256, 0, s>>>(L.T, L.M, L.Mp, L.Zo, L.Zp, nrz, J, E, I);
+    BPM_LAUNCH_CHECK("debye_accum_rem_kernel");
+  } else if (nrz > 1) {
+    debye_accum_rem_kernel<4><<<mtiles, 256, 0, s>>>(L.T, L.M, L.Mp, L.Zo, L.Zp, nrz, J, E, I);
+    BPM_LAUNCH_CHECK("debye_accum_rem_kernel");
+  }
   if (u || ex || ey || ez) {
     const dim3 grid((d->nx + 127) / 128, d->ny, d->nz);
     float2 *pex = static_cast<float2*>(ex), *pey = static_cast<float2*>(ey), *pez = static_cast<float2*>(ez);

@@ -54,6 +54,11 @@ def test_config2_psf_256(bpm):
     # full index c + k (k >= 1 along z, >= 0 along x, y) holds octant sample k, unconjugated
     for a, b, k in zip((u, ex, ey, ez), octant, ("u", "ex", "ey", "ez")):
         assert rel_l2(a[c + 1:, c:, c:], b[1:c, :c, :c]) < TOL, k
+        # full index m <= c holds octant sample c - m, conjugated: index 0 is the octant's
+        # last plane (z = 12.8 um), the one the plane-remainder kernel computes
+        assert rel_l2(a[:c, c:, c:], np.conj(b[c:0:-1, :c, :c])) < TOL, k
+        # that plane alone is far from focus, where the node sum cancels more: 1e-3
+        assert rel_l2(a[0, c:, c:], np.conj(b[c, :c, :c])) < 1e-3, k
     assert np.all(np.isfinite(u))
     u_only = bpm.psf(shape, (.1, .1, .1), .5, 1.1, 1.33, 512)
     assert np.array_equal(u_only, u)
