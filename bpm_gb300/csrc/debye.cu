@@ -291,22 +291,23 @@ __global__ void __launch_bounds__(256, 2) debye_accum_kernel(int T, int M, int M
 // The last nrz (1..RZ) octant planes when they are all that is left after whole 32-plane
 // tiles. The octant of an even shape has Nz/2 + 1 planes (129 at 256^3): one more 32-plane
 // tile for a single plane would cost a full tile's arithmetic, and at 256^3 a fifth wave
-// of blocks. Here the product is a matrix-vector one over the nodes, bound by reading A:
-// a block takes 64 radii (16 lanes of 4) and splits the nodes over its 16 thread rows
-// (row r takes t = r, r + 16, ...); the 16 partial sums are then added in row order, so the
-// result does not depend on timing.
-constexpr int REM_ROWS = 16;
+// of blocks. Here the product is a matrix-vector one over the nodes, bound by reading A
+// with few loads in flight per thread: a block takes 16 radii (4 lanes of 4) and splits
+// the nodes over its 64 thread rows (row r takes t = r, r + 64, ...), so each thread's
+// chain of dependent loads is T/64 long; the 64 partial sums are then added in row order,
+// so the result does not depend on timing.
+constexpr int REM_LANES = 4, REM_ROWS = 256 / REM_LANES, REM_M = 4 * REM_LANES;
 
 template <int RZ>
 __global__ void __launch_bounds__(256) debye_accum_rem_kernel(int T, int M, int Mp, int Zo, int Zp, int nrz,
                                                               const float* __restrict__ J,
                                                               const float2* __restrict__ E,
                                                               float2* __restrict__ I) {
-  __shared__ float2 red[REM_ROWS][AM];
+  __shared__ float2 red[REM_ROWS][REM_M];
   const int tid = threadIdx.x;
-  const int tm = tid & 15, tr = tid >> 4;
-  const int m0 = blockIdx.x * AM;
-  const int ma = m0 + tm * 4;  // first of this lane's 4 radii; Mp is a multiple of 4
+  const int tl = tid % REM_LANES, tr = tid / REM_LANES;
+  const int m0 = blockIdx.x * REM_M;
+  const int ma = m0 + tl * 4;  // first of this lane's 4 radii; Mp is a multiple of 4
   const int zb = Zo - nrz;
   const size_t TM = (size_t)T * Mp;
   float2 acc[3][4][RZ];
@@ -344,11 +345,10 @@ __global__ void __launch_bounds__(256) debye_accum_rem_kernel(int T, int M, int 
     for (int j = 0; j < RZ; j++) {
       if (j >= nrz) break;
 #pragma unroll
-      for (int a = 0; a < 4; a++) red[tr][tm * 4 + a] = acc[n][a][j];
+      for (int a = 0; a < 4; a++) red[tr][tl * 4 + a] = acc[n][a][j];
       __syncthreads();
-      if (tid < AM) {
+      if (tid < REM_M) {
         float2 s = red[0][tid];
-#pragma unroll
         for (int r = 1; r < REM_ROWS; r++) {
           s.x += red[r][tid].x;
           s.y += red[r][tid].y;
@@ -616,11 +616,12 @@ int run_octant(const debye_desc* d, bool gauss, double sig, float* u, void* ex, 
   debye_accum_kernel<<<dim3(mtiles, (L.Zo - nrz + AZ - 1) / AZ), 256, ACC_SMEM, s>>>(L.T, L.M, L.Mp, L.Zo, L.Zp, J,
                                                                                    E, I);
   BPM_LAUNCH_CHECK("debye_accum_kernel");
+  const int rtiles = (L.M + REM_M - 1) / REM_M;
   if (nrz == 1) {
-    debye_accum_rem_kernel<1><<<mtiles, 256, 0, s>>>(L.T, L.M, L.Mp, L.Zo, L.Zp, nrz, J, E, I);
+    debye_accum_rem_kernel<1><<<rtiles, 256, 0, s>>>(L.T, L.M, L.Mp, L.Zo, L.Zp, nrz, J, E, I);
     BPM_LAUNCH_CHECK("debye_accum_rem_kernel");
   } else if (nrz > 1) {
-    debye_accum_rem_kernel<4><<<mtiles, 256, 0, s>>>(L.T, L.M, L.Mp, L.Zo, L.Zp, nrz, J, E, I);
+    debye_accum_rem_kernel<4><<<rtiles, 256, 0, s>>>(L.T, L.M, L.Mp, L.Zo, L.Zp, nrz, J, E, I);
     BPM_LAUNCH_CHECK("debye_accum_rem_kernel");
   }
   if (u || ex || ey || ez) {
