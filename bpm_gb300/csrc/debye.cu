@@ -288,8 +288,8 @@ __global__ void __launch_bounds__(256, 2) debye_accum_kernel(int T, int M, int M
     }
 }
 
-// The last nrz (1..RZ) octant planes when they are all that is left after whole 32-plane
-// tiles. The octant of an even shape has Nz/2 + 1 planes (129 at 256^3): one more 32-plane
+// The last nrz (<= RZ) octant planes when they are all that is left after whole 32-plane
+// tiles (the host launches it for a single plane). The octant of an even shape has Nz/2 + 1 planes (129 at 256^3): one more 32-plane
 // tile for a single plane would cost a full tile's arithmetic, and at 256^3 a fifth wave
 // of blocks. Here the product is a matrix-vector one over the nodes, bound by reading A
 // with few loads in flight per thread: a block takes 16 radii (4 lanes of 4) and splits
@@ -608,10 +608,10 @@ int run_octant(const debye_desc* d, bool gauss, double sig, float* u, void* ex, 
     cudaFuncSetAttribute(debye_accum_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)ACC_SMEM);
     attr = true;
   }
-  // whole 32-plane tiles in the tile kernel; a remainder of 1..4 planes past them (the
-  // octant's Nz/2 + 1 planes) in the matrix-vector kernel
-  const int rem = L.Zo % AZ;
-  const int nrz = (L.Zo > AZ && rem <= 4) ? rem : 0;
+  // whole 32-plane tiles in the tile kernel; a single plane past them (the octant's
+  // Nz/2 + 1 planes of a power-of-two shape) in the matrix-vector kernel; other
+  // remainders stay a partial tile of the tile kernel
+  const int nrz = (L.Zo > AZ && L.Zo % AZ == 1) ? 1 : 0;
   const int mtiles = (L.M + AM - 1) / AM;
   debye_accum_kernel<<<dim3(mtiles, (L.Zo - nrz + AZ - 1) / AZ), 256, ACC_SMEM, s>>>(L.T, L.M, L.Mp, L.Zo, L.Zp, J,
                                                                                    E, I);
@@ -619,9 +619,6 @@ int run_octant(const debye_desc* d, bool gauss, double sig, float* u, void* ex, 
   const int rtiles = (L.M + REM_M - 1) / REM_M;
   if (nrz == 1) {
     debye_accum_rem_kernel<1><<<rtiles, 256, 0, s>>>(L.T, L.M, L.Mp, L.Zo, L.Zp, nrz, J, E, I);
-    BPM_LAUNCH_CHECK("debye_accum_rem_kernel");
-  } else if (nrz > 1) {
-    debye_accum_rem_kernel<4><<<rtiles, 256, 0, s>>>(L.T, L.M, L.Mp, L.Zo, L.Zp, nrz, J, E, I);
     BPM_LAUNCH_CHECK("debye_accum_rem_kernel");
   }
   if (u || ex || ey || ez) {
