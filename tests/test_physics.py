@@ -1,0 +1,121 @@
+"""Physical checks of the split-step march and the Debye-Wolf field, on the oracle (CPU, FP64
+and FP32). The reference's own test scripts make these comparisons by eye (tests/test_plane.py,
+test_gaussian.py, test_energy.py, test_refraction.py, test_single_focus.py); here each one
+asserts a bound. The CUDA path is held to the oracle at 1e-4 by the GPU parity tests, so
+these bounds carry over to it."""
+import numpy as np
+import pytest
+
+from conftest import rel_l2
+from oracle import bpm_ref, debye_ref
+
+
+def gaussian_beam(x, y, z, lam, NA):
+    """Paraxial Gaussian beam with waist lam / (pi asin NA) at z = 0, in bpm_3d's phase
+    convention exp(-i k z) (the form of tests/test_gaussian.py)."""
+    r2 = x ** 2 + y ** 2
+    k = 2 * np.pi / lam
+    w0 = lam / np.pi / np.arcsin(NA)
+    zr = np.pi * w0 ** 2 / lam
+    w = w0 * np.sqrt(1 + (z / zr) ** 2)
+    R = z * (1 + (zr / z) ** 2)
+    return w0 / w * np.exp(-r2 / w ** 2) * np.exp(-1j * (k * z + k * r2 / 2. / R - np.arctan(z / zr)))
+
+
+@pytest.mark.parametrize("precision", ["fp64", "fp32"])
+def test_gaussian_beam_free_space(precision):
+    """A Gaussian beam started at z = -Nz dz / 2 and marched through free space follows the
+    paraxial formula, the closer the smaller its NA (the formula's error grows as NA^4)."""
+    errs = []
+    for (Nx, Ny, Nz), (dx, dy, dz), NA in (((128, 128, 128), (.2, .2, .2), .1),
+                                          ((64, 128, 96), (.2, .1, .1), .15)):
+        x = dx * (np.arange(-Nx / 2, Nx / 2) + .5)
+        y = dy * (np.arange(-Ny / 2, Ny / 2) + .5)
+        z = dz * (np.arange(-Nz / 2, Nz / 2) + .5)
+        Z, Y, X = np.meshgrid(z, y, x, indexing="ij")
+        ua = gaussian_beam(X, Y, Z, .5, NA)
+        u = bpm_ref.bpm_3d((Nx, Ny, Nz), (dx, dy, dz), lam=.5, n0=1., u0=ua[0].astype(np.complex64),
+                           precision=precision)
+        errs.append(rel_l2(u, ua))
+    assert errs[0] < .005 and errs[1] < .01, errs     # observed 0.0029 and 0.0056
+    assert errs[0] < errs[1]
+
+
+@pytest.mark.parametrize("mode", ["ignore", "simple", "weighted"])
+@pytest.mark.parametrize("precision", ["fp64", "fp32"])
+def test_energy_never_grows(mode, precision):
+    """Real dn and no absorbing taper: the propagator has modulus <= 1 (0 past the
+    evanescent cut), the phase mask modulus 1 and the FFT pair is unitary up to its
+    1/(Nx Ny), so sum |u|^2 cannot grow from one plane to the next; over smooth dn it
+    barely falls."""
+    Nx, Ny, Nz = 64, 32, 40
+    rng = np.random.default_rng(11)
+    dn = (.05 * rng.uniform(-1, 1, (Nz, Ny, Nx))).astype(np.float32)
+    x = .1 * np.arange(Nx)
+    # a frequency of the grid (3 periods across it): no spectral leakage past the
+    # evanescent cut, which would take energy out in the first step
+    u0 = np.exp(-1j * 2 * np.pi * 3 / (Nx * .1) * x)[None, :].repeat(Ny, 0).astype(np.complex64)
+    I = bpm_ref.bpm_3d((Nx, Ny, Nz), (.1, .1, .1), lam=.5, n0=1.33, u0=u0, dn=dn, mean_mode=mode,
+                       return_field=False, precision=precision)
+    E = I.reshape(Nz, -1).sum(1).astype(np.float64)
+    tol = 1e-12 if precision == "fp64" else 1e-5
+    assert np.all(E[1:] <= E[:-1] * (1 + tol)), np.diff(E) / E[:-1]
+    assert E[-1] > .9 * E[0]
+    # the same march through the uniform dn mean keeps the energy to rounding
+    I0 = bpm_ref.bpm_3d((Nx, Ny, Nz), (.1, .1, .1), lam=.5, n0=1.33, u0=u0, mean_mode=mode,
+                        return_field=False, precision=precision)
+    E0 = I0.reshape(Nz, -1).sum(1).astype(np.float64)
+    assert np.allclose(E0, E0[0], rtol=10 * tol, atol=0)
+
+
+@pytest.mark.parametrize("mode", ["ignore", "simple", "weighted"])
+@pytest.mark.parametrize("precision", ["fp64", "fp32"])
+def test_refraction_in_a_uniform_medium(mode, precision):
+    """A tilted plane wave in a medium of index n0 + dn keeps its transverse wavenumber kx
+    and advances exp(-i kz dz) per step. With the mean-index correction (simple and
+    weighted modes) the propagator runs at n0 + dn, so kz = sqrt((n0 + dn)^2 k0^2 - kx^2):
+    Snell's law in the refracted medium. Without it (ignore) the step splits into the
+    free-space propagator at n0 and the phase mask: kz = sqrt(n0^2 k0^2 - kx^2) + k0 dn."""
+    Nx, Ny, Nz = 64, 16, 30
+    dx = dz = .1
+    lam, n0, dnv = .5, 1.33, .05
+    k0 = 2 * np.pi / lam
+    kx = 2 * np.pi * 9 / (Nx * dx)      # a frequency of the grid: an exact mode of the march
+    x = dx * np.arange(Nx)
+    u0 = np.exp(-1j * kx * x)[None, :].repeat(Ny, 0).astype(np.complex64)
+    dn = np.full((Nz, Ny, Nx), dnv, np.float32)
+    u = bpm_ref.bpm_3d((Nx, Ny, Nz), (dx, dx, dz), lam=lam, n0=n0, u0=u0, dn=dn, mean_mode=mode,
+                       precision=precision)
+    if mode == "ignore":
+        kz = np.sqrt((n0 * k0) ** 2 - kx ** 2) + k0 * float(np.float32(dnv))
+    else:
+        kz = np.sqrt(((n0 + float(np.float32(dnv))) * k0) ** 2 - kx ** 2)
+    want = u0[None] * np.exp(-1j * kz * dz * np.arange(Nz))[:, None, None]
+    # the FP64 flavour still takes the reference's float32 inputs (dn, simple mode's dn0 as a
+    # float32 mean): observed up to 3e-7
+    assert rel_l2(u, want) < (2e-6 if precision == "fp64" else 1e-4)
+    # the refracted direction: sin(theta) = kx / kz' scales as 1 / n
+    if mode != "ignore":
+        th0 = np.arcsin(kx / (n0 * k0))
+        th1 = np.arctan(kx / kz)
+        assert np.isclose(n0 * np.sin(th0), (n0 + dnv) * np.sin(th1), rtol=1e-6)
+
+
+def test_bpm_carries_the_debye_focus():
+    """The two hot paths agree: marching the Debye field of the first plane with the
+    split-step propagator reproduces the Debye field of every later plane (each quadrature
+    node is a cone of plane waves with kz = k cos t). The Debye kernel's phase is
+    exp(+i k z cos t) and bpm_3d's exp(-i k z), so the march takes conjugated fields:
+    conj(psf_u0) focuses zfoc downstream in bpm_3d, psf_u0 itself (as in the reference)
+    moves away from the focus."""
+    for size, units, lam, NA, n0, err in (((64, 64, 64), (.1, .1, .1), .5, .3, 1., .05),
+                                          ((128, 128, 64), (.1, .1, .1), .5, .5, 1.33, .025)):
+        _, ex, _, _ = debye_ref.focus_field_debye(size, units, lam, NA, n0, 200, real_dtype=np.float64,
+                                                  complex_dtype=np.complex128)
+        u0 = debye_ref.psf_u0(size[:2], units[:2], zfoc=.5 * units[2] * size[2], NA=NA, lam=lam, n0=n0)
+        assert rel_l2(u0, ex[0]) < 1e-6
+        u = bpm_ref.bpm_3d(size, units, lam=lam, n0=n0, u0=np.conj(u0), precision="fp64")
+        assert rel_l2(u, np.conj(ex)) < err, size      # observed 0.038, 0.017
+        assert rel_l2(np.abs(u) ** 2, np.abs(ex) ** 2) < err / 2, size
+        away = bpm_ref.bpm_3d(size, units, lam=lam, n0=n0, u0=u0, precision="fp64")
+        assert rel_l2(np.abs(away[-1]) ** 2, np.abs(ex[-1]) ** 2) > .3
