@@ -1,10 +1,11 @@
 """Physical checks of the split-step march and the Debye-Wolf field, on the oracle (CPU, FP64
-and FP32). The reference's own test scripts make these comparisons by eye (tests/test_plane.py,
-test_gaussian.py, test_energy.py, test_refraction.py, test_single_focus.py); here each one
+and FP32). The reference's own test scripts make these comparisons by eye (tests/test_gaussian.py,
+test_energy.py, test_refraction.py, test_single_focus.py, test_psf.py); here each one
 asserts a bound. The CUDA path is held to the oracle at 1e-4 by the GPU parity tests, so
 these bounds carry over to it."""
 import numpy as np
 import pytest
+from scipy.special import jn
 
 from conftest import rel_l2
 from oracle import bpm_ref, debye_ref
@@ -119,3 +120,45 @@ def test_bpm_carries_the_debye_focus():
         assert rel_l2(np.abs(u) ** 2, np.abs(ex) ** 2) < err / 2, size
         away = bpm_ref.bpm_3d(size, units, lam=lam, n0=n0, u0=u0, precision="fp64")
         assert rel_l2(np.abs(away[-1]) ** 2, np.abs(ex[-1]) ** 2) > .3
+
+
+def _airy(r, lam, NA):
+    v = 2. * np.pi * NA / lam * np.abs(r)
+    safe = np.where(v > 1e-12, v, 1.)
+    return np.where(v > 1e-12, (2 * jn(1, safe) / safe) ** 2, 1.)
+
+
+@pytest.mark.parametrize("NA,n0", [(.1, 1.), (.2, 1.), (.2, 1.3), (.4, 1.)])
+def test_focal_plane_and_the_airy_disk(NA, n0):
+    """The scalar limit of tests/test_psf.py, in the focal plane. The plane kernel
+    (debye_wolf_plane) weights its nodes with sqrt(cos t) sin t, the aperture's area
+    element, and its intensity is the Airy disk (2 J1(v)/v)^2 within 1.2 %. The octant
+    kernel behind psf (debye_wolf) drops sin t (psf_debye.cl:77-78), which weighs the small
+    angles more: its focal plane departs from the Airy disk by 15 % or more. Both are the
+    reference's behaviour and both are kept."""
+    N, dx, lam = 64, .05, .5
+    ex = debye_ref.focus_field_debye_plane((N, N), (dx, dx), z=0., lam=lam, NA=NA, n0=n0)
+    x = -(N // 2) * dx + np.arange(N) * (N * dx) / (N - 1)   # the plane kernel's grid
+    Y, X = np.meshgrid(x, x, indexing="ij")
+    I, th = np.abs(ex) ** 2, _airy(np.hypot(X, Y), lam, NA)
+    assert rel_l2(I, th * (I * th).sum() / (th * th).sum()) < .012       # observed 0.004-0.011
+    u = debye_ref.psf((N, N, 8), (dx, dx, .1), lam, NA, n0=n0)[4]        # focal plane, index N/2
+    xo = dx * (np.arange(N) - N // 2)
+    Yo, Xo = np.meshgrid(xo, xo, indexing="ij")
+    tho = _airy(np.hypot(Xo, Yo), lam, NA)
+    assert rel_l2(u, tho * (u * tho).sum() / (tho * tho).sum()) > .1      # observed 0.14-0.31
+
+
+@pytest.mark.parametrize("n0", [1., 1.3, 1.5])
+def test_axial_profile_scalar_limit(n0):
+    """tests/test_psf.py's axial profile: at NA 0.2 the on-axis intensity of psf follows
+    the scalar paraxial form 16 sin^2(u/4) / u^2, u = 2 pi NA^2 z / (lam n0)."""
+    Nx, Ny, Nz, dx, lam, NA = 64, 64, 256, .05, .5, .2
+    u = debye_ref.psf((Nx, Ny, Nz), (dx,) * 3, lam, NA, n0=n0)
+    prof = u[:, Ny // 2, Nx // 2] / u.max()
+    z = dx * (np.arange(Nz) - Nz // 2)
+    a = 2. * np.pi / lam * NA ** 2 / n0 * z
+    safe = np.where(a != 0, a, 1.)
+    theory = np.where(a != 0, 16. / safe ** 2 * np.sin(safe / 4.) ** 2, 1.)
+    assert np.argmax(u) == np.ravel_multi_index((Nz // 2, Ny // 2, Nx // 2), u.shape)
+    assert np.sqrt(np.mean((prof - theory / theory.max()) ** 2)) < .015   # observed 0.004-0.009
