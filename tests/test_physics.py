@@ -1,6 +1,7 @@
 """Physical checks of the split-step march and the Debye-Wolf field, on the oracle (CPU, FP64
 and FP32). The reference's own test scripts make these comparisons by eye (tests/test_gaussian.py,
-test_energy.py, test_refraction.py, test_single_focus.py, test_psf.py); here each one
+test_energy.py, test_refraction.py, test_single_focus.py, test_psf.py, test_psf_vectorial.py);
+here each one
 asserts a bound. The CUDA path is held to the oracle at 1e-4 by the GPU parity tests, so
 these bounds carry over to it."""
 import numpy as np
@@ -162,3 +163,44 @@ def test_axial_profile_scalar_limit(n0):
     theory = np.where(a != 0, 16. / safe ** 2 * np.sin(safe / 4.) ** 2, 1.)
     assert np.argmax(u) == np.ravel_multi_index((Nz // 2, Ny // 2, Nx // 2), u.shape)
     assert np.sqrt(np.mean((prof - theory / theory.max()) ** 2)) < .015   # observed 0.004-0.009
+
+
+def _debye_trapezoid(x, y, z, k, NA, n_int=4001):
+    """The vectorial Debye integral of an x-polarised aperture (sqrt(cos t) apodisation, area
+    element sin t) by the trapezoid rule on n_int nodes over [0, asin NA], in FP64."""
+    a = np.arcsin(NA)
+    t = np.linspace(0., a, n_int)
+    dt = a / (n_int - 1.)
+    kr = k * np.hypot(x, y)[:, None]
+    phi = np.arctan2(y, x)
+    c, s = np.cos(t), np.sin(t)
+    e = np.exp(1j * k * z[:, None] * c)
+
+    def trap(f):
+        return dt * (f.sum(1) - .5 * (f[:, 0] + f[:, -1]))
+    I0 = trap(np.sqrt(c) * s * (c + 1) * jn(0, kr * s) * e)
+    I1 = trap(np.sqrt(c) * s ** 2 * jn(1, kr * s) * e)
+    I2 = trap(np.sqrt(c) * s * (c - 1) * jn(2, kr * s) * e)
+    return I0 + I2 * np.cos(2 * phi), I2 * np.sin(2 * phi), -2j * I1 * np.cos(phi)
+
+
+@pytest.mark.parametrize("NA", [.5, .95])
+def test_free_points_match_an_independent_quadrature(NA):
+    """tests/test_psf_vectorial.py: the free-point kernel (debye_wolf_at) against the Debye
+    integral evaluated independently on a fine trapezoid grid. Its nodes run one step past
+    the aperture edge (i = 0..INT_STEPS with dt = (a2 - a1) / (INT_STEPS - 1)), so the fields
+    agree to O(1 / INT_STEPS). Its intensity output is |ex|^2 alone, as the reference kernel
+    writes it (psf_debye.cl:266)."""
+    rng = np.random.default_rng(3)
+    x, y = (rng.uniform(-1, 1, 200).astype(np.float32) for _ in range(2))
+    z = rng.uniform(-1.5, 1.5, 200).astype(np.float32)
+    want = _debye_trapezoid(x.astype(np.float64), y.astype(np.float64), z.astype(np.float64),
+                            2 * np.pi / .5, NA)
+    errs = []
+    for steps in (200, 1000):
+        u, ex, ey, ez = debye_ref.focus_field_debye_at(x, y, z, .5, NA, n0=1., n_integration_steps=steps)
+        e = [rel_l2(g, w) for g, w in zip((ex, ey, ez), want)]
+        assert max(e) < 10. / steps, (steps, e)      # observed at most 5 / steps
+        errs.append(max(e))
+        assert np.allclose(u, np.abs(ex) ** 2, rtol=1e-5, atol=0)
+    assert errs[1] < errs[0] / 3
