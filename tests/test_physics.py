@@ -1,9 +1,8 @@
-"""Physical checks of the split-step march and the Debye-Wolf field, on the oracle (CPU, FP64
-and FP32). The reference's own test scripts make these comparisons by eye (tests/test_gaussian.py,
-test_energy.py, test_refraction.py, test_single_focus.py, test_psf.py, test_psf_vectorial.py);
-here each one
-asserts a bound. The CUDA path is held to the oracle at 1e-4 by the GPU parity tests, so
-these bounds carry over to it."""
+"""Physical checks of the split-step march and the Debye-Wolf field, on the oracle (CPU,
+FP64 and FP32). The reference's own test scripts make these comparisons by eye
+(tests/test_gaussian.py, test_energy.py, test_refraction.py, test_single_focus.py,
+test_psf.py, test_psf_vectorial.py); here each one asserts a bound. The CUDA path is held
+to the oracle at 1e-4 by the GPU parity tests, so these bounds carry over to it."""
 import numpy as np
 import pytest
 from scipy.special import jn
