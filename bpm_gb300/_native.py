@@ -33,6 +33,7 @@ PASS_FIRST_ROW, PASS_COLUMN, PASS_COLUMN_REDUCE, PASS_COLUMN_PROPAGATE, PASS_ROW
 
 
 class GridDesc(ctypes.Structure):
+    """bpm_grid_desc of include/bpm_gb300.h: grid, units and physics of a plan."""
     _fields_ = [("nx", c_int), ("ny", c_int), ("nz", c_int),
                 ("dx", c_double), ("dy", c_double), ("dz", c_double),
                 ("lam", c_double), ("n0", c_double),
@@ -41,6 +42,7 @@ class GridDesc(ctypes.Structure):
 
 
 class Request(ctypes.Structure):
+    """bpm_request of include/bpm_gb300.h: the device buffers and options of one march."""
     _fields_ = [("batch", c_int), ("u0", c_vp), ("dn", c_vp), ("dn_dtype", c_int),
                 ("dn_batch_stride", c_ll), ("slice_n", c_vp), ("slice_dn0", c_vp),
                 ("out", c_vp), ("out_kind", c_int), ("out_batch_stride", c_ll),
@@ -50,6 +52,8 @@ class Request(ctypes.Structure):
 
 
 class DebyeDesc(ctypes.Structure):
+    """debye_desc of include/bpm_gb300.h: grid, units, optics and polarisation of a
+    Debye-Wolf field."""
     _fields_ = [("nx", c_int), ("ny", c_int), ("nz", c_int),
                 ("dx", c_double), ("dy", c_double), ("dz", c_double),
                 ("lam", c_double), ("n0", c_double),
@@ -117,6 +121,7 @@ def lib():
 
 
 def last_error():
+    """Text of the calling thread's last library error (bpm_last_error)."""
     return lib().bpm_last_error().decode(errors="replace")
 
 
@@ -135,4 +140,5 @@ def check(rc, what=""):
 
 
 def launch_count():
+    """Kernels this process has launched through the library (bpm_launch_count)."""
     return int(lib().bpm_launch_count())

@@ -22,6 +22,8 @@ _cache = None
 
 
 def cache_path():
+    """The JSON file of measured group sizes: BPM_GB300_TUNE_CACHE, else
+    ~/.cache/bpm_gb300/autotune.json."""
     return os.environ.get("BPM_GB300_TUNE_CACHE",
                           os.path.join(os.path.expanduser("~"), ".cache", "bpm_gb300", "autotune.json"))
 

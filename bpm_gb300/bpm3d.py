@@ -79,7 +79,10 @@ def _ptr(t):
 
 class Plan:
     """A propagation plan: grid, propagator, twiddle, taper and scattering tables on one
-    device (bpm_plan_create)."""
+    device (bpm_plan_create). It holds what the setup of _bpm_3d builds per call
+    (bpm/bpm/bpm_3d.py:140-278: k-grid, propagator and evanescent mask, taper, scattering
+    weights), or for prop_kind PROP_CLASS the class path's host FP64 propagator
+    (bpm/bpmclass/bpm3d.py:64-115)."""
 
     def __init__(self, size, units, lam, n0, absorbing_width=0, mean_mode="weighted",
                  prop_kind=N.PROP_FUNCTIONAL, use_fresnel_approx=False, base=None):
@@ -200,7 +203,10 @@ def mask_pays(batch, Nx, Ny):
 
 def precompute_mask(plan, dn_t, dn_kind):
     """Phase masks (Nz, Ny, Nx) complex64 of a shared dn volume (bpm_mask_precompute): every
-    field then reads them instead of re-evaluating exp(-i k0 dz dn) (see mask_pays)."""
+    field then reads them instead of re-evaluating exp(-i k0 dz dn) (see mask_pays). The
+    mask is the factor the reference's mult_dn* kernels apply per step
+    (bpm/bpm/kernels/bpm_3d_kernels.cl:20-283) without the mean-index shift, which stays
+    per field."""
     Nx, Ny, Nz = plan.size
     mask = torch.empty((Nz, Ny, Nx), dtype=torch.complex64, device=dn_t.device)
     N.check(N.lib().bpm_mask_precompute(plan.handle, _ptr(dn_t), dn_kind, _ptr(mask), _stream_ptr()),
@@ -393,7 +399,8 @@ def _bpm_3d_split(size, units, lam=.5, u0=None, dn=None, n_volumes=1, n0=1., sub
 def bpm_3d_batched(size, units, lam=.5, u0=None, dn=None, n0=1., return_full=True, return_field=True,
                    absorbing_width=0, use_fresnel_approx=False, store_dn_as_half=False,
                    mean_mode="weighted", group=0, out=None):
-    """Batched bpm_3d: u0 of shape (B, Ny, Nx) marches through one shared dn (Nz, Ny, Nx),
+    """Batched bpm_3d (bpm/bpm/bpm_3d.py:39, once per field): u0 of shape (B, Ny, Nx)
+    marches through one shared dn (Nz, Ny, Nx),
     or through per-field dn volumes of shape (B, Nz, Ny, Nx). Each field's result equals
     bpm_3d on that field alone. Returns (B, Nz, Ny, Nx) volumes or (B, Ny, Nx) last planes.
     `out`, if given, is a host buffer of the result's shape and dtype (a numpy array or a

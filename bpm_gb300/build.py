@@ -22,11 +22,14 @@ ARCH = "-gencode=arch=compute_103a,code=sm_103a"
 
 
 def nvcc():
+    """The nvcc of CUDA_HOME (default /usr/local/cuda), else the one on PATH."""
     cand = os.path.join(os.environ.get("CUDA_HOME", "/usr/local/cuda"), "bin", "nvcc")
     return cand if os.path.exists(cand) else "nvcc"
 
 
 def flags():
+    """nvcc flags of every translation unit: sm_103a only, line info for profiles, host
+    code without FP contraction."""
     return [ARCH, "-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC",
             "-Xcompiler", "-ffp-contract=off", "-Xptxas", "-O3"]
 
@@ -50,6 +53,8 @@ def _stale():
 
 
 def build(force=False, verbose=True):
+    """Compile the sources (in parallel) and link libbpm_gb300.so when a source or the
+    header is newer than the library (always with force). Returns the library's path."""
     if not force and not _stale():
         return LIB
     os.makedirs(BUILD, exist_ok=True)

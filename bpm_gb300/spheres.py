@@ -19,8 +19,9 @@ __all__ = ["create_dn_buffer", "bpm_3d_spheres"]
 def create_dn_buffer(size, units, points, dn_inner=.0, rad_inner=0, dn_outer=.1, rad_outer=.4):
     """dn volume (Nz, Ny, Nx) float32 on the device: coated spheres centred at `points`
     ([[x, y, z], ...] in microns), inner radius/index rad_inner/dn_inner, outer
-    rad_outer/dn_outer. Returns a torch CUDA tensor (the reference returns its device
-    buffer, an OCLArray)."""
+    rad_outer/dn_outer (bpm/bpm/bpm_3d_spheres.py:11-38, kernel fill_dn in
+    bpm_3d_spheres.cl:31-74). Returns a torch CUDA tensor (the reference returns its
+    device buffer, an OCLArray)."""
     Nx, Ny, Nz = (int(s) for s in size)
     dx, dy, dz = (float(u) for u in units)
     ps = np.asarray(points, np.float64).reshape(-1, 3)
