@@ -1,7 +1,7 @@
 """Physical checks of the split-step march and the Debye-Wolf field, on the oracle (CPU,
 FP64 and FP32). The reference's own test scripts make these comparisons by eye
 (tests/test_gaussian.py, test_energy.py, test_refraction.py, test_single_focus.py,
-test_psf.py, test_psf_vectorial.py); here each one asserts a bound. The CUDA path is held
+test_focus_reflect.py, test_psf.py, test_psf_vectorial.py); here each one asserts a bound. The CUDA path is held
 to the oracle at 1e-4 by the GPU parity tests, so these bounds carry over to it."""
 import numpy as np
 import pytest
@@ -203,3 +203,28 @@ def test_free_points_match_an_independent_quadrature(NA):
         errs.append(max(e))
         assert np.allclose(u, np.abs(ex) ** 2, rtol=1e-5, atol=0)
     assert errs[1] < errs[0] / 3
+
+
+@pytest.mark.parametrize("precision", ["fp64", "fp32"])
+def test_absorbing_boundary(precision):
+    """tests/test_focus_reflect.py's absorbing layer: the taper 0.5 (1 - cos(pi d / w)) is 0
+    at the grid's edge (d = 0), so every plane after u0 has its outermost ring at exactly 0,
+    and a beam spreading from focus loses energy into the layer instead of wrapping round
+    the periodic grid. Complex dn takes no taper (bpm_3d_kernels.cl:174-195)."""
+    N, Nz, w = 64, 48, 8
+    _, ex, _, _ = debye_ref.focus_field_debye((N, N, 2), (.1, .1, .1), .5, .7, 1., 100)
+    u0 = ex[1].astype(np.complex64)                          # the focal plane
+    kw = dict(lam=.5, n0=1., u0=u0, precision=precision)
+    free = bpm_ref.bpm_3d((N, N, Nz), (.1, .1, .1), dn=np.zeros((Nz, N, N), np.float32), **kw)
+    damp = bpm_ref.bpm_3d((N, N, Nz), (.1, .1, .1), dn=np.zeros((Nz, N, N), np.float32),
+                          absorbing_width=w, **kw)
+    ring = np.ones((N, N), bool)
+    ring[1:-1, 1:-1] = False
+    assert np.all(damp[1:, ring] == 0)
+    E_free = (np.abs(free) ** 2).sum((1, 2))
+    E_damp = (np.abs(damp) ** 2).sum((1, 2))
+    assert np.all(E_damp[1:] <= E_damp[:-1] * (1 + 1e-6))
+    assert E_damp[-1] < .9 * E_free[-1]                      # the spread beam reached the layer
+    cplx = bpm_ref.bpm_3d((N, N, Nz), (.1, .1, .1), dn=np.zeros((Nz, N, N), np.complex64),
+                          absorbing_width=w, mean_mode="ignore", **kw)
+    assert rel_l2(cplx, free) < (1e-12 if precision == "fp64" else 1e-5)
