@@ -33,7 +33,7 @@ import torch
 
 from . import _native as N
 from .bpm3d import _dn_kind, _ptr, get_plan, mask_pays, precompute_mask
-from .psf import _debye
+from .psf import _debye, _desc
 
 __all__ = ["BpmRequest", "PsfRequest", "Server"]
 
@@ -104,6 +104,13 @@ class PsfRequest:
         T = n_na // 2 * (self.n_integration_steps + 1)
         M = (Nx // 2 + 1) * (Ny // 2 + 1)
         ws = 4 * 3 * T * M + 8 * 3 * (Nz // 2 + 1) * M + 8 * T * (Nz // 2 + 1)
+        try:
+            # the library's figure (node, radius and angle tables and row padding included);
+            # 0 for an invalid description, which the launch then reports
+            desc, _na = _desc(self.shape, self.units, self.lam, self.NA, self.n0, self.n_integration_steps)
+            ws = max(ws, int(N.lib().debye_workspace_bytes(ctypes.byref(desc))))
+        except (AssertionError, TypeError, ValueError):
+            pass
         return ws + Nx * Ny * Nz * (28 if self.return_field else 4)
 
 

@@ -100,3 +100,19 @@ def test_autotune_pick_group():
     assert pick_group({4: 7.0, 8: 7.5, 16: 7.6}) == 4
     assert pick_group({8: 5.}) == 8
     assert pick_group({2: 3., 4: 3.09}, tol=.03) == 4
+
+
+def test_psf_request_footprint_covers_the_workspace(native):
+    """The serving loop admits a PSF request by its footprint: never less than the
+    library's workspace plus the outputs; a request the library rejects still gets one."""
+    from bpm_gb300.psf import _desc
+    from bpm_gb300.serve import PsfRequest
+    for shape, NA, steps, field in (((128, 128, 128), .8, 200, True), ((256, 256, 256), 1.1, 512, False),
+                                    ((130, 96, 200), [.2, .5, .6, .9], 100, True), ((16, 16, 16), .5, 20, False)):
+        desc, _na = _desc(shape, (.1, .1, .1), .5, NA, 1.33, steps)
+        ws = native.lib().debye_workspace_bytes(ctypes.byref(desc))
+        out = shape[0] * shape[1] * shape[2] * (28 if field else 4)
+        assert ws > 0
+        assert PsfRequest(shape, (.1, .1, .1), .5, NA, 1.33, steps, return_field=field).footprint() == ws + out
+    assert PsfRequest((15, 16, 16), (.1, .1, .1)).footprint() > 0          # odd shape: rejected at launch
+    assert PsfRequest((16, 16, 16), (.1, .1, .1), NA=[.1, .2, .3]).footprint() > 0
