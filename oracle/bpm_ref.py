@@ -91,7 +91,9 @@ def propagator_f32(n, k0, dx, dy, dz, Nx, Ny):
 
 
 def propagator_f64(n, k0, dx, dy, dz, Nx, Ny):
-    """FP64 flavour: mask from the FP32 recipe at float32(n), phase exp(-i dz kz) in FP64."""
+    """FP64 flavour of compute_propagator (bpm/bpm/kernels/bpm_3d_kernels.cl:408-432) and of
+    the host H0/H of _bpm_3d (bpm/bpm/bpm_3d.py:171-181): mask from the FP32 recipe at
+    float32(n), phase exp(-i dz kz) in FP64."""
     kx32, ky32 = k_axes_f32(Nx, Ny, dx, dy)
     mask = prop_tmp_f32(np.float32(n), np.float32(k0), kx32, ky32) >= 0
     kx = 2 * np.pi * np.fft.fftfreq(Nx, dx)
@@ -123,7 +125,8 @@ def taper_values_f32(absorb):
 
 
 def taper_f32(Nx, Ny, absorb):
-    """(Ny, Nx) float32 taper of the mult_dn* kernels; 1 where dist >= absorb."""
+    """(Ny, Nx) float32 taper of the mult_dn* kernels (bpm_3d_kernels.cl:20-51, :104-136:
+    0.5 (1 - cos(pi d / absorb)) for d < absorb); 1 where dist >= absorb."""
     dist = taper_dist(Nx, Ny)
     vals = taper_values_f32(absorb)
     t = np.ones((Ny, Nx), np.float32)
@@ -134,6 +137,8 @@ def taper_f32(Nx, Ny, absorb):
 
 
 def half_to_f32(dn):
+    """dn stored as float16 and read back as float32, as store_dn_as_half does
+    (bpm/bpm/bpm_3d.py:208-209; the *_half kernels, bpm_3d_kernels.cl:52-81, :139-171)."""
     return np.asarray(dn, dtype=np.float16).astype(np.float32)
 
 

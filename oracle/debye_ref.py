@@ -65,7 +65,8 @@ def quadrature_nodes(alphas, int_steps):
 
 
 def debye_octant(params, int_steps, Ex0=1., Ey0=0.):
-    """FP64 evaluation of debye_wolf over the octant. Returns (u, ex, ey, ez) of shape
+    """FP64 evaluation of debye_wolf (bpm/psf/kernels/psf_debye.cl:24-113) over the octant,
+    node weights as its :62-78. Returns (u, ex, ey, ez) of shape
     (Nz, Ny, Nx) in float64/complex128."""
     Nx, Ny, Nz = params["Nx"], params["Ny"], params["Nz"]
     x = coord_f32(Nx, params["x2"]).astype(np.float64)
@@ -124,13 +125,15 @@ def mirror_octant(shape, u, ex, ey, ez, real_dtype=np.float32, complex_dtype=np.
 
 
 def mirror_index(N0):
-    """Index form of the same spreading along one axis: full index m -> octant |m - N0/2|."""
+    """Index form of the same spreading along one axis (_focus_fields_debye.py:116-144):
+    full index m -> octant |m - N0/2|."""
     return np.abs(np.arange(N0) - N0 // 2)
 
 
 def focus_field_debye(shape, units, lam, NA, n0=1., n_integration_steps=200,
                       real_dtype=np.float32, complex_dtype=np.complex64):
-    """FP64 restatement of focus_field_debye; returns (u, ex, ey, ez) on (Nz0, Ny0, Nx0)."""
+    """FP64 restatement of focus_field_debye (bpm/psf/_focus_fields_debye.py:48-146);
+    returns (u, ex, ey, ez) on (Nz0, Ny0, Nx0)."""
     params = octant_params(shape, units, lam, NA, n0)
     oct_ = debye_octant(params, n_integration_steps)
     return mirror_octant(shape, *oct_, real_dtype=real_dtype, complex_dtype=complex_dtype)
@@ -165,8 +168,9 @@ def _assemble(I0, I1, I2, phi, Ex0, Ey0):
 
 
 def _integrals_points(kr, kz, t, pre):
-    """I_n at arbitrary points (kr, kz): (P,) arrays; pre: (T,) weights without the
-    component factors. FP64."""
+    """I_n at arbitrary points (kr, kz), the node sums of debye_wolf_plane and debye_wolf_at
+    (psf_debye.cl:117-269): (P,) arrays; pre: (T,) weights without the component factors.
+    FP64."""
     co, si = np.cos(t), np.sin(t)
     arg = kr[:, None] * si[None, :]
     E = np.exp(1j * kz[:, None] * co[None, :])
@@ -232,7 +236,8 @@ def mirror_octant_gauss(shape, u, ex, ey, ez, real_dtype=np.float32, complex_dty
 
 
 def mirror_index_gauss(N0):
-    """Index form of mirror_octant_gauss along one axis: full index p -> octant index."""
+    """Index form of mirror_octant_gauss along one axis (_focus_fields_debye.py:426-438):
+    full index p -> octant index."""
     N = (N0 + 1) // 2
     p = np.arange(N0)
     return np.where(p >= N0 - N, p - (N0 - N), N - 1 - p)

@@ -10,6 +10,9 @@ import numpy as np
 
 
 def create_dn_buffer(size, units, points, dn_inner=.0, rad_inner=0, dn_outer=.1, rad_outer=.4):
+    """Restatement of create_dn_buffer (bpm/bpm/bpm_3d_spheres.py:11-38) and its kernel
+    fill_dn (bpm/bpm/kernels/bpm_3d_spheres.cl:31-74), float32 with every operation rounded
+    as the kernel writes it. Returns (Nz, Ny, Nx) float32."""
     Nx, Ny, Nz = size
     f = np.float32
     dx, dy, dz = (f(u) for u in units)

@@ -189,7 +189,7 @@ def test_free_points_match_an_independent_quadrature(NA):
     integral evaluated independently on a fine trapezoid grid. Its nodes run one step past
     the aperture edge (i = 0..INT_STEPS with dt = (a2 - a1) / (INT_STEPS - 1)), so the fields
     agree to O(1 / INT_STEPS). Its intensity output is |ex|^2 alone, as the reference kernel
-    writes it (psf_debye.cl:266)."""
+    writes it (psf_debye.cl:267)."""
     rng = np.random.default_rng(3)
     x, y = (rng.uniform(-1, 1, 200).astype(np.float32) for _ in range(2))
     z = rng.uniform(-1.5, 1.5, 200).astype(np.float32)
