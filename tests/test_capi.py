@@ -116,3 +116,35 @@ def test_psf_request_footprint_covers_the_workspace(native):
         assert PsfRequest(shape, (.1, .1, .1), .5, NA, 1.33, steps, return_field=field).footprint() == ws + out
     assert PsfRequest((15, 16, 16), (.1, .1, .1)).footprint() > 0          # odd shape: rejected at launch
     assert PsfRequest((16, 16, 16), (.1, .1, .1), NA=[.1, .2, .3]).footprint() > 0
+
+
+def test_mask_policy():
+    """Phase masks are precomputed for several fields through one dn, and for one field
+    from 512 x 512 points up."""
+    from bpm_gb300.bpm3d import mask_pays
+    assert mask_pays(2, 64, 32) and mask_pays(64, 512, 512)
+    assert mask_pays(1, 512, 512) and mask_pays(1, 1024, 256) and mask_pays(1, 1024, 1024)
+    assert not mask_pays(1, 256, 256) and not mask_pays(1, 512, 256) and not mask_pays(1, 16, 16)
+
+
+def test_serve_request_keys_and_footprint():
+    """Requests merge into one launch when grid, physics, dn kind and output form agree
+    (each field may bring its own dn); the admission footprint counts u0, last plane and
+    workspace plane, the dn volume, its phase masks and the output volume."""
+    import numpy as np
+    from bpm_gb300.serve import BpmRequest
+    size, units = (64, 32, 8), (.1, .1, .1)
+    dn = np.zeros((8, 32, 64), np.float32)
+    a = BpmRequest(size, units, dn=dn)
+    assert a.key() == BpmRequest(size, units, dn=dn.copy()).key()
+    for other in (BpmRequest(size, units, lam=.6, dn=dn), BpmRequest(size, units, n0=1.33, dn=dn),
+                  BpmRequest(size, units, dn=dn.astype(np.complex64)), BpmRequest(size, units),
+                  BpmRequest(size, units, dn=dn, mean_mode="ignore"), BpmRequest(size, units, dn=dn, return_field=True),
+                  BpmRequest((64, 32, 9), units, dn=np.zeros((9, 32, 64), np.float32))):
+        assert other.key() != a.key()
+    plane = 64 * 32
+    assert a.voxel_updates() == plane * 7
+    assert a.footprint() == plane * 8 * 3 + 8 * plane * 4 + 8 * plane * 8 + 8 * plane * 4
+    assert BpmRequest(size, units, dn=dn.astype(np.complex64)).footprint() - a.footprint() == 8 * plane * 4
+    assert BpmRequest(size, units, dn=dn, return_field=True).footprint() - a.footprint() == 8 * plane * 4
+    assert BpmRequest(size, units, return_full=False).footprint() == plane * 8 * 3
