@@ -99,6 +99,13 @@ class PsfRequest:
         return 0
 
     def footprint(self):
+        # computed once: the scheduler asks at submission and again at admission
+        fp = self.__dict__.get("_footprint")
+        if fp is None:
+            fp = self.__dict__["_footprint"] = self._footprint()
+        return fp
+
+    def _footprint(self):
         Nx, Ny, Nz = self.shape
         n_na = 2 if np.isscalar(self.NA) else len(self.NA)
         T = n_na // 2 * (self.n_integration_steps + 1)
