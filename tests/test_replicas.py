@@ -96,3 +96,19 @@ def test_sharded_gradient_equals_single_process():
     g_full = grad_for(slice(0, u0.shape[0]), dn, u0, target, H, k0).numpy()
     assert t == 2.0
     assert np.allclose(g_sharded, g_full, rtol=1e-10, atol=1e-14)
+
+
+def test_torch_restatement_matches_the_oracle():
+    """The FP64 torch march differentiated above is the oracle's ignore-mode march (the
+    reference's mult_propagator + mult_dn step, no taper): same last plane to rounding."""
+    from oracle import bpm_ref
+    dn, u0, _, H, k0 = problem()
+    Nz, Ny, Nx = dn.shape
+    dn32 = dn.astype(np.float32)
+    for b in range(u0.shape[0]):
+        f0 = u0[b].astype(np.complex64)
+        got = march64(torch.tensor(dn32.astype(np.float64)), torch.tensor(f0.astype(np.complex128)), .1, k0,
+                      torch.tensor(H)).numpy()
+        want = bpm_ref.bpm_3d((Nx, Ny, Nz), (.1, .1, .1), lam=.5, n0=1.33, u0=f0, dn=dn32, mean_mode="ignore",
+                              return_full=False, precision="fp64")
+        assert np.linalg.norm(got - want) / np.linalg.norm(want) < 1e-6, b
