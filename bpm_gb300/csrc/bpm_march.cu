@@ -2563,6 +2563,17 @@ extern "C" int bpm_propagate_noalloc(bpm_plan* pl, const bpm_request* r, void* s
   if (!pl) { set_error("plan is NULL"); return BPM_ERR_ARG; }
   int rc = check_request(pl, r);
   if (rc) return rc;
+  // the scratch array is looked up on the current device, and the plan's tables and
+  // streams live on the device it was created on: the two must be the same
+  {
+    int dev = -1;
+    BPM_CUDA_TRY(cudaGetDevice(&dev));
+    if (dev != pl->device) {
+      set_error("bpm_propagate_noalloc: the plan belongs to device " + std::to_string(pl->device) +
+                " but device " + std::to_string(dev) + " is current; make the plan's device current");
+      return BPM_ERR_ARG;
+    }
+  }
   // march as many fields together as the fixed scratch holds (the result does not depend
   // on the grouping); refuse grids whose single-field scratch does not fit
   int G = group_size(pl, r);

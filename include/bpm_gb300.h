@@ -178,10 +178,12 @@ int bpm_propagate_to_host(bpm_plan* plan, const bpm_request* req, void* host_out
  * scratch is one fixed array of BPM_NOALLOC_SCRATCH_BYTES inside the library's device
  * image, held by every GPU that loads the library until the process exits. It allocates
  * nothing: no cudaMalloc, no cudaFree, no allocating library call. Fields are marched in
- * as many groups as the array needs; a grid whose one-field scratch exceeds the array
- * (grids larger than 512x512) is refused with BPM_ERR_OOM and a message naming the limit.
- * The first call on a device looks up the array's device address (with that device
- * current) and caches it; make that first call before any stream capture. All calls
+ * as many groups as the array needs. The limit is an area: one field's scratch, its plane
+ * of nx*ny*8 bytes plus under 1 KiB of per-tile partial sums, must fit the array, so
+ * nx*ny must stay below 2^20: every supported grid but 1024x1024 (1024x512 is accepted);
+ * 1024x1024 is refused with BPM_ERR_OOM and a message naming the limit. The plan's device must be the current device (else
+ * BPM_ERR_ARG). The first call on a device looks up the array's device address (with
+ * that device current) and caches it; make that first call before any stream capture. All calls
  * share the one array: calls that can overlap on the GPU (different streams or threads)
  * race on it and must be serialised by the caller. Every byte of the array a call reads
  * was written earlier in the same call, so nothing needs clearing between calls.

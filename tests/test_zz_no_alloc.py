@@ -1,8 +1,10 @@
 """bpm_propagate_noalloc, the march for callers that may not allocate device memory (a host
 with a fixed device budget, a plugin whose host owns all allocations, a loop where a
-synchronising cudaMalloc would stall other streams): through the C ABI, its results match
-bpm_propagate's with a caller workspace, on two calls in a row (the shared scratch keeps
-the previous call's contents), and grids too large for its fixed scratch are refused.
+synchronising cudaMalloc would stall other streams): through the C ABI, its results equal
+bpm_propagate's with a caller workspace bit for bit (the march's result does not depend
+on how its fields are grouped), on two calls in a row (the shared scratch keeps the
+previous call's contents), the second call leaves the device's free memory unchanged, and
+grids too large for its fixed scratch are refused.
 
 This file is named to be collected last, so a run that stops at the first failure has
 already run every other test."""
@@ -11,11 +13,7 @@ import ctypes
 import numpy as np
 import pytest
 
-from conftest import rel_l2
-
 pytestmark = pytest.mark.gpu
-
-TOL = 1e-4
 
 
 @pytest.fixture(scope="module")
@@ -38,8 +36,10 @@ def inputs(torch, size, batch, seed):
     return u0, dn
 
 
-def run(torch, N, plan, u0, dn, out_kind, noalloc, tabs=(None, None)):
-    """One march through the C ABI; returns (status, output volume, exit planes)."""
+def run(torch, N, plan, u0, dn, out_kind, noalloc, tabs=(None, None), group=0, free_bytes=None):
+    """One march through the C ABI; returns (status, output volume, exit planes). With
+    `free_bytes` (a list), the device's free memory just before and just after the call is
+    appended to it."""
     Nx, Ny, Nz = plan.size
     B = u0.shape[0]
 
@@ -49,11 +49,17 @@ def run(torch, N, plan, u0, dn, out_kind, noalloc, tabs=(None, None)):
     out = torch.full((B, Nz, Ny, Nx), float("nan"), dtype=dt, device="cuda")
     last = torch.full((B, Ny, Nx), float("nan"), dtype=torch.complex64, device="cuda")
     req = N.Request(B, p(u0), p(dn), N.DN_F32, 0, p(tabs[0]), p(tabs[1]), p(out), out_kind, Nz * Ny * Nx,
-                    p(last), None, None, 0, 0)
+                    p(last), None, None, 0, group)
     stream = ctypes.c_void_p(torch.cuda.current_stream().cuda_stream)
     L = N.lib()
     if noalloc:
+        torch.cuda.synchronize()
+        if free_bytes is not None:
+            free_bytes.append(torch.cuda.mem_get_info()[0])
         rc = L.bpm_propagate_noalloc(plan.handle, ctypes.byref(req), stream)
+        torch.cuda.synchronize()
+        if free_bytes is not None:
+            free_bytes.append(torch.cuda.mem_get_info()[0])
     else:
         wsb = plan.workspace_bytes(B, 0)
         ws = torch.empty(wsb, dtype=torch.uint8, device="cuda")
@@ -62,12 +68,14 @@ def run(torch, N, plan, u0, dn, out_kind, noalloc, tabs=(None, None)):
     return rc, out.cpu().numpy(), last.cpu().numpy()
 
 
-@pytest.mark.parametrize("size,batch,mode,out_kind", [
-    ((256, 128, 12), 5, "weighted", "intensity"),   # all fields in one group
-    ((512, 512, 8), 4, "ignore", "field"),          # the scratch holds 3 fields: two groups
-    ((64, 128, 20), 3, "simple", "intensity"),
+@pytest.mark.parametrize("size,batch,group,mode,out_kind", [
+    ((256, 128, 12), 5, 0, "weighted", "intensity"),   # all fields in one group
+    ((512, 512, 8), 4, 0, "ignore", "field"),          # the scratch holds 3 fields: two groups
+    ((64, 128, 20), 3, 0, "simple", "intensity"),
+    ((256, 256, 10), 16, 4, "weighted", "intensity"),  # 3 groups of 4 march at once in the array
+    ((1024, 512, 5), 2, 0, "ignore", "field"),         # above 512x512: 4 MiB of plane per field
 ])
-def test_noalloc_matches_workspace_march_twice(env, size, batch, mode, out_kind):
+def test_noalloc_matches_workspace_march_twice(env, size, batch, group, mode, out_kind):
     torch, N, Plan, slice_tables = env
     plan = Plan(size, (.1, .1, .1), .5, 1.33, absorbing_width=3, mean_mode=mode)
     u0, dn = inputs(torch, size, batch, 0)
@@ -75,12 +83,15 @@ def test_noalloc_matches_workspace_march_twice(env, size, batch, mode, out_kind)
     tabs = slice_tables(dn, 1.33, torch.device("cuda")) if mode == "simple" else (None, None)
     ref = run(torch, N, plan, u0, dn, ok, False, tabs)
     assert ref[0] == 0
-    for _ in range(2):
-        rc, out, last = run(torch, N, plan, u0, dn, ok, True, tabs)
+    free = []
+    for k in range(2):
+        rc, out, last = run(torch, N, plan, u0, dn, ok, True, tabs, group=group, free_bytes=free if k else None)
         assert rc == 0, N.last_error()
         assert np.all(np.isfinite(out)) and np.all(np.isfinite(last))
-        assert rel_l2(out, ref[1]) <= TOL
-        assert rel_l2(last, ref[2]) <= TOL
+        assert np.array_equal(out, ref[1])
+        assert np.array_equal(last, ref[2])
+    # the second call allocated nothing on the device
+    assert free[0] == free[1], free
 
 
 def test_noalloc_refuses_grids_beyond_its_scratch(env):
