@@ -200,6 +200,11 @@ def bench_ours(args, rank, world, local_rank):
         barrier()
     launches = bpm_gb300.launch_count() - l0
     t_ms = ev0.elapsed_time(ev1) / args.steps
+    # field 0 of the last timed step, its input and the dn volume, for the FP64 parity check
+    check = None
+    if rank == 0 and not args.no_cpu_baseline:
+        check = {"u0": u0[0].cpu().numpy(), "dn": dn.cpu().numpy(), "vol": march.out[0].cpu().numpy(),
+                 "last": march.last[0].cpu().numpy()}
     if world > 1:
         t = torch.tensor([t_ms], device=dev)
         torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
@@ -340,7 +345,7 @@ def bench_ours(args, rank, world, local_rank):
                               "note": "FFT flops counted as 5 N log2 N per 1-D transform"}},
         "clocks": clocks,
     }
-    return res
+    return res, check
 
 
 def psf_timing(reps=20, cpu=False):
@@ -460,8 +465,10 @@ def adjoint_timing():
     torch.cuda.synchronize()
     t = a.elapsed_time(b) / 3
     vu = 16 * 256 * 256 * 127
+    case = {"dn": dn.detach(), "u0": u0, "target": target, "grad": dn.grad.detach().clone(), "size": size,
+            "units": units}
     return {"workload": "config 4: 256x256x128, 16 angles, ckpt 16, forward + adjoint", "ms": t,
-            "forward_voxel_updates_per_s_equiv": vu / (t * 1e-3)}
+            "forward_voxel_updates_per_s_equiv": vu / (t * 1e-3)}, case
 
 
 def sphere_pool(side, nz, seed, n=50):
@@ -706,6 +713,42 @@ def cpu_sample(fields=1, steps=48):
         fields, NX, NY, steps, MODE)
 
 
+def parity_vs_fp64(check):
+    """Relative L2 of the timed march's field 0 (|u|^2 volume over all 256 planes, and the
+    exit field) against the oracle's FP64 march of the same input through the same dn."""
+    from oracle import bpm_ref
+    t0 = time.perf_counter()
+    vol, last = bpm_ref._bpm_3d((NX, NY, NZ), UNITS, lam=LAM, n0=N0, u0=check["u0"], dn=check["dn"],
+                                mean_mode=MODE, return_field=False, return_last_plane=True, precision="fp64",
+                                workers=host_cores())
+    num = den = 0.
+    for z in range(NZ):
+        d = check["vol"][z].astype(np.float64) - vol[z]
+        num += float(np.vdot(d, d).real)
+        den += float(np.vdot(vol[z], vol[z]).real)
+    dl = check["last"].astype(np.complex128) - last
+    return {"field": 0, "rel_l2_intensity_volume": (num / den) ** .5,
+            "rel_l2_exit_field": float(np.linalg.norm(dl) / np.linalg.norm(last)),
+            "against": "oracle FP64 march (numpy/scipy) of the same u0 and dn, all %d planes" % NZ,
+            "oracle_s": time.perf_counter() - t0}
+
+
+def adjoint_grad_check(case):
+    """Relative L2 of the timed adjoint's d(loss)/d(dn) against FP64 torch autograd through
+    the oracle's restatement of the ignore-mode march (same dn, illuminations, target)."""
+    import torch
+    from oracle import torch_ref
+    dn64 = case["dn"].double().requires_grad_(True)
+    ref = torch_ref.march_exit_fp64(torch, dn64, case["u0"].to(torch.complex128), case["size"], case["units"],
+                                    LAM, N0)
+    ((ref.abs() ** 2 - case["target"].double()) ** 2).sum().backward()
+    g, r = case["grad"].double(), dn64.grad
+    e = float(torch.linalg.vector_norm(g - r) / torch.linalg.vector_norm(r))
+    del dn64, ref
+    torch.cuda.empty_cache()
+    return e
+
+
 def bench_reference(args, rank):
     if rank != 0:
         return None
@@ -730,6 +773,44 @@ def bench_reference(args, rank):
             "e2e": {"value": v, "unit": "voxel-updates/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
 
 
+def launch_ranks(n, argv):
+    """Re-run this script as n ranks on this node (torch.distributed.run, one process per
+    GPU, rendezvous on 127.0.0.1); rank 0 prints the JSON line. Returns the launcher's exit
+    status."""
+    import socket
+    with socket.socket() as so:
+        so.bind(("127.0.0.1", 0))
+        port = so.getsockname()[1]
+    cmd = [sys.executable, "-m", "torch.distributed.run", "--nnodes=1", "--nproc-per-node=%d" % n,
+           "--master-addr=127.0.0.1", "--master-port=%d" % port, os.path.abspath(__file__), *argv]
+    return subprocess.call(cmd)
+
+
+def rank_census():
+    """Number of ranks in the initialised process group that reach this point (a sum of
+    ones over every rank)."""
+    import torch
+    dev = torch.device("cuda", torch.cuda.current_device()) if torch.distributed.get_backend() == "nccl" \
+        else torch.device("cpu")
+    t = torch.ones(1, device=dev)
+    torch.distributed.all_reduce(t)
+    return int(t.item())
+
+
+def print_rank_census(world, rank):
+    """--check-launch: every rank joins a CPU (gloo) process group and rank 0 prints how
+    many ranks reached the benchmark's entry, with no GPU work."""
+    import torch
+    n = 1
+    if world > 1:
+        torch.distributed.init_process_group("gloo")
+        n = rank_census()
+    if rank == 0:
+        print(json.dumps({"check_launch": True, "ranks": n, "world_size": world}))
+    if world > 1:
+        torch.distributed.destroy_process_group()
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -746,6 +827,8 @@ def main():
     ap.add_argument("--profile-case", default="batched", choices=["batched", "config1", "kernels"],
                     help="with --profile: the batched march, one 128^3 weighted request per step, or one "
                          "small call of every other kernel family")
+    ap.add_argument("--check-launch", action="store_true",
+                    help="only start the ranks and report how many joined (no GPU work)")
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3
@@ -755,9 +838,17 @@ def main():
         profile_run(args)
         return
 
+    if args.gpus > 1 and "WORLD_SIZE" not in os.environ:
+        # --gpus N without an external launcher: start the N ranks here
+        sys.exit(launch_ranks(args.gpus, sys.argv[1:]))
+
     world = env_int("WORLD_SIZE", 1)
     rank = env_int("RANK", 0)
     local_rank = env_int("LOCAL_RANK", 0)
+
+    if args.check_launch:
+        print_rank_census(world, rank)
+        return
 
     if args.impl == "reference":
         res = bench_reference(args, rank)
@@ -767,17 +858,27 @@ def main():
 
     if world > 1:
         import torch
+        if torch.cuda.device_count() < world:
+            raise SystemExit("bench.py: %d ranks but %d visible GPUs" % (world, torch.cuda.device_count()))
         torch.cuda.set_device(local_rank)
         torch.distributed.init_process_group("nccl")
-    res = bench_ours(args, rank, world, local_rank)
+        # n_gpus counts the ranks that joined the job, not the requested number
+        world = rank_census()
+    res, check = bench_ours(args, rank, world, local_rank)
     if rank == 0:
         if not args.no_serve:
             res["serve"] = serve_trace()
         res["psf"] = psf_timing(cpu=not args.no_cpu_baseline)
         res["mixed_batch"] = mixed_batch_timing()
         res["single_requests"] = single_request_timing()
-        res["adjoint"] = adjoint_timing()
+        res["adjoint"], adj_case = adjoint_timing()
         if not args.no_cpu_baseline:
+            # the oracle as the checker: the timed results against FP64, and the CPU baseline
+            res["adjoint"]["grad_rel_l2_vs_fp64"] = adjoint_grad_check(adj_case)
+            del adj_case
+            res["parity"] = parity_vs_fp64(check)
+            res["rel_l2_vs_fp64"] = res["parity"]["rel_l2_intensity_volume"]
+            del check
             v, t, sample = cpu_sample(4, NZ - 1)
             res["cpu_baseline"] = {"value": v, "unit": "voxel-updates/s", "cores": host_cores(), "kind": "port",
                                    "sample": sample + ", %.1f s" % t}

@@ -12,6 +12,8 @@ Modules:
   debye_ref  -- numpy restatement of focus_field_debye / psf / psf_u0
                 (bpm/psf/_focus_fields_debye.py, bpm/psf/kernels/psf_debye.cl,
                 bpm/psf/psf_functions.py) in FP64 with scipy Bessel functions.
+  torch_ref  -- FP64 torch restatement of the ignore-mode march (autograd reference
+                for the adjoint's gradient).
   reflib     -- ctypes loader for oracle/_ref/libref_cl.so, the reference's own
                 OpenCL kernel sources compiled as host C++ (built by oracle/Makefile
                 where the reference checkout exists; absent elsewhere).

@@ -6,7 +6,7 @@ import numpy as np
 import pytest
 
 from conftest import rel_l2
-from oracle import bpm_ref
+from oracle import bpm_ref, torch_ref
 
 pytestmark = pytest.mark.gpu
 
@@ -45,17 +45,7 @@ def tilted_waves(B, Nx, Ny, dx, lam, na_max, seed):
 
 def torch_march64(torch, dn, u0, size, units, lam, n0, absorbing_width=0):
     """FP64 torch restatement of the ignore-mode march (FP32-recipe mask, FP64 phase)."""
-    Nx, Ny, Nz = size
-    dx, dy, dz = units
-    k0 = 2 * np.pi / lam
-    H, _ = bpm_ref.propagator_f64(n0, k0, dx, dy, dz, Nx, Ny)
-    H = torch.as_tensor(H, device=dn.device)
-    T = torch.as_tensor(bpm_ref.taper_f32(Nx, Ny, absorbing_width).astype(np.float64), device=dn.device)
-    u = u0
-    for i in range(Nz - 1):
-        u = torch.fft.ifft2(torch.fft.fft2(u) * H)
-        u = u * torch.exp(-1j * (k0 * dz) * dn[i + 1]) * T
-    return u
+    return torch_ref.march_exit_fp64(torch, dn, u0, size, units, lam, n0, absorbing_width)
 
 
 def test_gradient_vs_fp64_finite_differences(torch_bpm):
@@ -143,7 +133,9 @@ def test_checkpoint_spacing_does_not_change_the_gradient(torch_bpm):
 def test_config4_inversion_gradient(torch_bpm):
     """256x256x128 grid, 16 illumination angles within NA 0.6, checkpoints every 16
     slices; I_target from a ground-truth dn of 20 spheres (dn 0.01-0.04). The gradient at
-    dn = 0 against FP64 torch autograd of the restated march."""
+    an inversion iterate dn = 0.5 dn_true (the march through the spheres scatters, so every
+    mask derivative sees a scattered field) against FP64 torch autograd of the restated
+    march, relative L2 <= 1e-4."""
     torch, bpm, propagate_exit = torch_bpm
     size, units, lam, n0 = (256, 256, 128), (.1, .1, .1), .5, 1.33
     Nx, Ny, Nz = size
@@ -151,12 +143,13 @@ def test_config4_inversion_gradient(torch_bpm):
     dn_true = torch.tensor(spheres(Nx, Ny, Nz, 20, 12, rmin=3, rmax=15), dtype=torch.float32, device="cuda")
     with torch.no_grad():
         I_t = propagate_exit(dn_true, u0, size, units, lam, n0).abs() ** 2
-    dn = torch.zeros_like(dn_true, requires_grad=True)
+    dn = (.5 * dn_true).requires_grad_(True)
     out = propagate_exit(dn, u0, size, units, lam, n0, ckpt_every=16)
     L = ((out.abs() ** 2 - I_t) ** 2).sum()
     L.backward()
-    dn64 = torch.zeros(dn.shape, dtype=torch.float64, device="cuda", requires_grad=True)
+    dn64 = (.5 * dn_true).double().requires_grad_(True)
     ref = torch_march64(torch, dn64, u0.to(torch.complex128), size, units, lam, n0)
     ((ref.abs() ** 2 - I_t.double()) ** 2).sum().backward()
     err = rel_l2(dn.grad.cpu().numpy(), dn64.grad.cpu().numpy())
-    assert err < 1e-3, err
+    print("config 4 gradient at 0.5 dn_true: rel-L2 %.3e against FP64 autograd" % err)
+    assert err < 1e-4, err

@@ -103,3 +103,17 @@ def test_reference_arm_line(bench, monkeypatch):
     assert line["cpu_baseline"]["value"] == line["value"] and line["cpu_baseline"]["kind"] == "port"
     assert line["e2e"] == {"value": 2.5e7, "unit": "voxel-updates/s", "h2d_bytes_per_step": 0,
                            "d2h_bytes_per_step": 0}
+
+
+def test_gpus_flag_launches_the_ranks():
+    """bench.py --gpus 2 with no external launcher starts two ranks itself (one process each,
+    rendezvous on 127.0.0.1); --check-launch makes every rank join a gloo group and rank 0
+    report how many arrived, with no GPU work."""
+    import subprocess
+    import sys
+    r = subprocess.run([sys.executable, os.path.join(ROOT, "bench.py"), "--gpus", "2", "--check-launch"],
+                       capture_output=True, text=True, timeout=600)
+    assert r.returncode == 0, r.stderr[-2000:]
+    lines = [ln for ln in r.stdout.splitlines() if ln.startswith("{")]
+    assert len(lines) == 1, r.stdout
+    assert json.loads(lines[0]) == {"check_launch": True, "ranks": 2, "world_size": 2}
