@@ -110,12 +110,15 @@ class PsfRequest:
         n_na = 2 if np.isscalar(self.NA) else len(self.NA)
         T = n_na // 2 * (self.n_integration_steps + 1)
         M = (Nx // 2 + 1) * (Ny // 2 + 1)
+        # an upper estimate of the tables (Bessel rows, phases, integrals), used when the
+        # library rejects the description (the launch then reports the error)
         ws = 4 * 3 * T * M + 8 * 3 * (Nz // 2 + 1) * M + 8 * T * (Nz // 2 + 1)
         try:
-            # the library's figure (node, radius and angle tables and row padding included);
-            # 0 for an invalid description, which the launch then reports
+            # the library's exact figure (node, radius and angle tables and row padding)
             desc, _na = _desc(self.shape, self.units, self.lam, self.NA, self.n0, self.n_integration_steps)
-            ws = max(ws, int(N.lib().debye_workspace_bytes(ctypes.byref(desc))))
+            exact = int(N.lib().debye_workspace_bytes(ctypes.byref(desc)))
+            if exact > 0:
+                ws = exact
         except (AssertionError, TypeError, ValueError):
             pass
         return ws + Nx * Ny * Nz * (28 if self.return_field else 4)
@@ -133,6 +136,7 @@ class _Entry:
 class _Launch:
     entries: list
     stream: torch.cuda.Stream
+    start: torch.cuda.Event
     done: torch.cuda.Event
     footprint: int
     keep: list = field(default_factory=list)
@@ -163,6 +167,15 @@ class Server:
         self.completed = 0
         self.voxel_updates = 0
         self.peak_used = 0
+        # what the scheduler did: launches, launches that merged several requests, the most
+        # launches in flight at once, and each retired launch's device interval (ms after
+        # the server started), measured by CUDA events on the launch's stream
+        self.launches = 0
+        self.merged_launches = 0
+        self.max_inflight_seen = 0
+        self.spans = []
+        self._t0 = torch.cuda.Event(enable_timing=True)
+        self._t0.record(torch.cuda.current_stream(self.device))
         self.error = None
         self._thread = threading.Thread(target=self._loop, name="bpm-serve", daemon=True)
         self._thread.start()
@@ -189,7 +202,9 @@ class Server:
                 "p99_ms": float(np.percentile(lat, 99)) if len(lat) else None,
                 "mean_ms": float(lat.mean()) if len(lat) else None,
                 "voxel_updates": int(self.voxel_updates), "peak_hbm_bytes": int(self.peak_used),
-                "budget_bytes": self.budget}
+                "budget_bytes": self.budget, "launches": self.launches,
+                "merged_launches": self.merged_launches, "max_inflight_seen": self.max_inflight_seen,
+                "overlapped_launches": overlapped(self.spans)}
 
     # ---------------------------------------------------------------------------------
     def _loop(self):
@@ -234,6 +249,7 @@ class Server:
                     if en.req.host:
                         res = _to_host(res)
                     en.fut.set_result(res)
+                self.spans.append((self._t0.elapsed_time(la.start), self._t0.elapsed_time(la.done)))
                 self._used -= la.footprint
                 self._free_streams.append(la.stream)
                 la.keep.clear()
@@ -264,9 +280,10 @@ class Server:
     def _launch(self, group):
         stream = self._free_streams.pop()
         fp = sum(en.req.footprint() for en in group)
-        la = _Launch(group, stream, torch.cuda.Event(), fp)
+        la = _Launch(group, stream, torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True), fp)
         try:
             with torch.cuda.stream(stream):
+                la.start.record(stream)
                 if isinstance(group[0].req, BpmRequest):
                     la.results = self._run_bpm([en.req for en in group], la, stream)
                 else:
@@ -284,6 +301,9 @@ class Server:
         self._used += fp
         self.peak_used = max(self.peak_used, self._used)
         self._inflight.append(la)
+        self.launches += 1
+        self.merged_launches += len(group) > 1
+        self.max_inflight_seen = max(self.max_inflight_seen, len(self._inflight))
 
     def _run_bpm(self, reqs, la, stream):
         r0 = reqs[0]
@@ -330,6 +350,20 @@ class Server:
         if r0.return_full:
             return [out[i] for i in range(B)]
         return [last[i] if r0.return_field else (last[i].abs() ** 2) for i in range(B)]
+
+
+def overlapped(spans):
+    """How many of the device intervals (start, end) overlap at least one other."""
+    order = sorted(range(len(spans)), key=lambda i: spans[i][0])
+    hit = [False] * len(spans)
+    end, who = float("-inf"), -1
+    for i in order:
+        s, e = spans[i]
+        if s < end:
+            hit[i] = hit[who] = True
+        if e > end:
+            end, who = e, i
+    return sum(hit)
 
 
 def _device_volume(v, dtype, shape, dev):

@@ -148,3 +148,12 @@ def test_serve_request_keys_and_footprint():
     assert BpmRequest(size, units, dn=dn.astype(np.complex64)).footprint() - a.footprint() == 8 * plane * 4
     assert BpmRequest(size, units, dn=dn, return_field=True).footprint() - a.footprint() == 8 * plane * 4
     assert BpmRequest(size, units, return_full=False).footprint() == plane * 8 * 3
+
+
+def test_serve_overlap_count():
+    """The server's count of launches whose device intervals overlap another's."""
+    from bpm_gb300.serve import overlapped
+    assert overlapped([]) == 0
+    assert overlapped([(0., 1.), (1., 2.)]) == 0            # touching intervals do not overlap
+    assert overlapped([(0., 2.), (1., 3.), (4., 5.)]) == 2
+    assert overlapped([(0., 10.), (1., 2.), (3., 4.), (11., 12.)]) == 3

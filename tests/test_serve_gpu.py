@@ -82,8 +82,37 @@ def test_budget_admission_and_merging(env):
     out = [f.result(timeout=60) for f in futs]
     srv.close()
     assert srv.peak_used <= srv.budget
+    st = srv.stats()
+    # requests with the same grid and physics were merged into batched launches
+    assert st["merged_launches"] >= 1 and st["launches"] < len(reqs), st
     for r, o in zip(reqs, out):
         want = bpm.bpm_3d(r.size, r.units, lam=r.lam, n0=r.n0, u0=r.u0, dn=r.dn, return_field=False)
+        assert np.array_equal(o.cpu().numpy(), want)
+
+
+def test_launches_overlap_on_the_device(env):
+    """Requests that cannot merge (four Nz) submitted together run as four launches on their
+    own streams: more than one is in flight at once, and their device intervals (CUDA
+    events on each launch's stream) overlap; each result equals the request alone."""
+    torch, bpm, BpmRequest, PsfRequest, Server = env
+    side = 512
+    reqs = []
+    for k, nz in enumerate((96, 112, 128, 144)):
+        u0 = np.exp(1j * .03 * (k + 1) * np.arange(side))[None].repeat(side, 0).astype(np.complex64)
+        reqs.append(BpmRequest((side, side, nz), (.1, .1, .1), n0=1.33, u0=u0, mean_mode="ignore",
+                               return_field=False, return_full=False))
+    for _ in range(2):   # the first pass builds the plans and fills the allocator's cache
+        srv = Server(max_inflight=4, max_batch=8)
+        futs = [srv.submit(r) for r in reqs]
+        out = [f.result(timeout=60) for f in futs]
+        srv.close()
+    st = srv.stats()
+    assert st["launches"] == 4 and st["merged_launches"] == 0, st
+    assert st["max_inflight_seen"] >= 2, st
+    assert st["overlapped_launches"] >= 2, (st, srv.spans)
+    for r, o in zip(reqs, out):
+        want = bpm.bpm_3d(r.size, r.units, lam=r.lam, n0=r.n0, u0=r.u0, mean_mode="ignore", return_field=False,
+                          return_full=False)
         assert np.array_equal(o.cpu().numpy(), want)
 
 
