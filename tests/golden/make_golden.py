@@ -1,7 +1,7 @@
 """Generate the golden vectors in tests/golden/*.npz from the reference's own kernels.
 
-Run here, where the reference checkout exists:
-    make -C oracle REF=/root/reference && python tests/golden/make_golden.py
+Run where the reference checkout exists (REF = the directory holding its bpm/ package):
+    make -C oracle REF=<reference checkout> && python tests/golden/make_golden.py
 
 Golden outputs come from the reference's OpenCL kernel sources compiled as host C++
 (oracle/_ref/libref_cl.so, see oracle/Makefile):
