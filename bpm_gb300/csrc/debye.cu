@@ -18,12 +18,22 @@
 // full volume directly, mirroring each voxel to its octant sample (index |m - N0/2|,
 // conjugate where z <= Nz0/2, as the reference's slice loop does), so no octant buffer
 // and no host-side spreading is needed.
+//
+// The three products run on the tensor cores (tcgen05.mma, kind::tf32, operands staged by
+// TMA, accumulators in tensor memory) in a 3xTF32 split that keeps FP32 accuracy: with
+// A = Ah + Al and B = Bh + Bl, Ah and Bh exact TF32 values, D = Ah Bh + Ah Bl + Al Bh (the
+// dropped Al Bl is below 2^-20 of the product). Where the octant's x and y grids coincide
+// (dx = dy, nx = ny) the integrals depend on the radius only through x^2 + y^2 and the
+// rows of A are the distinct (min, max) index pairs of the octant's columns, nxo (nxo + 1)
+// / 2 of them instead of nxo^2. BPM_GB300_DEBYE=fma selects the FP32 FMA kernel instead.
 #include <cmath>
+#include <cstdlib>
 #include <cstring>
 #include <algorithm>
 #include <vector>
 
 #include "common.cuh"
+#include "tcgen05.cuh"
 
 using namespace bpmgb;
 
@@ -364,10 +374,19 @@ __device__ __forceinline__ int mirror_gauss(int p, int N0, int N) {
   return p >= N0 - N ? p - (N0 - N) : N - 1 - p;
 }
 
-// full-volume assembly fused with the octant mirroring
+// row of the integrals of octant column (ix, jy): with a symmetric octant (the x and y
+// grids equal) the distinct pair (min, max) in triangular order, else jy * nxo + ix
+__host__ __device__ __forceinline__ int radius_index(int ix, int jy, int nxo, bool sym) {
+  if (!sym) return jy * nxo + ix;
+  const int a = ix < jy ? ix : jy, b = ix < jy ? jy : ix;
+  return b * (b + 1) / 2 + a;
+}
+
+// full-volume assembly fused with the octant mirroring; I is (3, Zo, Mr) over the rows of
+// radius_index
 template <int MIR>
-__global__ void debye_assemble_kernel(int nx, int ny, int nz, OctGeom g, int M, int Zo, float ex0, float ey0,
-                                      const float2* __restrict__ I, const float* __restrict__ trig,
+__global__ void debye_assemble_kernel(int nx, int ny, int nz, OctGeom g, int M, int Mr, int sym, int Zo, float ex0,
+                                      float ey0, const float2* __restrict__ I, const float* __restrict__ trig,
                                       float* __restrict__ u, float2* __restrict__ ex, float2* __restrict__ ey,
                                       float2* __restrict__ ez) {
   const int x = blockIdx.x * blockDim.x + threadIdx.x;
@@ -383,7 +402,8 @@ __global__ void debye_assemble_kernel(int nx, int ny, int nz, OctGeom g, int M, 
     conj = false;
   }
   const int m = jy * g.nxo + ix;
-  const size_t ZM = (size_t)Zo * M, o = (size_t)kz * M + m;
+  const int r = radius_index(ix, jy, g.nxo, sym != 0);
+  const size_t ZM = (size_t)Zo * Mr, o = (size_t)kz * Mr + r;
   const float2 I0 = __ldg(I + o), I1 = __ldg(I + ZM + o), I2 = __ldg(I + 2 * ZM + o);
   const float c1 = __ldg(trig + m), s1 = __ldg(trig + M + m);
   const float c2 = __ldg(trig + 2 * M + m), s2 = __ldg(trig + 3 * M + m);
@@ -503,6 +523,243 @@ __global__ void __launch_bounds__(PT_THREADS) debye_points_kernel(
   if (ez) ez[p] = make_float2(2.f * I1.y * pz, -2.f * I1.x * pz);
 }
 
+
+// ---------------------------------------------------------------------------------------
+// Tensor-core quadrature. Operands are K-major (node index t contiguous) so TMA tiles of
+// 32 nodes x 128 rows land in the 128-byte swizzle layout tcgen05.mma reads:
+//   A (3 Mr, T): row n Mr + r = p_n(t) J_n(kr_r sin t), r over the radius rows
+//   Bh, Bl (2 Zo, T): row 2z = cos(kz_z cos t), row 2z + 1 = sin(kz_z cos t), split into an
+//                     exact TF32 high part and the FP32 remainder
+// and the product D = A B^T lands in tensor memory as I[(n, r), (z, re/im)].
+// ---------------------------------------------------------------------------------------
+__device__ int g_tc_status;  // nonzero once a tensor-core wait gave up (bpm_device_status)
+
+__device__ __forceinline__ float tf32_hi(float v) { return __uint_as_float(__float_as_uint(v) & 0xffffe000u); }
+
+// octant column (ix, jy) of radius row r (inverse of radius_index)
+__device__ __forceinline__ int radius_column(int r, int nxo, bool sym) {
+  if (!sym) return r;
+  int b = (int)((sqrtf(8.f * (float)r + 1.f) - 1.f) * .5f);
+  while (b * (b + 1) / 2 > r) b--;
+  while ((b + 1) * (b + 2) / 2 <= r) b++;
+  const int a = r - b * (b + 1) / 2;
+  return b * nxo + a;
+}
+
+// A(n Mr + r, t) = p_n(t) J_n(kr sin t): the same values as debye_bessel_kernel's tables
+__global__ void debye_bessel_tc_kernel(int T, int Tp, int Mr, int nxo, int sym, const double* __restrict__ si,
+                                       const double* __restrict__ kr, const float* __restrict__ wf,
+                                       float* __restrict__ A) {
+  const int tb = (T + 127) / 128;
+  const int r = blockIdx.x / tb;
+  const int t = (blockIdx.x - r * tb) * 128 + threadIdx.x;
+  if (t >= T) return;
+  const int m = radius_column(r, nxo, sym != 0);
+  const float x = (float)(kr[m] * si[t]);
+  const float j0 = j0f(x), j1 = j1f(x);
+  const float j2 = bessel_j2(x, j0, j1);
+  const size_t o = (size_t)r * Tp + t, RT = (size_t)Mr * Tp;
+  A[o] = wf[t] * j0;
+  A[RT + o] = wf[T + t] * j1;
+  A[2 * RT + o] = wf[2 * T + t] * j2;
+}
+
+// Bh/Bl(2z + {0, 1}, t) = high/low parts of (cos, sin)(kz_z cos t), phase formed and
+// reduced in FP64 as debye_phase_kernel's
+__global__ void debye_phase_tc_kernel(int T, int Tp, int Zo, float z1, float z2, double k, const double* ct,
+                                      float* __restrict__ Bh, float* __restrict__ Bl) {
+  const int tb = (T + 127) / 128;
+  const int z = blockIdx.x / tb;
+  const int t = (blockIdx.x - z * tb) * 128 + threadIdx.x;
+  if (t >= T) return;
+  const double kz = k * (double)(Zo == 1 ? z1 : coord_f32(z, z1, z2, Zo));
+  double sd, cd;
+  sincos(kz * ct[t], &sd, &cd);
+  const float c = (float)cd, sn = (float)sd;
+  const size_t o = (size_t)(2 * z) * Tp + t;
+  Bh[o] = tf32_hi(c);
+  Bl[o] = c - tf32_hi(c);
+  Bh[o + Tp] = tf32_hi(sn);
+  Bl[o + Tp] = sn - tf32_hi(sn);
+}
+
+constexpr int TC_BM = 128, TC_BK = 32, TC_THREADS = 128;
+constexpr uint64_t TC_WAIT_NS = 2000000000ull;  // a wait gives up after 2 s
+
+struct TcArgs {
+  int T;           // quadrature nodes (the K extent)
+  int rows;        // 3 Mr
+  int Mr;          // radius rows
+  int Zo;          // octant planes
+  int BN;          // product columns per block: a multiple of 16, <= 256
+  int stages;      // shared-memory pipeline depth
+  uint32_t tmem_cols;
+  int nacc;        // accumulators in tensor memory (2 or 3), acc_stride columns apart
+  int acc_stride;
+  float2* I;       // (3, Zo, Mr)
+};
+
+__host__ __device__ constexpr uint32_t tc_a_bytes() { return TC_BM * TC_BK * 4; }
+__host__ __device__ constexpr uint32_t tc_b_bytes(int BN) { return (uint32_t)BN * TC_BK * 4; }
+__host__ __device__ constexpr uint32_t tc_stage_bytes(int BN) { return 2 * tc_a_bytes() + 2 * tc_b_bytes(BN); }
+__host__ __device__ constexpr size_t tc_smem_bytes(int BN, int S) {
+  return 1024 + (size_t)S * tc_stage_bytes(BN) + (2 * S + 1) * 8 + 16;
+}
+
+// One 128-row x BN-column tile of the product per block of 4 warps. Thread 0 issues the TMA
+// loads (A, Bh, Bl of a 32-node slice per stage, S stages in flight) and the MMAs; every
+// thread splits the stage's A tile into its TF32 high part (in place) and the remainder
+// (next to it) before the MMAs of that stage are issued; a stage is refilled once the
+// MMAs that read it have completed (tcgen05.commit on its mbarrier). The accumulator is
+// one 128-lane x BN-column region of tensor memory; the 4 warps read their 32 lanes back
+// and store I. The products go to separate accumulators so that each adds fewer terms
+// (the tensor core rounds its FP32 sums with a bias that grows with the number of
+// accumulations): Ah Bh of even and of odd node slices to two accumulators and the small
+// cross terms to a third (with room for two only, Ah Bh to one and the cross terms to the
+// other); the epilogue adds them in FP32. Every wait is bounded in time: on expiry the
+// block records g_tc_status,
+// waits (bounded) for its own copies and products in flight, frees its tensor memory
+// and returns.
+__global__ void __launch_bounds__(TC_THREADS, 1)
+debye_accum_tc_kernel(const __grid_constant__ CUtensorMap mapA, const __grid_constant__ CUtensorMap mapBh,
+                      const __grid_constant__ CUtensorMap mapBl, TcArgs a) {
+  extern __shared__ uint8_t tc_smem_raw[];
+  uint8_t* sm = reinterpret_cast<uint8_t*>((reinterpret_cast<uintptr_t>(tc_smem_raw) + 1023) & ~uintptr_t(1023));
+  const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+  const int S = a.stages;
+  const uint32_t AB = tc_a_bytes(), BB = tc_b_bytes(a.BN), SB = tc_stage_bytes(a.BN);
+  uint64_t* full = reinterpret_cast<uint64_t*>(sm + (size_t)S * SB);
+  uint64_t* empty = full + S;
+  uint64_t* done = empty + S;
+  uint32_t* tmem_slot = reinterpret_cast<uint32_t*>(done + 1);
+  const int m0 = blockIdx.y * TC_BM, n0 = blockIdx.x * a.BN;
+  const int KT = (a.T + TC_BK - 1) / TC_BK;
+
+  if (tid == 0) {
+    for (int i = 0; i < S; i++) {
+      tc::mbar_init(&full[i], 1);
+      tc::mbar_init(&empty[i], 1);
+    }
+    tc::mbar_init(done, 1);
+    tc::fence_mbar_init();
+    tc::tma_prefetch_map(&mapA);
+    tc::tma_prefetch_map(&mapBh);
+    tc::tma_prefetch_map(&mapBl);
+  }
+  if (warp == 0) {
+    tc::tmem_alloc(tmem_slot, a.tmem_cols);
+    tc::tmem_relinquish();
+  }
+  tc::fence_before_sync();
+  __syncthreads();
+  tc::fence_after_sync();
+  const uint32_t tmem = *tmem_slot;
+
+  auto issue = [&](int st, int kt) {
+    uint8_t* base = sm + (size_t)st * SB;
+    tc::mbar_expect_tx(&full[st], AB + 2 * BB);
+    tc::tma_load_2d(base, &mapA, &full[st], kt * TC_BK, m0);
+    tc::tma_load_2d(base + 2 * AB, &mapBh, &full[st], kt * TC_BK, n0);
+    tc::tma_load_2d(base + 2 * AB + BB, &mapBl, &full[st], kt * TC_BK, n0);
+  };
+  int issued = 0;  // slices whose loads thread 0 has issued
+  if (tid == 0)
+    for (; issued < S && issued < KT; issued++) issue(issued, issued);
+
+  const uint32_t idesc = tc::idesc_tf32(TC_BM, a.BN);
+  bool ok = true;
+  int consumed = 0;  // slices whose products were issued
+  for (int kt = 0; kt < KT; kt++) {
+    const int st = kt % S;
+    const bool landed = tc::mbar_wait(&full[st], (uint32_t)(kt / S) & 1u, TC_WAIT_NS);
+    if (!__syncthreads_and(landed && ok)) {
+      ok = false;
+      break;
+    }
+    // A = Ah + Al: Ah (exact TF32) in place, Al in the next 16 KB
+    uint8_t* base = sm + (size_t)st * SB;
+    float4* pa = reinterpret_cast<float4*>(base);
+    float4* pl = reinterpret_cast<float4*>(base + AB);
+#pragma unroll 4
+    for (int i = tid; i < (int)(AB / 16); i += TC_THREADS) {
+      const float4 v = pa[i];
+      const float4 h = make_float4(tf32_hi(v.x), tf32_hi(v.y), tf32_hi(v.z), tf32_hi(v.w));
+      pl[i] = make_float4(v.x - h.x, v.y - h.y, v.z - h.z, v.w - h.w);
+      pa[i] = h;
+    }
+    tc::fence_proxy_async();
+    __syncthreads();
+    if (tid == 0) {
+      tc::fence_after_sync();
+      const uint32_t sa = tc::smem_u32(base), sl = sa + AB, sbh = sa + 2 * AB, sbl = sbh + BB;
+#pragma unroll
+      for (int k = 0; k < TC_BK / 8; k++) {  // 8 TF32 (32 bytes) of K per instruction
+        const uint64_t dah = tc::desc_sw128_kmajor(sa + 32 * k), dal = tc::desc_sw128_kmajor(sl + 32 * k);
+        const uint64_t dbh = tc::desc_sw128_kmajor(sbh + 32 * k), dbl = tc::desc_sw128_kmajor(sbl + 32 * k);
+        // accumulators: big (Ah Bh) and cross (Ah Bl + Al Bh)
+        const uint32_t big = a.nacc == 3 ? tmem + (uint32_t)((kt & 1) * a.acc_stride) : tmem;
+        const uint32_t cross = tmem + (uint32_t)((a.nacc - 1) * a.acc_stride);
+        const uint32_t first_big = a.nacc == 3 ? (kt < 2 && k == 0) : (kt == 0 && k == 0);
+        tc::mma_tf32(big, dah, dbh, idesc, first_big ? 0u : 1u);
+        tc::mma_tf32(cross, dah, dbl, idesc, (kt > 0 || k > 0) ? 1u : 0u);
+        tc::mma_tf32(cross, dal, dbh, idesc, 1u);
+      }
+      tc::mma_commit(&empty[st]);
+      // refill the stage of the previous slice once its products have read it
+      if (kt >= 1 && issued < KT) {
+        const int sp = (kt - 1) % S;
+        if (tc::mbar_wait(&empty[sp], (uint32_t)((kt - 1) / S) & 1u, TC_WAIT_NS)) {
+          issue(sp, issued);
+          issued++;
+        } else {
+          ok = false;
+        }
+      }
+    }
+    consumed = kt + 1;
+  }
+  ok = __syncthreads_and(ok);
+  if (tid == 0) tc::mma_commit(done);  // arrives once every product issued so far has completed
+  const bool fin = tc::mbar_wait(done, 0, TC_WAIT_NS);
+  ok = __syncthreads_and(ok && fin);
+  tc::fence_after_sync();
+  if (ok) {
+    const int row = m0 + warp * 32 + lane;
+    const bool rv = row < a.rows;
+    const int n = rv ? row / a.Mr : 0, r = rv ? row - n * a.Mr : 0;
+    const size_t ob = ((size_t)n * a.Zo) * a.Mr + r;
+    const uint32_t lane_base = tmem + ((uint32_t)(warp * 32) << 16);
+    const bool two_big = a.nacc == 3 && KT > 1;  // the odd-slice accumulator was written
+    for (int c0 = 0; c0 < a.BN; c0 += 16) {
+      float v[16], w[16], x[16];
+      tc::tmem_ld_32x32b_x16(lane_base + (uint32_t)c0, v);
+      tc::tmem_ld_32x32b_x16(lane_base + (uint32_t)((a.nacc - 1) * a.acc_stride + c0), x);
+      if (two_big) {
+        tc::tmem_ld_32x32b_x16(lane_base + (uint32_t)(a.acc_stride + c0), w);
+#pragma unroll
+        for (int j = 0; j < 16; j++) v[j] += w[j];
+      }
+#pragma unroll
+      for (int j = 0; j < 16; j++) v[j] += x[j];
+      if (rv) {
+#pragma unroll
+        for (int j = 0; j < 8; j++) {
+          const int z = (n0 + c0) / 2 + j;
+          if (z < a.Zo) a.I[ob + (size_t)z * a.Mr] = make_float2(v[2 * j], v[2 * j + 1]);
+        }
+      }
+    }
+  } else if (tid == 0) {
+    atomicExch(&g_tc_status, 1);
+    // loads issued but never consumed still land in this block's shared memory: wait
+    // for them (bounded) before the block exits
+    for (int kt = consumed; kt < issued; kt++) tc::mbar_wait(&full[kt % S], (uint32_t)(kt / S) & 1u, TC_WAIT_NS);
+  }
+  tc::fence_before_sync();
+  __syncthreads();
+  if (warp == 0) tc::tmem_dealloc(tmem, a.tmem_cols);
+}
+
 enum Variant { V_STD = 0, V_GAUSS = 1, V_PLANE = 2, V_AT = 3 };
 
 int check_desc(const debye_desc* d, Variant v = V_STD) {
@@ -556,8 +813,199 @@ double wave_number(const debye_desc* d) {
 }
 
 // the octant pipeline shared by focus_field_debye and focus_field_debye_gauss
+// ---- tensor-core path (host) -------------------------------------------------------------
+}  // namespace
+
+int bpmgb::tc::encode_f32_kmajor(CUtensorMap* map, const float* base, uint64_t rows, uint64_t cols,
+                                 uint64_t pitch_elems, uint32_t box_rows) {
+  using EncodeFn = CUresult (*)(CUtensorMap*, CUtensorMapDataType, cuuint32_t, void*, const cuuint64_t*,
+                                const cuuint64_t*, const cuuint32_t*, const cuuint32_t*, CUtensorMapInterleave,
+                                CUtensorMapSwizzle, CUtensorMapL2promotion, CUtensorMapFloatOOBfill);
+  static EncodeFn fn = [] {
+    void* f = nullptr;
+    cudaDriverEntryPointQueryResult q;
+    if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &f, 12000, cudaEnableDefault, &q) != cudaSuccess ||
+        q != cudaDriverEntryPointSuccess)
+      f = nullptr;
+    cudaGetLastError();
+    return reinterpret_cast<EncodeFn>(f);
+  }();
+  if (!fn) return -1;
+  const cuuint64_t dims[2] = {cols, rows};
+  const cuuint64_t strides[1] = {pitch_elems * sizeof(float)};
+  const cuuint32_t box[2] = {32, box_rows};
+  const cuuint32_t estr[2] = {1, 1};
+  return (int)fn(map, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 2, const_cast<float*>(base), dims, strides, box, estr,
+                 CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_128B, CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
+                 CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+}
+
+namespace {
+
+// the octant quadrature on the tensor cores unless BPM_GB300_DEBYE=fma
+bool debye_tc_enabled() {
+  static const bool on = [] {
+    const char* e = getenv("BPM_GB300_DEBYE");
+    return !(e && strcmp(e, "fma") == 0);
+  }();
+  return on;
+}
+
+// octant grid and node weights shared by both quadrature kernels
+void octant_setup(const debye_desc* d, bool gauss, double sig, int nxo, int nyo, int nzo, OctGeom& g, NodeArgs& na) {
+  na = node_args(d, gauss ? W_GAUSS : W_STD);
+  g.nxo = nxo;
+  g.nyo = nyo;
+  g.nzo = nzo;
+  g.x1 = g.y1 = g.z1 = 0.f;
+  if (gauss) {
+    // _focus_fields_debye.py:404-412: x2 = dx*Nx with Nx the octant size
+    g.x2 = (float)(d->dx * nxo);
+    g.y2 = (float)(d->dy * nyo);
+    g.z2 = (float)(d->dz * nzo);
+    // psf_debye.cl:310-311: exp_prefac = -.5/alpha_max^2/sig^2, from the float32 arguments
+    const double amax = na.alpha[d->n_na - 1], sg = (float)sig;
+    na.gauss_prefac = -.5 / amax / amax / sg / sg;
+  } else {
+    // _focus_fields_debye.py:102-109
+    g.x2 = (float)(d->dx * (nxo - 1.));
+    g.y2 = (float)(d->dy * (nyo - 1.));
+    g.z2 = (float)(d->dz * (nzo - 1.));
+  }
+}
+
+struct TcLayout {
+  size_t si, ct, wf, kr, trig, A, Bh, Bl, I, total;
+  int T, Tp, M, Mr, Zo, nxo, nyo, nzo, BN, ntn, stages;
+  bool sym;
+};
+
+TcLayout tc_layout(const debye_desc* d, bool gauss) {
+  TcLayout L;
+  if (gauss) {
+    L.nxo = (d->nx + 1) / 2;
+    L.nyo = (d->ny + 1) / 2;
+    L.nzo = (d->nz + 1) / 2;
+  } else {
+    L.nxo = d->nx / 2 + 1;
+    L.nyo = d->ny / 2 + 1;
+    L.nzo = d->nz / 2 + 1;
+  }
+  OctGeom g;
+  NodeArgs na;
+  octant_setup(d, gauss, 1., L.nxo, L.nyo, L.nzo, g, na);
+  L.sym = L.nxo == L.nyo && g.x1 == g.y1 && g.x2 == g.y2;
+  L.T = (d->n_na / 2) * (d->n_integration_steps + 1);
+  L.Tp = (L.T + 3) & ~3;  // 16-byte rows for TMA
+  L.M = L.nxo * L.nyo;
+  L.Mr = L.sym ? L.nxo * (L.nxo + 1) / 2 : L.M;
+  L.Zo = L.nzo;
+  // product columns 2 Zo in ntn blocks of BN (a multiple of 16, <= 256)
+  const int cols = 2 * L.Zo;
+  L.ntn = (cols + 255) / 256;
+  L.BN = ((cols + L.ntn - 1) / L.ntn + 15) & ~15;
+  L.stages = tc_smem_bytes(L.BN, 3) <= 227 * 1024 ? 3 : 2;
+  size_t off = 0;
+  L.si = off; off += align256(sizeof(double) * L.T);
+  L.ct = off; off += align256(sizeof(double) * L.T);
+  L.wf = off; off += align256(sizeof(float) * 3 * L.T);
+  L.kr = off; off += align256(sizeof(double) * L.M);
+  L.trig = off; off += align256(sizeof(float) * 4 * L.M);
+  L.A = off; off += align256(sizeof(float) * 3 * (size_t)L.Mr * L.Tp);
+  L.Bh = off; off += align256(sizeof(float) * 2 * (size_t)L.Zo * L.Tp);
+  L.Bl = off; off += align256(sizeof(float) * 2 * (size_t)L.Zo * L.Tp);
+  L.I = off; off += align256(sizeof(float2) * 3 * (size_t)L.Zo * L.Mr);
+  L.total = off;
+  return L;
+}
+
+size_t octant_workspace_bytes(const debye_desc* d, bool gauss) {
+  return debye_tc_enabled() ? tc_layout(d, gauss).total : debye_layout(d, gauss).total;
+}
+
+int run_octant_tc(const debye_desc* d, bool gauss, double sig, float* u, void* ex, void* ey, void* ez, void* ws,
+                  size_t ws_bytes, cudaStream_t s) {
+  TcLayout L = tc_layout(d, gauss);
+  if (!ws || ws_bytes < L.total) {
+    set_error("workspace too small: need " + std::to_string(L.total) + " bytes");
+    return BPM_ERR_OOM;
+  }
+  if (!aligned16(ws)) { set_error("workspace must be 16-byte aligned"); return BPM_ERR_ARG; }
+  char* w = static_cast<char*>(ws);
+  double* si = reinterpret_cast<double*>(w + L.si);
+  double* ct = reinterpret_cast<double*>(w + L.ct);
+  float* wf = reinterpret_cast<float*>(w + L.wf);
+  double* kr = reinterpret_cast<double*>(w + L.kr);
+  float* trig = reinterpret_cast<float*>(w + L.trig);
+  float* A = reinterpret_cast<float*>(w + L.A);
+  float* Bh = reinterpret_cast<float*>(w + L.Bh);
+  float* Bl = reinterpret_cast<float*>(w + L.Bl);
+  float2* I = reinterpret_cast<float2*>(w + L.I);
+  OctGeom g;
+  NodeArgs na;
+  octant_setup(d, gauss, sig, L.nxo, L.nyo, L.nzo, g, na);
+  const double k = wave_number(d);
+  const int rows = 3 * L.Mr;
+
+  CUtensorMap mA, mBh, mBl;
+  if (tc::encode_f32_kmajor(&mA, A, (uint64_t)rows, (uint64_t)L.T, (uint64_t)L.Tp, TC_BM) ||
+      tc::encode_f32_kmajor(&mBh, Bh, (uint64_t)2 * L.Zo, (uint64_t)L.T, (uint64_t)L.Tp, (uint32_t)L.BN) ||
+      tc::encode_f32_kmajor(&mBl, Bl, (uint64_t)2 * L.Zo, (uint64_t)L.T, (uint64_t)L.Tp, (uint32_t)L.BN)) {
+    set_error("cuTensorMapEncodeTiled failed for the quadrature operands");
+    return BPM_ERR_CUDA;
+  }
+  const int tb = (L.T + 127) / 128;
+  debye_nodes_kernel<<<(L.T + 127) / 128, 128, 0, s>>>(na, si, ct, wf, L.T);
+  BPM_LAUNCH_CHECK("debye_nodes_kernel");
+  debye_radii_kernel<<<(L.M + 127) / 128, 128, 0, s>>>(g, k, kr, trig, L.M);
+  BPM_LAUNCH_CHECK("debye_radii_kernel");
+  debye_phase_tc_kernel<<<(unsigned)(tb * L.Zo), 128, 0, s>>>(L.T, L.Tp, L.Zo, g.z1, g.z2, k, ct, Bh, Bl);
+  BPM_LAUNCH_CHECK("debye_phase_tc_kernel");
+  debye_bessel_tc_kernel<<<(unsigned)((size_t)tb * L.Mr), 128, 0, s>>>(L.T, L.Tp, L.Mr, L.nxo, L.sym ? 1 : 0, si,
+                                                                      kr, wf, A);
+  BPM_LAUNCH_CHECK("debye_bessel_tc_kernel");
+  TcArgs ta;
+  ta.T = L.T;
+  ta.rows = rows;
+  ta.Mr = L.Mr;
+  ta.Zo = L.Zo;
+  ta.BN = L.BN;
+  ta.stages = L.stages;
+  // accumulators 32-column aligned; three when they fit the 512 columns, else two
+  ta.acc_stride = (L.BN + 31) & ~31;
+  ta.nacc = 3 * ta.acc_stride <= 512 ? 3 : 2;
+  {
+    uint32_t need = (uint32_t)(ta.nacc * ta.acc_stride), c = 32;
+    while (c < need) c <<= 1;
+    ta.tmem_cols = c;
+  }
+  ta.I = I;
+  const size_t smem = tc_smem_bytes(L.BN, L.stages);
+  static size_t smem_set = 0;
+  if (smem > smem_set) {
+    BPM_CUDA_TRY(cudaFuncSetAttribute(debye_accum_tc_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    smem_set = smem;
+  }
+  const dim3 grid(L.ntn, (rows + TC_BM - 1) / TC_BM);
+  debye_accum_tc_kernel<<<grid, TC_THREADS, smem, s>>>(mA, mBh, mBl, ta);
+  BPM_LAUNCH_CHECK("debye_accum_tc_kernel");
+  if (u || ex || ey || ez) {
+    const dim3 ag((d->nx + 127) / 128, d->ny, d->nz);
+    float2 *pex = static_cast<float2*>(ex), *pey = static_cast<float2*>(ey), *pez = static_cast<float2*>(ez);
+    if (gauss)
+      debye_assemble_kernel<MIR_GAUSS><<<ag, 128, 0, s>>>(d->nx, d->ny, d->nz, g, L.M, L.Mr, L.sym ? 1 : 0, L.Zo,
+                                                          (float)d->ex0, (float)d->ey0, I, trig, u, pex, pey, pez);
+    else
+      debye_assemble_kernel<MIR_STD><<<ag, 128, 0, s>>>(d->nx, d->ny, d->nz, g, L.M, L.Mr, L.sym ? 1 : 0, L.Zo,
+                                                        (float)d->ex0, (float)d->ey0, I, trig, u, pex, pey, pez);
+    BPM_LAUNCH_CHECK("debye_assemble_kernel");
+  }
+  return BPM_OK;
+}
+
 int run_octant(const debye_desc* d, bool gauss, double sig, float* u, void* ex, void* ey, void* ez, void* ws,
                size_t ws_bytes, cudaStream_t s) {
+  if (debye_tc_enabled()) return run_octant_tc(d, gauss, sig, u, ex, ey, ez, ws, ws_bytes, s);
   DebyeLayout L = debye_layout(d, gauss);
   if (!ws || ws_bytes < L.total) {
     set_error("workspace too small: need " + std::to_string(L.total) + " bytes");
@@ -573,26 +1021,9 @@ int run_octant(const debye_desc* d, bool gauss, double sig, float* u, void* ex, 
   float2* E = reinterpret_cast<float2*>(w + L.E);
   float2* I = reinterpret_cast<float2*>(w + L.I);
 
-  NodeArgs na = node_args(d, gauss ? W_GAUSS : W_STD);
   OctGeom g;
-  g.nxo = L.nxo;
-  g.nyo = L.nyo;
-  g.nzo = L.nzo;
-  g.x1 = g.y1 = g.z1 = 0.f;
-  if (gauss) {
-    // _focus_fields_debye.py:404-412: x2 = dx*Nx with Nx the octant size
-    g.x2 = (float)(d->dx * L.nxo);
-    g.y2 = (float)(d->dy * L.nyo);
-    g.z2 = (float)(d->dz * L.nzo);
-    // psf_debye.cl:310-311: exp_prefac = -.5/alpha_max^2/sig^2, from the float32 arguments
-    const double amax = na.alpha[d->n_na - 1], sg = (float)sig;
-    na.gauss_prefac = -.5 / amax / amax / sg / sg;
-  } else {
-    // _focus_fields_debye.py:102-109
-    g.x2 = (float)(d->dx * (L.nxo - 1.));
-    g.y2 = (float)(d->dy * (L.nyo - 1.));
-    g.z2 = (float)(d->dz * (L.nzo - 1.));
-  }
+  NodeArgs na;
+  octant_setup(d, gauss, sig, L.nxo, L.nyo, L.nzo, g, na);
   const double k = wave_number(d);
 
   debye_nodes_kernel<<<(L.T + 127) / 128, 128, 0, s>>>(na, si, ct, wf, L.T);
@@ -625,11 +1056,13 @@ int run_octant(const debye_desc* d, bool gauss, double sig, float* u, void* ex, 
     const dim3 grid((d->nx + 127) / 128, d->ny, d->nz);
     float2 *pex = static_cast<float2*>(ex), *pey = static_cast<float2*>(ey), *pez = static_cast<float2*>(ez);
     if (gauss)
-      debye_assemble_kernel<MIR_GAUSS><<<grid, 128, 0, s>>>(d->nx, d->ny, d->nz, g, L.M, L.Zo, (float)d->ex0,
-                                                            (float)d->ey0, I, trig, u, pex, pey, pez);
+      debye_assemble_kernel<MIR_GAUSS><<<grid, 128, 0, s>>>(d->nx, d->ny, d->nz, g, L.M, L.M, 0, L.Zo,
+                                                            (float)d->ex0, (float)d->ey0, I, trig, u, pex, pey,
+                                                            pez);
     else
-      debye_assemble_kernel<MIR_STD><<<grid, 128, 0, s>>>(d->nx, d->ny, d->nz, g, L.M, L.Zo, (float)d->ex0,
-                                                          (float)d->ey0, I, trig, u, pex, pey, pez);
+      debye_assemble_kernel<MIR_STD><<<grid, 128, 0, s>>>(d->nx, d->ny, d->nz, g, L.M, L.M, 0, L.Zo,
+                                                          (float)d->ex0, (float)d->ey0, I, trig, u, pex, pey,
+                                                          pez);
     BPM_LAUNCH_CHECK("debye_assemble_kernel");
   }
   return BPM_OK;
@@ -707,7 +1140,7 @@ int run_points(const debye_desc* d, bool grid, double zplane, const float* xs, c
 
 extern "C" size_t debye_workspace_bytes(const debye_desc* d) {
   if (check_desc(d)) return 0;
-  return debye_layout(d).total;
+  return octant_workspace_bytes(d, false);
 }
 
 extern "C" int debye_focus_field(const debye_desc* d, float* u, void* ex, void* ey, void* ez, void* ws,
@@ -720,7 +1153,7 @@ extern "C" int debye_focus_field(const debye_desc* d, float* u, void* ex, void* 
 
 extern "C" size_t debye_gauss_workspace_bytes(const debye_desc* d) {
   if (check_desc(d, V_GAUSS)) return 0;
-  return debye_layout(d, true).total;
+  return octant_workspace_bytes(d, true);
 }
 
 extern "C" int debye_focus_field_gauss(const debye_desc* d, double sig, float* u, void* ex, void* ey, void* ez,
@@ -756,4 +1189,14 @@ extern "C" int debye_focus_field_at(const debye_desc* d, const float* x, const f
   if (n < 0) { set_error("n must be >= 0"); return BPM_ERR_ARG; }
   if (n > 0 && (!x || !y || !z)) { set_error("coordinate arrays are NULL"); return BPM_ERR_ARG; }
   return run_points(d, false, 0., x, y, z, n, u, ex, ey, ez, ws, ws_bytes, static_cast<cudaStream_t>(stream));
+}
+
+extern "C" int bpm_device_status(int clear) {
+  int v = 0;
+  BPM_CUDA_TRY(cudaMemcpyFromSymbol(&v, g_tc_status, sizeof(int)));
+  if (clear && v) {
+    const int zero = 0;
+    BPM_CUDA_TRY(cudaMemcpyToSymbol(g_tc_status, &zero, sizeof(int)));
+  }
+  return v;
 }

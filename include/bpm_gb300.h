@@ -273,10 +273,19 @@ typedef struct {
 /* Bytes of scratch debye_focus_field needs for this description (256-aligned). */
 size_t debye_workspace_bytes(const debye_desc* desc);
 
+/* Sticky device-side status of the tensor-core kernels: nonzero once one of their bounded
+ * waits (an mbarrier that a TMA copy or a tensor-core product should complete) gave up
+ * after 2 s, in which case that launch left its outputs unwritten. Synchronises with the
+ * device to read it; clear != 0 resets it to 0. A negative bpm_status on a CUDA error.
+ * No counterpart in the reference (its OpenCL kernels have no such waits). */
+int bpm_device_status(int clear);
+
 /* Compute the focus field on the full (nz, ny, nx) grid centred at index n/2.
  * Replaces bpm/psf/_focus_fields_debye.py:focus_field_debye (:48-146): the debye_wolf
  * octant launch (:102-109, kernel bpm/psf/kernels/psf_debye.cl:24-113) and the host-side
- * spreading of the octant to the full volume (:116-144), fused into device kernels.
+ * spreading of the octant to the full volume (:116-144), fused into device kernels. The
+ * quadrature sums run as a 3xTF32 product on the tensor cores (tcgen05, TMA-staged
+ * operands); BPM_GB300_DEBYE=fma selects FP32 FMA kernels (set before the first call).
  * u: float32 |E|^2 (may be NULL); ex, ey, ez: complex64 (each may be NULL). */
 int debye_focus_field(const debye_desc* desc, float* u, void* ex, void* ey, void* ez,
                       void* workspace, size_t workspace_bytes, void* stream);

@@ -53,6 +53,7 @@ def test_config2_psf_256(bpm):
     c = 128
     # full index c + k (k >= 1 along z, >= 0 along x, y) holds octant sample k, unconjugated
     for a, b, k in zip((u, ex, ey, ez), octant, ("u", "ex", "ey", "ez")):
+        print("psf 256^3 %s: relative L2 %.2e against the FP64 oracle" % (k, rel_l2(a[c + 1:, c:, c:], b[1:c, :c, :c])))
         assert rel_l2(a[c + 1:, c:, c:], b[1:c, :c, :c]) < TOL, k
         # full index m <= c holds octant sample c - m, conjugated: index 0 is the octant's
         # last plane (z = 12.8 um), the one the plane-remainder kernel computes
@@ -168,3 +169,38 @@ def test_variant_errors(bpm):
         bpm.focus_field_debye_at(np.zeros(3), np.zeros(3), np.zeros(4), .5, .8)
     u, ex, ey, ez = bpm.focus_field_debye_at(np.zeros(0), np.zeros(0), np.zeros(0), .5, .8)
     assert u.shape == (0,)
+
+
+def test_tensor_core_quadrature_matches_fma(bpm, tmp_path):
+    """The octant quadrature as a 3xTF32 tensor-core product (tcgen05, TMA-staged operands,
+    the default) against the FP32 FMA kernels (BPM_GB300_DEBYE=fma), each in a child
+    process: symmetric octants (radius rows deduplicated) and non-square ones, annuli, the
+    Gaussian pupil with odd shapes, the 256^3 PSF of the single-request configuration. Both
+    evaluate the same node tables; the sums differ only by rounding (relative L2 < 5e-5 on
+    every output; each path is within 1e-4 of the FP64 oracle in the parity tests), and no
+    bounded tensor-core wait gave up."""
+    import os
+    import subprocess
+    import sys
+    here = os.path.dirname(os.path.abspath(__file__))
+    script = os.path.join(here, "_psf_cases.py")
+    a, b = str(tmp_path / "tc.npz"), str(tmp_path / "fma.npz")
+    env = {k: v for k, v in os.environ.items() if k != "BPM_GB300_DEBYE"}
+    subprocess.run([sys.executable, script, a], check=True, timeout=600, env=env)
+    subprocess.run([sys.executable, script, b], check=True, timeout=600, env=dict(env, BPM_GB300_DEBYE="fma"))
+    A, B = np.load(a), np.load(b)
+    assert int(A["device_status"][0]) == 0 and int(B["device_status"][0]) == 0
+    keys = [k for k in A.files if k != "device_status"]
+    assert sorted(keys) == sorted(k for k in B.files if k != "device_status") and len(keys) == 28
+    errs = {k: rel_l2(A[k], B[k]) for k in keys}
+    print("tensor cores vs FMA, largest relative L2: %s %.2e" % max(errs.items(), key=lambda kv: kv[1]))
+    bad = [(k, e) for k, e in errs.items() if not e < 5e-5]
+    assert not bad, bad
+
+
+def test_tensor_core_status_is_clear(bpm):
+    """After a PSF on the tensor cores the library's sticky device status is 0 (no bounded
+    wait gave up)."""
+    from bpm_gb300 import _native as N
+    bpm.psf((128, 128, 128), (.1, .1, .1), .5, 1.1, 1.33, 200)
+    assert N.lib().bpm_device_status(0) == 0
