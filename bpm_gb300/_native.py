@@ -58,7 +58,7 @@ class DebyeDesc(ctypes.Structure):
                 ("dx", c_double), ("dy", c_double), ("dz", c_double),
                 ("lam", c_double), ("n0", c_double),
                 ("na", ctypes.POINTER(c_double)), ("n_na", c_int),
-                ("n_integration_steps", c_int), ("ex0", c_double), ("ey0", c_double)]
+                ("n_integration_steps", c_int), ("ex0", c_double), ("ey0", c_double), ("quadrature", c_int)]
 
 
 # every symbol include/bpm_gb300.h declares, with its ctypes signature

@@ -46,7 +46,11 @@ constexpr int MAX_NA = 16;
 //   W_SINE:  psf_debye.cl:155-159 / :240-244, half weight where the float32 angle equals an
 //            annulus limit, dt sqrt(cos t) sin t (debye_wolf_plane, debye_wolf_at)
 //   W_GAUSS: psf_debye.cl:336-339, W_SINE times exp(t^2 * gauss_prefac)
-enum WeightKind { W_STD = 0, W_SINE = 1, W_GAUSS = 2 };
+//   W_PHYS:  the Debye integral's own pupil factor sqrt(cos t) sin t with an exact
+//            trapezoid over [a1, a2]: INT_STEPS nodes t = a1 + i dt, dt = (a2 - a1) /
+//            (INT_STEPS - 1), half weight at both ends, the node i = INT_STEPS (past a2)
+//            weighted 0 (the formula of tests/test_psf_vectorial.py:15-42 in the reference)
+enum WeightKind { W_STD = 0, W_SINE = 1, W_GAUSS = 2, W_PHYS = 3 };
 
 struct NodeArgs {
   float alpha[MAX_NA];
@@ -122,6 +126,8 @@ __global__ void debye_nodes_kernel(NodeArgs a, double* si, double* ct, float* wf
   double w;
   if (a.kind == W_STD) {
     w = ((i == 0 || i == a.steps) ? .5 : 1.) * dt * sqrt(c);
+  } else if (a.kind == W_PHYS) {
+    w = (i == a.steps ? 0. : ((i == 0 || i == a.steps - 1) ? .5 : 1.)) * dt * sqrt(c) * s;
   } else {
     // the end test runs on the float32 angle, each operation rounded on its own
     const float a1f = a.alpha[2 * ann], a2f = a.alpha[2 * ann + 1];
@@ -374,19 +380,10 @@ __device__ __forceinline__ int mirror_gauss(int p, int N0, int N) {
   return p >= N0 - N ? p - (N0 - N) : N - 1 - p;
 }
 
-// row of the integrals of octant column (ix, jy): with a symmetric octant (the x and y
-// grids equal) the distinct pair (min, max) in triangular order, else jy * nxo + ix
-__host__ __device__ __forceinline__ int radius_index(int ix, int jy, int nxo, bool sym) {
-  if (!sym) return jy * nxo + ix;
-  const int a = ix < jy ? ix : jy, b = ix < jy ? jy : ix;
-  return b * (b + 1) / 2 + a;
-}
-
-// full-volume assembly fused with the octant mirroring; I is (3, Zo, Mr) over the rows of
-// radius_index
+// full-volume assembly fused with the octant mirroring
 template <int MIR>
-__global__ void debye_assemble_kernel(int nx, int ny, int nz, OctGeom g, int M, int Mr, int sym, int Zo, float ex0,
-                                      float ey0, const float2* __restrict__ I, const float* __restrict__ trig,
+__global__ void debye_assemble_kernel(int nx, int ny, int nz, OctGeom g, int M, int Zo, float ex0, float ey0,
+                                      const float2* __restrict__ I, const float* __restrict__ trig,
                                       float* __restrict__ u, float2* __restrict__ ex, float2* __restrict__ ey,
                                       float2* __restrict__ ez) {
   const int x = blockIdx.x * blockDim.x + threadIdx.x;
@@ -402,8 +399,7 @@ __global__ void debye_assemble_kernel(int nx, int ny, int nz, OctGeom g, int M, 
     conj = false;
   }
   const int m = jy * g.nxo + ix;
-  const int r = radius_index(ix, jy, g.nxo, sym != 0);
-  const size_t ZM = (size_t)Zo * Mr, o = (size_t)kz * Mr + r;
+  const size_t ZM = (size_t)Zo * M, o = (size_t)kz * M + m;
   const float2 I0 = __ldg(I + o), I1 = __ldg(I + ZM + o), I2 = __ldg(I + 2 * ZM + o);
   const float c1 = __ldg(trig + m), s1 = __ldg(trig + M + m);
   const float c2 = __ldg(trig + 2 * M + m), s2 = __ldg(trig + 3 * M + m);
@@ -536,7 +532,9 @@ __device__ int g_tc_status;  // nonzero once a tensor-core wait gave up (bpm_dev
 
 __device__ __forceinline__ float tf32_hi(float v) { return __uint_as_float(__float_as_uint(v) & 0xffffe000u); }
 
-// octant column (ix, jy) of radius row r (inverse of radius_index)
+// octant column jy * nxo + ix of radius row r: with a symmetric octant (the x and y grids
+// equal) the rows are the distinct pairs ix <= jy in triangular order r = jy (jy + 1) / 2 + ix,
+// else r is the column itself
 __device__ __forceinline__ int radius_column(int r, int nxo, bool sym) {
   if (!sym) return r;
   int b = (int)((sqrtf(8.f * (float)r + 1.f) - 1.f) * .5f);
@@ -596,7 +594,8 @@ struct TcArgs {
   uint32_t tmem_cols;
   int nacc;        // accumulators in tensor memory (2 or 3), acc_stride columns apart
   int acc_stride;
-  float2* I;       // (3, Zo, Mr)
+  int nxo, M, sym; // octant columns per row, octant columns, radius rows deduplicated
+  float2* I;       // (3, Zo, M): row r of the product goes to its octant column(s)
 };
 
 __host__ __device__ constexpr uint32_t tc_a_bytes() { return TC_BM * TC_BK * 4; }
@@ -727,7 +726,12 @@ debye_accum_tc_kernel(const __grid_constant__ CUtensorMap mapA, const __grid_con
     const int row = m0 + warp * 32 + lane;
     const bool rv = row < a.rows;
     const int n = rv ? row / a.Mr : 0, r = rv ? row - n * a.Mr : 0;
-    const size_t ob = ((size_t)n * a.Zo) * a.Mr + r;
+    // octant column (ix, jy) of the row and, for a deduplicated row off the diagonal, its
+    // mirror (jy, ix): both receive the integrals, so I keeps the plain column layout
+    const int m1 = radius_column(r, a.nxo, a.sym != 0);
+    const int ix = m1 % a.nxo, jy = m1 / a.nxo;
+    const int m2 = (a.sym && ix != jy) ? ix * a.nxo + jy : -1;
+    const size_t ob = ((size_t)n * a.Zo) * a.M;
     const uint32_t lane_base = tmem + ((uint32_t)(warp * 32) << 16);
     const bool two_big = a.nacc == 3 && KT > 1;  // the odd-slice accumulator was written
     for (int c0 = 0; c0 < a.BN; c0 += 16) {
@@ -745,7 +749,11 @@ debye_accum_tc_kernel(const __grid_constant__ CUtensorMap mapA, const __grid_con
 #pragma unroll
         for (int j = 0; j < 8; j++) {
           const int z = (n0 + c0) / 2 + j;
-          if (z < a.Zo) a.I[ob + (size_t)z * a.Mr] = make_float2(v[2 * j], v[2 * j + 1]);
+          if (z < a.Zo) {
+            const float2 val = make_float2(v[2 * j], v[2 * j + 1]);
+            a.I[ob + (size_t)z * a.M + m1] = val;
+            if (m2 >= 0) a.I[ob + (size_t)z * a.M + m2] = val;
+          }
         }
       }
     }
@@ -782,6 +790,10 @@ int check_desc(const debye_desc* d, Variant v = V_STD) {
     return BPM_ERR_ARG;
   }
   if (d->n_integration_steps < 2) { set_error("n_integration_steps must be >= 2"); return BPM_ERR_ARG; }
+  if (d->quadrature != DEBYE_QUAD_REFERENCE && (v != V_STD || d->quadrature != DEBYE_QUAD_PHYSICAL)) {
+    set_error("quadrature must be DEBYE_QUAD_REFERENCE, or DEBYE_QUAD_PHYSICAL for debye_focus_field");
+    return BPM_ERR_ARG;
+  }
   if ((long long)(d->n_na / 2) * (d->n_integration_steps + 1) > 65535) {
     set_error("too many quadrature nodes: (len(NA)/2) * (n_integration_steps+1) must be <= 65535");
     return BPM_ERR_ARG;
@@ -853,7 +865,7 @@ bool debye_tc_enabled() {
 
 // octant grid and node weights shared by both quadrature kernels
 void octant_setup(const debye_desc* d, bool gauss, double sig, int nxo, int nyo, int nzo, OctGeom& g, NodeArgs& na) {
-  na = node_args(d, gauss ? W_GAUSS : W_STD);
+  na = node_args(d, gauss ? W_GAUSS : (d->quadrature == DEBYE_QUAD_PHYSICAL ? W_PHYS : W_STD));
   g.nxo = nxo;
   g.nyo = nyo;
   g.nzo = nzo;
@@ -914,7 +926,7 @@ TcLayout tc_layout(const debye_desc* d, bool gauss) {
   L.A = off; off += align256(sizeof(float) * 3 * (size_t)L.Mr * L.Tp);
   L.Bh = off; off += align256(sizeof(float) * 2 * (size_t)L.Zo * L.Tp);
   L.Bl = off; off += align256(sizeof(float) * 2 * (size_t)L.Zo * L.Tp);
-  L.I = off; off += align256(sizeof(float2) * 3 * (size_t)L.Zo * L.Mr);
+  L.I = off; off += align256(sizeof(float2) * 3 * (size_t)L.Zo * L.M);
   L.total = off;
   return L;
 }
@@ -979,6 +991,9 @@ int run_octant_tc(const debye_desc* d, bool gauss, double sig, float* u, void* e
     while (c < need) c <<= 1;
     ta.tmem_cols = c;
   }
+  ta.nxo = L.nxo;
+  ta.M = L.M;
+  ta.sym = L.sym ? 1 : 0;
   ta.I = I;
   const size_t smem = tc_smem_bytes(L.BN, L.stages);
   static size_t smem_set = 0;
@@ -993,11 +1008,11 @@ int run_octant_tc(const debye_desc* d, bool gauss, double sig, float* u, void* e
     const dim3 ag((d->nx + 127) / 128, d->ny, d->nz);
     float2 *pex = static_cast<float2*>(ex), *pey = static_cast<float2*>(ey), *pez = static_cast<float2*>(ez);
     if (gauss)
-      debye_assemble_kernel<MIR_GAUSS><<<ag, 128, 0, s>>>(d->nx, d->ny, d->nz, g, L.M, L.Mr, L.sym ? 1 : 0, L.Zo,
-                                                          (float)d->ex0, (float)d->ey0, I, trig, u, pex, pey, pez);
+      debye_assemble_kernel<MIR_GAUSS><<<ag, 128, 0, s>>>(d->nx, d->ny, d->nz, g, L.M, L.Zo, (float)d->ex0,
+                                                          (float)d->ey0, I, trig, u, pex, pey, pez);
     else
-      debye_assemble_kernel<MIR_STD><<<ag, 128, 0, s>>>(d->nx, d->ny, d->nz, g, L.M, L.Mr, L.sym ? 1 : 0, L.Zo,
-                                                        (float)d->ex0, (float)d->ey0, I, trig, u, pex, pey, pez);
+      debye_assemble_kernel<MIR_STD><<<ag, 128, 0, s>>>(d->nx, d->ny, d->nz, g, L.M, L.Zo, (float)d->ex0,
+                                                        (float)d->ey0, I, trig, u, pex, pey, pez);
     BPM_LAUNCH_CHECK("debye_assemble_kernel");
   }
   return BPM_OK;
@@ -1056,11 +1071,11 @@ int run_octant(const debye_desc* d, bool gauss, double sig, float* u, void* ex, 
     const dim3 grid((d->nx + 127) / 128, d->ny, d->nz);
     float2 *pex = static_cast<float2*>(ex), *pey = static_cast<float2*>(ey), *pez = static_cast<float2*>(ez);
     if (gauss)
-      debye_assemble_kernel<MIR_GAUSS><<<grid, 128, 0, s>>>(d->nx, d->ny, d->nz, g, L.M, L.M, 0, L.Zo,
+      debye_assemble_kernel<MIR_GAUSS><<<grid, 128, 0, s>>>(d->nx, d->ny, d->nz, g, L.M, L.Zo,
                                                             (float)d->ex0, (float)d->ey0, I, trig, u, pex, pey,
                                                             pez);
     else
-      debye_assemble_kernel<MIR_STD><<<grid, 128, 0, s>>>(d->nx, d->ny, d->nz, g, L.M, L.M, 0, L.Zo,
+      debye_assemble_kernel<MIR_STD><<<grid, 128, 0, s>>>(d->nx, d->ny, d->nz, g, L.M, L.Zo,
                                                           (float)d->ex0, (float)d->ey0, I, trig, u, pex, pey,
                                                           pez);
     BPM_LAUNCH_CHECK("debye_assemble_kernel");

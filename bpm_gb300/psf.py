@@ -18,8 +18,13 @@ __all__ = ["focus_field_debye", "focus_field_debye_gauss", "focus_field_debye_pl
            "psf", "psf_u0", "psf_lightsheet"]
 
 
-def _desc(shape3, units3, lam, NA, n0, n_integration_steps, ex0=1., ey0=0.):
+QUADRATURES = {"reference": 0, "physical": 1}
+
+
+def _desc(shape3, units3, lam, NA, n0, n_integration_steps, ex0=1., ey0=0., quadrature="reference"):
     """debye_desc for the C ABI; returns (desc, keep-alive NA array)."""
+    if quadrature not in QUADRATURES:
+        raise ValueError("quadrature must be 'reference' or 'physical'")
     if np.isscalar(NA):
         NA = [0., NA]
     NA = [float(a) for a in np.asarray(NA, np.float64).ravel()]
@@ -27,7 +32,7 @@ def _desc(shape3, units3, lam, NA, n0, n_integration_steps, ex0=1., ey0=0.):
     na = (ctypes.c_double * len(NA))(*NA)
     desc = N.DebyeDesc(int(shape3[0]), int(shape3[1]), int(shape3[2]), float(units3[0]), float(units3[1]),
                        float(units3[2]), float(lam), float(n0), ctypes.cast(na, ctypes.POINTER(ctypes.c_double)),
-                       len(NA), int(n_integration_steps), float(ex0), float(ey0))
+                       len(NA), int(n_integration_steps), float(ex0), float(ey0), QUADRATURES[quadrature])
     return desc, na
 
 
@@ -40,11 +45,12 @@ def _workspace(size_fn, run_fn, desc, what):
     return torch.empty(wsb, dtype=torch.uint8, device=_device()), wsb
 
 
-def _debye(shape, units, lam, NA, n0, n_integration_steps, want_u, want_field, ex0=1., ey0=0.):
+def _debye(shape, units, lam, NA, n0, n_integration_steps, want_u, want_field, ex0=1., ey0=0.,
+           quadrature="reference"):
     Nx0, Ny0, Nz0 = (int(s) for s in shape)
     if not Nx0 % 2 + Ny0 % 2 + Nz0 % 2 == 0:
         raise NotImplementedError("odd shapes not supported yet")
-    desc, _na = _desc(shape, units, lam, NA, n0, n_integration_steps, ex0, ey0)
+    desc, _na = _desc(shape, units, lam, NA, n0, n_integration_steps, ex0, ey0, quadrature)
     L = N.lib()
     ws, wsb = _workspace(L.debye_workspace_bytes,
                          lambda: L.debye_focus_field(ctypes.byref(desc), None, None, None, None, None, 0, None),
@@ -62,11 +68,17 @@ def _debye(shape, units, lam, NA, n0, n_integration_steps, want_u, want_field, e
     return u, ex, ey, ez
 
 
-def focus_field_debye(shape, units, lam, NA, n0=1., n_integration_steps=200, device=False):
+def focus_field_debye(shape, units, lam, NA, n0=1., n_integration_steps=200, device=False,
+                      quadrature="reference"):
     """Focus field of an aberration-free objective by the vectorial Debye integral
     (bpm/psf/_focus_fields_debye.py:48). Returns u, ex, ey, ez on (Nz, Ny, Nx), u being the
-    intensity. NA is a number or an even-length list of annulus limits."""
-    u, ex, ey, ez = _debye(shape, units, lam, NA, n0, n_integration_steps, True, True)
+    intensity. NA is a number or an even-length list of annulus limits.
+    quadrature="reference" (default) is the reference kernel's rule (n_integration_steps+1
+    nodes, the last one past the aperture angle, pupil factor sqrt(cos t) without sin t);
+    "physical" is the Debye integral's sqrt(cos t) sin t with an exact trapezoid of
+    n_integration_steps nodes over each annulus (an addition: the reference kernel has no
+    such option, its test script evaluates this formula)."""
+    u, ex, ey, ez = _debye(shape, units, lam, NA, n0, n_integration_steps, True, True, quadrature=quadrature)
     if device:
         return u, ex, ey, ez
     return _d2h(u), _d2h(ex), _d2h(ey), _d2h(ez)
@@ -156,10 +168,13 @@ def focus_field_debye_at(x, y, z, lam, NA, n0=1., n_integration_steps=200, devic
     return tuple(_d2h(a) for a in res)
 
 
-def psf(shape, units, lam, NA, n0=1., n_integration_steps=200, return_field=False, device=False):
+def psf(shape, units, lam, NA, n0=1., n_integration_steps=200, return_field=False, device=False,
+        quadrature="reference"):
     """3d PSF of an aberration-free optical system (bpm/psf/psf_functions.py:18): the
-    intensity u, or (u, ex, ey, ez) with return_field=True."""
-    u, ex, ey, ez = _debye(shape, units, lam, NA, n0, n_integration_steps, True, return_field)
+    intensity u, or (u, ex, ey, ez) with return_field=True. quadrature as in
+    focus_field_debye."""
+    u, ex, ey, ez = _debye(shape, units, lam, NA, n0, n_integration_steps, True, return_field,
+                           quadrature=quadrature)
     conv = (lambda t: t) if device else _d2h
     if return_field:
         return conv(u), conv(ex), conv(ey), conv(ez)

@@ -259,6 +259,16 @@ int bpm_spheres_fill(int nx, int ny, int nz, double dx, double dy, double dz, co
 /* Vectorial Debye-Wolf focus field                                                    */
 /* ---------------------------------------------------------------------------------- */
 
+/* quadrature rule of debye_focus_field */
+typedef enum {
+  DEBYE_QUAD_REFERENCE = 0, /* the reference kernel's: INT_STEPS+1 nodes with dt = (a2-a1)/(INT_STEPS-1),
+                               the last past a2, pupil factor sqrt(cos t) without sin t
+                               (bpm/psf/kernels/psf_debye.cl:62-78)                              */
+  DEBYE_QUAD_PHYSICAL = 1   /* the Debye integral's sqrt(cos t) sin t, exact trapezoid of INT_STEPS
+                               nodes over [a1, a2] (the formula of the reference's
+                               tests/test_psf_vectorial.py:15-42)                                */
+} debye_quadrature;
+
 typedef struct {
   int nx, ny, nz;            /* full output shape (even), arrays (nz, ny, nx)                  */
   double dx, dy, dz;         /* voxel size, microns                                            */
@@ -268,6 +278,7 @@ typedef struct {
   int n_na;                  /* even, >= 2                                                     */
   int n_integration_steps;   /* INT_STEPS: the rule uses INT_STEPS+1 nodes per annulus         */
   double ex0, ey0;           /* input polarisation (the reference launches with 1, 0)          */
+  int quadrature;            /* debye_quadrature (debye_focus_field only; 0 elsewhere)         */
 } debye_desc;
 
 /* Bytes of scratch debye_focus_field needs for this description (256-aligned). */

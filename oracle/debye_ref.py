@@ -49,25 +49,30 @@ def coord_f32(N, x2, x1=0.):
     return x1 + (i * (np.float32(x2) - x1)) / np.float32(N - 1.)
 
 
-def quadrature_nodes(alphas, int_steps):
-    """Nodes and end weights of the kernel's trapezoid rule per annulus (psf_debye.cl:62-78)."""
+def quadrature_nodes(alphas, int_steps, quadrature="reference"):
+    """Nodes and end weights of the kernel's trapezoid rule per annulus (psf_debye.cl:62-78):
+    int_steps+1 nodes, dt = (a2-a1)/(int_steps-1), half weights at i = 0 and i = int_steps.
+    quadrature="physical": the exact trapezoid of int_steps nodes over [a1, a2] (half weights
+    at both ends), the rule of the reference's tests/test_psf_vectorial.py:15-42."""
     ts, ws = [], []
     for a1, a2 in zip(alphas[0::2], alphas[1::2]):
         a1 = float(a1)
         a2 = float(a2)
         dt = (a2 - a1) / (int_steps - 1.)
-        i = np.arange(int_steps + 1)
+        n = int_steps + 1 if quadrature == "reference" else int_steps
+        i = np.arange(n)
         t = a1 + i * dt
-        w = np.where((i == 0) | (i == int_steps), .5, 1.) * dt
+        w = np.where((i == 0) | (i == n - 1), .5, 1.) * dt
         ts.append(t)
         ws.append(w)
     return np.concatenate(ts), np.concatenate(ws)
 
 
-def debye_octant(params, int_steps, Ex0=1., Ey0=0.):
+def debye_octant(params, int_steps, Ex0=1., Ey0=0., quadrature="reference"):
     """FP64 evaluation of debye_wolf (bpm/psf/kernels/psf_debye.cl:24-113) over the octant,
-    node weights as its :62-78. Returns (u, ex, ey, ez) of shape
-    (Nz, Ny, Nx) in float64/complex128."""
+    node weights as its :62-78 (pupil factor sqrt(cos t)); quadrature="physical" takes the
+    exact trapezoid of quadrature_nodes and the Debye integral's sqrt(cos t) sin t.
+    Returns (u, ex, ey, ez) of shape (Nz, Ny, Nx) in float64/complex128."""
     Nx, Ny, Nz = params["Nx"], params["Ny"], params["Nz"]
     x = coord_f32(Nx, params["x2"]).astype(np.float64)
     y = coord_f32(Ny, params["y2"]).astype(np.float64)
@@ -78,10 +83,12 @@ def debye_octant(params, int_steps, Ex0=1., Ey0=0.):
     kr = (k * np.sqrt(X ** 2 + Y ** 2)).ravel()
     phi = np.arctan2(Y, X).ravel()
     kz = k * z
-    t, w = quadrature_nodes(params["alphas"], int_steps)
+    t, w = quadrature_nodes(params["alphas"], int_steps, quadrature)
     co, si = np.cos(t), np.sin(t)
     with np.errstate(invalid="ignore"):
         pre = w * np.sqrt(co)
+    if quadrature == "physical":
+        pre = pre * si
     arg = kr[:, None] * si[None, :]
     A0 = (pre * (co + 1.))[None, :] * jv(0, arg)
     A1 = (pre * si)[None, :] * jv(1, arg)
@@ -131,11 +138,11 @@ def mirror_index(N0):
 
 
 def focus_field_debye(shape, units, lam, NA, n0=1., n_integration_steps=200,
-                      real_dtype=np.float32, complex_dtype=np.complex64):
+                      real_dtype=np.float32, complex_dtype=np.complex64, quadrature="reference"):
     """FP64 restatement of focus_field_debye (bpm/psf/_focus_fields_debye.py:48-146);
     returns (u, ex, ey, ez) on (Nz0, Ny0, Nx0)."""
     params = octant_params(shape, units, lam, NA, n0)
-    oct_ = debye_octant(params, n_integration_steps)
+    oct_ = debye_octant(params, n_integration_steps, quadrature=quadrature)
     return mirror_octant(shape, *oct_, real_dtype=real_dtype, complex_dtype=complex_dtype)
 
 

@@ -51,3 +51,21 @@ def golden_psf_case(g, name):
 BPM_GOLDEN = ["bpm_sphere_weighted", "bpm_sphere_simple", "bpm_sphere_ignore",
               "bpm_tilt_taper_weighted", "bpm_tilt_taper_ignore_half"]
 PSF_GOLDEN = ["psf_16_NA08", "psf_24x20x12_NA11", "psf_annulus", "psf_u0_like"]
+
+
+def debye_point_fp64(x, y, z, k, NA, n_int):
+    """The vectorial Debye integral at one point, x-polarised, by the trapezoid rule on
+    n_int equispaced angles over [0, arcsin NA] with the pupil factor sqrt(cos t) sin t:
+    the independent formula of the reference's tests/test_psf_vectorial.py:15-42, in FP64."""
+    from scipy.special import jv
+    a = np.arcsin(NA)
+    t = np.linspace(0., a, n_int)
+    w = np.full(n_int, a / (n_int - 1.))
+    w[0] *= .5
+    w[-1] *= .5
+    kr, kz, phi = k * np.hypot(x, y), k * z, np.arctan2(y, x)
+    pupil = w * np.sqrt(np.cos(t)) * np.sin(t) * np.exp(1j * kz * np.cos(t))
+    I0 = np.sum(pupil * (np.cos(t) + 1.) * jv(0, kr * np.sin(t)))
+    I1 = np.sum(pupil * np.sin(t) * jv(1, kr * np.sin(t)))
+    I2 = np.sum(pupil * (np.cos(t) - 1.) * jv(2, kr * np.sin(t)))
+    return I0 + I2 * np.cos(2 * phi), I2 * np.sin(2 * phi), -2j * I1 * np.cos(phi)

@@ -228,3 +228,20 @@ def test_absorbing_boundary(precision):
     cplx = bpm_ref.bpm_3d((N, N, Nz), (.1, .1, .1), dn=np.zeros((Nz, N, N), np.complex64),
                           absorbing_width=w, mean_mode="ignore", **kw)
     assert rel_l2(cplx, free) < (1e-12 if precision == "fp64" else 1e-5)
+
+
+def test_oracle_physical_quadrature_is_the_debye_integral():
+    """The oracle's quadrature="physical" octant equals the Debye integral evaluated point by
+    point with the reference test script's formula (tests/test_psf_vectorial.py:15-42 there),
+    to FP32 grid-coordinate rounding."""
+    from conftest import debye_point_fp64, rel_l2
+    NA, lam, dx = .95, .5, .008
+    shape = (64, 48, 32)
+    o = debye_ref.focus_field_debye(shape, (dx,) * 3, lam, NA, 1., 200, real_dtype=np.float64,
+                                    complex_dtype=np.complex128, quadrature="physical")
+    c, k = (32, 24, 16), 2 * np.pi / lam
+    pts = [(i, i // 2, l) for i in range(0, 32, 3) for l in (1, 7, 15)]
+    got = np.array([[o[q][c[2] + l, c[1] + j, c[0] + i] for q in (1, 2, 3)] for i, j, l in pts])
+    want = np.array([debye_point_fp64(i * dx, j * dx, l * dx, k, NA, 200) for i, j, l in pts])
+    for q in range(3):
+        assert rel_l2(got[:, q], want[:, q]) < 1e-6

@@ -3,7 +3,7 @@ reference's own kernel) and with the FP64 oracle. Tolerance: relative L2 <= 1e-4
 import numpy as np
 import pytest
 
-from conftest import PSF_GOLDEN, golden_psf_case, rel_l2
+from conftest import PSF_GOLDEN, debye_point_fp64, golden_psf_case, rel_l2
 from oracle import debye_ref
 
 pytestmark = pytest.mark.gpu
@@ -204,3 +204,38 @@ def test_tensor_core_status_is_clear(bpm):
     from bpm_gb300 import _native as N
     bpm.psf((128, 128, 128), (.1, .1, .1), .5, 1.1, 1.33, 200)
     assert N.lib().bpm_device_status(0) == 0
+
+
+@pytest.mark.parametrize("n_int", [200, 1000])
+def test_physical_quadrature_against_the_debye_integral(bpm, n_int):
+    """quadrature="physical" (sin t included, exact trapezoid) against the reference test
+    script's own point formula (NA 0.95, lambda 0.5, n0 1, dx 0.008 um as there) along the x
+    and y axes near the focus and off the focal plane, and against the oracle's octant;
+    relative L2 <= 1e-4. The default rule stays the reference kernel's (no sin t)."""
+    NA, lam, dx = .95, .5, .008
+    shape = (128, 96, 64)
+    u, ex, ey, ez = bpm.psf(shape, (dx,) * 3, lam, NA, 1., n_int, return_field=True, quadrature="physical")
+    c = (shape[0] // 2, shape[1] // 2, shape[2] // 2)
+    k = 2 * np.pi / lam
+    got, want = [], []
+    # grid index (cx + i, cy + j, cz + l) sits at (i dx, j dx, l dx) for i, j, l >= 0, l >= 1
+    for i, j, l in [(i, 0, 1) for i in range(0, 64, 3)] + [(0, j, 1) for j in range(0, 48, 3)] + \
+                   [(i, i // 2, l) for i in range(0, 40, 5) for l in (4, 17, 31)]:
+        got.append([ex[c[2] + l, c[1] + j, c[0] + i], ey[c[2] + l, c[1] + j, c[0] + i],
+                    ez[c[2] + l, c[1] + j, c[0] + i]])
+        want.append(debye_point_fp64(i * dx, j * dx, l * dx, k, NA, n_int))
+    got, want = np.array(got), np.array(want)
+    for comp in range(3):
+        if comp == 1:   # ey vanishes on the axes: compare where it does not
+            sel = np.abs(want[:, 1]) > 1e-3 * np.abs(want[:, 0]).max()
+            assert rel_l2(got[sel, 1], want[sel, 1]) < TOL
+        else:
+            assert rel_l2(got[:, comp], want[:, comp]) < TOL, comp
+    o = debye_ref.focus_field_debye(shape, (dx,) * 3, lam, NA, 1., n_int, real_dtype=np.float64,
+                                    complex_dtype=np.complex128, quadrature="physical")
+    for a, b, name in zip((u, ex, ey, ez), o, ("u", "ex", "ey", "ez")):
+        assert rel_l2(a, b) < TOL, name
+    ref = bpm.psf(shape, (dx,) * 3, lam, NA, 1., n_int)
+    assert rel_l2(ref, u) > 1e-2          # the reference rule (no sin t) is another PSF
+    with pytest.raises(ValueError):
+        bpm.psf(shape, (dx,) * 3, lam, NA, 1., n_int, quadrature="midpoint")
