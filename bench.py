@@ -180,6 +180,7 @@ def bench_ours(args, rank, world, local_rank):
     march = bpm_gb300.BatchedMarch((NX, NY, NZ), UNITS, LAM, N0, BATCH, dn=dn, mean_mode=MODE,
                                    out_kind="intensity", group=args.group or "auto")
     march.u0.copy_(u0)
+    launch = dict(march.launch)
     stream = torch.cuda.current_stream()
 
     def barrier():
@@ -280,7 +281,7 @@ def bench_ours(args, rank, world, local_rank):
     e2e_steps = min(max(15, args.steps), 25)
     for _ in range(1):
         bpm_gb300.bpm_3d_batched((NX, NY, NZ), UNITS, lam=LAM, u0=u0_h, dn=dn_h, n0=N0, return_field=False,
-                                 mean_mode=MODE, group=grp, out=out_h)
+                                 mean_mode=MODE, out=out_h, launch=launch)
     barrier()
     step_ms, step_gpu_ms = [], []
     t0 = time.perf_counter()
@@ -289,7 +290,7 @@ def bench_ours(args, rank, world, local_rank):
         e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
         e0.record()
         bpm_gb300.bpm_3d_batched((NX, NY, NZ), UNITS, lam=LAM, u0=u0_h, dn=dn_h, n0=N0, return_field=False,
-                                 mean_mode=MODE, group=grp, out=out_h)
+                                 mean_mode=MODE, out=out_h, launch=launch)
         e1.record()
         step_ms.append((time.perf_counter() - ts) * 1e3)
         e1.synchronize()
@@ -321,7 +322,7 @@ def bench_ours(args, rank, world, local_rank):
         "vs_baseline": None, "dtype": "c64", "data": "synthetic (seeded)",
         "config": {"workload": WORKLOAD, "nx": NX, "ny": NY, "nz": NZ,
                    "batch_per_gpu": BATCH, "units_um": UNITS, "lam_um": LAM, "n0": N0,
-                   "mean_mode": MODE, "output": "intensity volume", "group": grp,
+                   "mean_mode": MODE, "output": "intensity volume", "group": grp, "launch_shape": launch,
                    "dn": "gaussian random field corr 5 px sigma 0.02 clip 0.06 (shared)",
                    "u0": "64 plane waves, tilts area-uniform in NA 0.8",
                    "l2": "inputs larger than L2 (dn 256 MiB, output 16 GiB per step)",
@@ -591,7 +592,7 @@ def mixed_batch_timing(n=48, seed=5):
     # the same requests replayed as one CUDA graph (MixedBatch): groups of a grid and Nz march
     # together, every group a parallel branch
     mb = bpm_gb300.MixedBatch([BpmRequest((side, side, nz), UNITS, lam=LAM, n0=N0, u0=u0, dn=dns[side][:nz])
-                               for side, nz, u0 in reqs])
+                               for side, nz, u0 in reqs], tune=True)
     mb.run()
     torch.cuda.synchronize()
     a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
@@ -603,6 +604,8 @@ def mixed_batch_timing(n=48, seed=5):
     t_graph = a.elapsed_time(b) / 3 * 1e-3
     same = same and all(bool(torch.equal(mb.result(i), ref[i])) for i in range(0, n, 5))
     n_groups = len(mb.groups)
+    shapes = ["%dx%dx%d b%d: %s" % (g["u0"].shape[2], g["u0"].shape[1], g["out"].shape[1], g["u0"].shape[0],
+                                    g["launch"]) for g in mb.groups]
     del mb
     del dns, reqs, ref, out
     torch.cuda.empty_cache()
@@ -612,6 +615,7 @@ def mixed_batch_timing(n=48, seed=5):
             "speedup": t_seq / t_mix, "p50_ms": st["p50_ms"], "p99_ms": st["p99_ms"],
             "one_graph_ms": t_graph * 1e3, "one_graph_voxel_updates_per_s": vu / t_graph,
             "one_graph_groups": n_groups, "one_graph_speedup": t_seq / t_graph,
+            "one_graph_launch_shapes": shapes,
             "same_result_as_alone": same,
             "api": "bpm_gb300.serve.Server (all submitted at once) and bpm_gb300.MixedBatch (one CUDA graph) "
                    "vs bpm_gb300.bpm_3d per request"}

@@ -48,7 +48,8 @@ class Request(ctypes.Structure):
                 ("out", c_vp), ("out_kind", c_int), ("out_batch_stride", c_ll),
                 ("last_plane", c_vp), ("scatter_p", c_vp), ("scatter_g", c_vp),
                 ("scattering_plane_ind", c_int), ("group", c_int),
-                ("ckpt", c_vp), ("ckpt_every", c_int), ("mask", c_vp)]
+                ("ckpt", c_vp), ("ckpt_every", c_int), ("mask", c_vp),
+                ("conc", c_int), ("col_block", c_int), ("cluster", c_int)]
 
 
 class DebyeDesc(ctypes.Structure):
@@ -72,6 +73,7 @@ SIGNATURES = {
     "bpm_plan_destroy": (c_int, [c_vp]),
     "bpm_group_size": (c_int, [c_vp, c_int, c_int]),
     "bpm_workspace_bytes": (c_size, [c_vp, c_int, c_int]),
+    "bpm_workspace_bytes_conc": (c_size, [c_vp, c_int, c_int, c_int]),
     "bpm_propagate": (c_int, [c_vp, ctypes.POINTER(Request), c_vp, c_size, c_vp]),
     "bpm_mask_precompute": (c_int, [c_vp, c_vp, c_int, c_vp, c_vp]),
     "bpm_propagate_noalloc": (c_int, [c_vp, ctypes.POINTER(Request), c_vp]),

@@ -1,13 +1,24 @@
 """Autotuner for the launch shape of the batched march.
 
-The march advances `group` fields per kernel launch and up to four groups at the same
-time on separate streams (see bpm_workspace_bytes in include/bpm_gb300.h). The best group
-depends on the grid, the batch, the mean mode and the device: larger groups fill more of
-the GPU per launch, smaller ones keep every concurrent group's planes inside L2. The tuner
-times a short probe march (the same kernels on the first few dn slices, captured as a CUDA
-graph) for each candidate group, best of three trials, and keeps the largest group within
-3 % of the fastest (pick_group); results are cached per device and shape in a JSON file
-(BPM_GB300_TUNE_CACHE, default ~/.cache/bpm_gb300/autotune.json).
+A march's launch shape is four choices, none of which changes a result's bits (except the
+cluster kernel at 64x64, whose FFT has another radix order; see bpm_request in
+include/bpm_gb300.h):
+  group      fields advanced per kernel launch: larger groups fill more of the GPU per
+             launch and read a shared mask slice once for more fields, smaller ones keep
+             every concurrent group's planes inside L2;
+  conc       groups marching at once on their own streams (1, 2, 4, 8), so one group's
+             kernels fill the SMs another group's tail wave leaves idle;
+  col_block  columns per block of the non-weighted column passes (8 or 16): 8-column blocks
+             spread a small pass over twice the SMs, 16-column blocks issue fewer
+             instructions per column;
+  cluster    the whole-march cluster kernel (the field in distributed shared memory, square
+             64..256 grids) against the row/column pass kernels.
+The tuner times a short probe march for each candidate (the same kernels on the first few
+dn slices, captured as a CUDA graph, best of three trials): first the group (pick_group:
+the largest group within 3 % of the fastest), then each other choice in turn, which
+replaces the current one only when it is more than 3 % faster (pick_option). Results are
+cached per device, grid, batch and mode in a JSON file (BPM_GB300_TUNE_CACHE, default
+~/.cache/bpm_gb300/autotune.json).
 """
 import json
 import os
@@ -16,13 +27,14 @@ import torch
 
 from . import _native as N
 
-__all__ = ["tune_group", "pick_group", "cache_path"]
+__all__ = ["tune_shape", "tune_group", "pick_group", "pick_option", "shape_candidates", "cache_path"]
 
 _cache = None
+_VERSION = 2  # cache entries of another layout are measured again
 
 
 def cache_path():
-    """The JSON file of measured group sizes: BPM_GB300_TUNE_CACHE, else
+    """The JSON file of measured launch shapes: BPM_GB300_TUNE_CACHE, else
     ~/.cache/bpm_gb300/autotune.json."""
     return os.environ.get("BPM_GB300_TUNE_CACHE",
                           os.path.join(os.path.expanduser("~"), ".cache", "bpm_gb300", "autotune.json"))
@@ -64,25 +76,55 @@ def pick_group(times, tol=.03):
     return max(g for g, t in times.items() if t <= (1. + tol) * tmin)
 
 
-def tune_group(size, units, lam, n0, batch, dn, mean_mode="weighted", out_kind="intensity",
+def pick_option(current, t_current, times, tol=.03):
+    """The option to keep: the fastest of `times` (option -> ms) if it beats the current
+    choice by more than `tol`, else the current one."""
+    best = min(times, key=times.get)
+    if times[best] < (1. - tol) * t_current:
+        return best, times[best]
+    return current, t_current
+
+
+def shape_candidates(size, batch, group, mean_mode):
+    """The options of each launch-shape choice after the group that apply to a march of
+    `batch` fields in groups of `group` on grid `size` (0 is the library's own rule)."""
+    Nx, Ny = int(size[0]), int(size[1])
+    ngroups = -(-batch // max(1, group))
+    out = {}
+    if ngroups > 1:
+        out["conc"] = [1, 2, 4, 8]
+    if mean_mode != "weighted" and Ny >= 128:
+        out["col_block"] = [8, 16]    # the weighted passes keep 16-column blocks
+    if Nx == Ny and Nx in (64, 128, 256):
+        out["cluster"] = [1, 2]
+    return out
+
+
+def _key(size, batch, mean_mode, dn_kind, out_kind, absorbing_width):
+    dev = torch.cuda.get_device_properties(torch.cuda.current_device()).name
+    Nx, Ny = int(size[0]), int(size[1])
+    return "%s|%dx%d|b%d|%s|dn%d|%s|aw%d" % (dev, Nx, Ny, batch, mean_mode, dn_kind, out_kind, absorbing_width)
+
+
+def tune_shape(size, units, lam, n0, batch, dn, mean_mode="weighted", out_kind="intensity",
                absorbing_width=0, nz_probe=12, reps=3, trials=3, force=False):
-    """Fields per launch that march `batch` fields of grid `size` fastest on this device.
-    dn: the (Nz, Ny, Nx) volume of the real run (its first slices drive the probe)."""
+    """Launch shape {group, conc, col_block, cluster} that marches `batch` fields of grid
+    `size` fastest on this device. dn: the (Nz, Ny, Nx) volume of the real run (its first
+    slices drive the probe)."""
     from .bpm3d import BatchedMarch, _dn_kind
 
     Nx, Ny, Nz = (int(s) for s in size)
     kind, _ = _dn_kind(dn, False)
-    dev = torch.cuda.get_device_properties(torch.cuda.current_device()).name
-    key = "%s|%dx%d|b%d|%s|dn%d|%s|aw%d" % (dev, Nx, Ny, batch, mean_mode, kind, out_kind, absorbing_width)
+    key = _key(size, batch, mean_mode, kind, out_kind, absorbing_width)
     cache = _load()
-    if not force and key in cache:
-        return int(cache[key]["group"])
+    if not force and key in cache and cache[key].get("version") == _VERSION:
+        return dict(cache[key]["shape"])
     nzp = max(2, min(Nz, nz_probe))
     dnp = dn[:nzp] if dn is not None else None
-    times = {}
-    for g in _candidates(batch):
+
+    def probe(shape):
         m = BatchedMarch((Nx, Ny, nzp), units, lam, n0, batch, dn=dnp, mean_mode=mean_mode,
-                         absorbing_width=absorbing_width, out_kind=out_kind, group=g)
+                         absorbing_width=absorbing_width, out_kind=out_kind, group=shape["group"], launch=shape)
         m.run()
         torch.cuda.synchronize()
         a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
@@ -94,9 +136,24 @@ def tune_group(size, units, lam, n0, batch, dn, mean_mode="weighted", out_kind="
             b.record()
             torch.cuda.synchronize()
             t = min(t, a.elapsed_time(b) / reps)
-        times[g] = t
         del m
-    best = pick_group(times)
-    cache[key] = {"group": int(best), "ms_probe": times, "nz_probe": nzp}
+        return t
+
+    base = {"group": 0, "conc": 0, "col_block": 0, "cluster": 0}
+    log = {"group": {g: probe(dict(base, group=g)) for g in _candidates(batch)}}
+    g = pick_group(log["group"])
+    shape, t_best = dict(base, group=g), log["group"][g]
+    for axis, options in shape_candidates((Nx, Ny), batch, g, mean_mode).items():
+        log[axis] = {v: probe(dict(shape, **{axis: v})) for v in options}
+        choice, t_best = pick_option(shape[axis], t_best, log[axis])
+        shape[axis] = int(choice)
+    cache[key] = {"version": _VERSION, "shape": shape, "group": int(g), "nz_probe": nzp,
+                  "ms_probe": {a: {str(k): v for k, v in d.items()} for a, d in log.items()}}
     _save()
-    return int(best)
+    return dict(shape)
+
+
+def tune_group(size, units, lam, n0, batch, dn, mean_mode="weighted", out_kind="intensity",
+               absorbing_width=0, **kw):
+    """Fields per launch of the tuned launch shape (tune_shape)."""
+    return int(tune_shape(size, units, lam, n0, batch, dn, mean_mode, out_kind, absorbing_width, **kw)["group"])

@@ -109,8 +109,8 @@ class Plan:
                 N.check(L.bpm_plan_create(ctypes.byref(self.desc), ctypes.byref(h)), "bpm_plan_create")
         self.handle = h
 
-    def workspace_bytes(self, batch, group=0):
-        return int(N.lib().bpm_workspace_bytes(self.handle, int(batch), int(group)))
+    def workspace_bytes(self, batch, group=0, conc=0):
+        return int(N.lib().bpm_workspace_bytes_conc(self.handle, int(batch), int(group), int(conc)))
 
     def __del__(self):
         h = getattr(self, "handle", None)
@@ -214,8 +214,18 @@ def precompute_mask(plan, dn_t, dn_kind):
     return mask
 
 
+def _apply_launch(req, launch):
+    """Set the launch-shape fields of a request from a dict with keys conc, col_block,
+    cluster (absent or 0: the library's rule; see bpm_request in include/bpm_gb300.h)."""
+    if launch:
+        req.conc = int(launch.get("conc", 0))
+        req.col_block = int(launch.get("col_block", 0))
+        req.cluster = int(launch.get("cluster", 0))
+    return req
+
+
 def _run(plan, u0_t, dn_t, dn_kind, dn_bstride, out_kind, want_last=True, scattering=False,
-         return_g=False, scattering_plane_ind=0, slice_tabs=(None, None), group=0, mask=None):
+         return_g=False, scattering_plane_ind=0, slice_tabs=(None, None), group=0, mask=None, launch=None):
     """Launch bpm_propagate on the current stream. u0_t: (B, Ny, Nx) complex64 CUDA tensor."""
     Nx, Ny, Nz = plan.size
     B = u0_t.shape[0]
@@ -228,11 +238,12 @@ def _run(plan, u0_t, dn_t, dn_kind, dn_bstride, out_kind, want_last=True, scatte
     last = torch.empty((B, Ny, Nx), dtype=torch.complex64, device=dev) if want_last else None
     p = torch.empty((B, Nz), dtype=torch.float32, device=dev) if scattering else None
     g = torch.empty((B, Nz), dtype=torch.float32, device=dev) if (scattering and return_g) else None
-    wsb = plan.workspace_bytes(B, group)
+    wsb = plan.workspace_bytes(B, group, (launch or {}).get("conc", 0))
     ws = torch.empty(wsb, dtype=torch.uint8, device=dev)
     req = N.Request(B, _ptr(u0_t), _ptr(dn_t), dn_kind, int(dn_bstride), _ptr(slice_tabs[0]),
                     _ptr(slice_tabs[1]), _ptr(out), out_kind, Nz * Ny * Nx, _ptr(last), _ptr(p),
                     _ptr(g), int(scattering_plane_ind), int(group), None, 0, _ptr(mask))
+    _apply_launch(req, launch)
     N.check(N.lib().bpm_propagate(plan.handle, ctypes.byref(req), _ptr(ws), wsb, _stream_ptr()),
             "bpm_propagate")
     return out, last, p, g
@@ -398,14 +409,18 @@ def _bpm_3d_split(size, units, lam=.5, u0=None, dn=None, n_volumes=1, n0=1., sub
 
 def bpm_3d_batched(size, units, lam=.5, u0=None, dn=None, n0=1., return_full=True, return_field=True,
                    absorbing_width=0, use_fresnel_approx=False, store_dn_as_half=False,
-                   mean_mode="weighted", group=0, out=None):
+                   mean_mode="weighted", group=0, out=None, launch=None):
     """Batched bpm_3d (bpm/bpm/bpm_3d.py:39, once per field): u0 of shape (B, Ny, Nx)
     marches through one shared dn (Nz, Ny, Nx),
     or through per-field dn volumes of shape (B, Nz, Ny, Nx). Each field's result equals
     bpm_3d on that field alone. Returns (B, Nz, Ny, Nx) volumes or (B, Ny, Nx) last planes.
     `out`, if given, is a host buffer of the result's shape and dtype (a numpy array or a
-    CPU tensor, ideally pinned) that receives the result and is returned.
+    CPU tensor, ideally pinned) that receives the result and is returned. `launch`: a
+    launch shape (keys group, conc, col_block, cluster; autotune.tune_shape gives one) that
+    never changes the result's bits except cluster at 64x64.
     No counterpart in the reference, which marches one field per call."""
+    if launch and not group:
+        group = int(launch.get("group", 0))
     _validate(mean_mode, 1, False, False)
     Nx, Ny, Nz = (int(s) for s in size)
     as_tensor = _is_tensor(u0) or _is_tensor(dn)
@@ -445,12 +460,12 @@ def bpm_3d_batched(size, units, lam=.5, u0=None, dn=None, n0=1., return_full=Tru
         if tuple(host.shape) != (B, Nz, Ny, Nx) or host.dtype != vdt:
             raise ValueError("out must have shape %s and dtype %s" % ((B, Nz, Ny, Nx), vdt))
         if host.is_contiguous() and host.is_pinned():
-            _run_streamed_to_host(plan, u0_t, dn_t, kind, bstride, out_kind, tabs, group, mask, host)
+            _run_streamed_to_host(plan, u0_t, dn_t, kind, bstride, out_kind, tabs, group, mask, host, launch=launch)
         else:
-            _run_to_host(plan, u0_t, dn_t, kind, bstride, out_kind, tabs, group, mask, host)
+            _run_to_host(plan, u0_t, dn_t, kind, bstride, out_kind, tabs, group, mask, host, launch=launch)
         return out
     vol, last, _, _ = _run(plan, u0_t, dn_t, kind, bstride, out_kind, True, slice_tabs=tabs, group=group,
-                           mask=mask)
+                           mask=mask, launch=launch)
     res = vol if return_full else (last if return_field else last.abs() ** 2)
     if out is not None:
         host = torch.from_numpy(out) if isinstance(out, np.ndarray) else out
@@ -462,7 +477,8 @@ def bpm_3d_batched(size, units, lam=.5, u0=None, dn=None, n0=1., return_full=Tru
     return res if as_tensor else _d2h(res)
 
 
-def _run_streamed_to_host(plan, u0_t, dn_t, kind, bstride, out_kind, tabs, group, mask, host, chunk_planes=16):
+def _run_streamed_to_host(plan, u0_t, dn_t, kind, bstride, out_kind, tabs, group, mask, host, chunk_planes=16,
+                          launch=None):
     """March the whole batch into a device volume while the library's copy stream moves
     each finished run of `chunk_planes` planes into the page-locked host buffer
     (bpm_propagate_to_host), so the device->host copy runs alongside the march."""
@@ -472,17 +488,18 @@ def _run_streamed_to_host(plan, u0_t, dn_t, kind, bstride, out_kind, tabs, group
     vdt = torch.complex64 if out_kind == N.OUT_FIELD else torch.float32
     vol = torch.empty((B, Nz, Ny, Nx), dtype=vdt, device=dev)
     last = torch.empty((B, Ny, Nx), dtype=torch.complex64, device=dev)
-    wsb = plan.workspace_bytes(B, group)
+    wsb = plan.workspace_bytes(B, group, (launch or {}).get("conc", 0))
     ws = torch.empty(wsb, dtype=torch.uint8, device=dev)
     req = N.Request(B, _ptr(u0_t), _ptr(dn_t), kind, int(bstride), _ptr(tabs[0]), _ptr(tabs[1]), _ptr(vol),
                     out_kind, Nz * Ny * Nx, _ptr(last), None, None, 0, int(group), None, 0, _ptr(mask))
+    _apply_launch(req, launch)
     N.check(N.lib().bpm_propagate_to_host(plan.handle, ctypes.byref(req), ctypes.c_void_p(host.data_ptr()),
                                           int(chunk_planes), _ptr(ws), wsb, _stream_ptr()),
             "bpm_propagate_to_host")
     torch.cuda.current_stream().synchronize()
 
 
-def _run_to_host(plan, u0_t, dn_t, kind, bstride, out_kind, tabs, group, mask, host):
+def _run_to_host(plan, u0_t, dn_t, kind, bstride, out_kind, tabs, group, mask, host, launch=None):
     """March a batch in chunks of fields into two alternating device volumes while a copy
     stream drains the previous chunk to the host buffer, so the device->host copy of the
     output volumes overlaps the march of the next chunk."""
@@ -495,7 +512,7 @@ def _run_to_host(plan, u0_t, dn_t, kind, bstride, out_kind, tabs, group, mask, h
     vdt = torch.complex64 if out_kind == N.OUT_FIELD else torch.float32
     bufs = [torch.empty((min(chunk, B), Nz, Ny, Nx), dtype=vdt, device=dev) for _ in range(2 if B > chunk else 1)]
     last = torch.empty((min(chunk, B), Ny, Nx), dtype=torch.complex64, device=dev)
-    wsb = plan.workspace_bytes(min(chunk, B), group)
+    wsb = plan.workspace_bytes(min(chunk, B), group, (launch or {}).get("conc", 0))
     ws = torch.empty(wsb, dtype=torch.uint8, device=dev)
     cs = torch.cuda.current_stream()
     copy_s = torch.cuda.Stream(device=dev)
@@ -509,6 +526,7 @@ def _run_to_host(plan, u0_t, dn_t, kind, bstride, out_kind, tabs, group, mask, h
         req = N.Request(nb, _ptr(u0_t[b0:b0 + nb]), _ptr(dn_k), kind, int(bstride), _ptr(tabs[0]),
                         _ptr(tabs[1]), _ptr(buf), out_kind, Nz * Ny * Nx, _ptr(last), None, None, 0,
                         int(group), None, 0, _ptr(mask))
+        _apply_launch(req, launch)
         N.check(N.lib().bpm_propagate(plan.handle, ctypes.byref(req), _ptr(ws), wsb, _stream_ptr()),
                 "bpm_propagate")
         done = torch.cuda.Event()
@@ -530,7 +548,7 @@ class BatchedMarch:
 
     def __init__(self, size, units, lam, n0, batch, dn=None, mean_mode="weighted", absorbing_width=0,
                  out_kind="intensity", prop_kind=N.PROP_FUNCTIONAL, group=0, store_dn_as_half=False,
-                 use_graph=True, use_mask=True):
+                 use_graph=True, use_mask=True, launch=None):
         dev = _device()
         Nx, Ny, Nz = (int(s) for s in size)
         self.size = (Nx, Ny, Nz)
@@ -550,13 +568,18 @@ class BatchedMarch:
         elif ok == N.OUT_INTENSITY:
             self.out = torch.empty((batch, Nz, Ny, Nx), dtype=torch.float32, device=dev)
         self.last = torch.empty((batch, Ny, Nx), dtype=torch.complex64, device=dev)
+        # group="auto": the autotuner's launch shape (fields per launch, concurrent groups,
+        # column block, cluster kernel) for this device, grid, batch and mode
         if group == "auto":
-            from .autotune import tune_group
-            group = tune_group(self.size, units, lam, n0, batch, dn if dn is None else self.dn, mean_mode,
-                               out_kind, absorbing_width)
+            from .autotune import tune_shape
+            launch = tune_shape(self.size, units, lam, n0, batch, dn if dn is None else self.dn, mean_mode,
+                                out_kind, absorbing_width)
+            group = launch["group"]
+        self.launch = dict(launch or {})
+        self.launch["group"] = int(group)
         self.group = int(group)
         self.group_used = int(N.lib().bpm_group_size(self.plan.handle, self.batch, self.group))
-        self.ws_bytes = self.plan.workspace_bytes(batch, group)
+        self.ws_bytes = self.plan.workspace_bytes(batch, group, self.launch.get("conc", 0))
         self.ws = torch.empty(self.ws_bytes, dtype=torch.uint8, device=dev)
         # the phase masks of a shared dn are computed once and reused by every run
         self.mask = (precompute_mask(self.plan, self.dn, kind)
@@ -565,6 +588,7 @@ class BatchedMarch:
                              _ptr(self.tabs[0]), _ptr(self.tabs[1]), _ptr(self.out), ok,
                              Nz * Ny * Nx, _ptr(self.last), None, None, 0, self.group, None, 0,
                              _ptr(self.mask))
+        _apply_launch(self.req, self.launch)
         self.exec = None
         if use_graph:
             torch.cuda.synchronize()
@@ -601,7 +625,7 @@ class MixedBatch:
     Each request's |u|^2 volume (out_kind "intensity") or field volume ("field") is result(i);
     its exit field last(i). A group is bit-identical to the same requests marched alone."""
 
-    def __init__(self, requests, out_kind="intensity", use_graph=True):
+    def __init__(self, requests, out_kind="intensity", use_graph=True, tune=False):
         dev = _device()
         ok = {"field": N.OUT_FIELD, "intensity": N.OUT_INTENSITY}[out_kind]
         self.requests = list(requests)
@@ -637,12 +661,18 @@ class MixedBatch:
             shape = (B, Nz, Ny, Nx)
             out = torch.empty(shape, dtype=torch.complex64 if ok == N.OUT_FIELD else torch.float32, device=dev)
             last = torch.empty((B, Ny, Nx), dtype=torch.complex64, device=dev)
-            wsb = plan.workspace_bytes(B, 0)
+            launch = {}
+            if tune:
+                from .autotune import tune_shape
+                launch = tune_shape((Nx, Ny, Nz), r0.units, r0.lam, r0.n0, B, dn, r0.mean_mode, out_kind,
+                                    r0.absorbing_width)
+            wsb = plan.workspace_bytes(B, launch.get("group", 0), launch.get("conc", 0))
             ws = torch.empty(wsb, dtype=torch.uint8, device=dev)
             req = N.Request(B, _ptr(u0), _ptr(dn), kind, 0, None, None, _ptr(out), ok, Nz * Ny * Nx, _ptr(last),
-                            None, None, 0, 0, None, 0, _ptr(mask))
+                            None, None, 0, int(launch.get("group", 0)), None, 0, _ptr(mask))
+            _apply_launch(req, launch)
             self.groups.append(dict(plan=plan, u0=u0, dn=dn, mask=mask, out=out, last=last, ws=ws, wsb=wsb,
-                                    req=req, stream=torch.cuda.Stream(device=dev)))
+                                    req=req, stream=torch.cuda.Stream(device=dev), launch=launch))
             for k, i in enumerate(idx):
                 self.where[i] = (gi, k)
         torch.cuda.synchronize()

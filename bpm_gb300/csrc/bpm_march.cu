@@ -438,6 +438,7 @@ struct ColParams {
   const float2* tw;
   const float2* wtw;         // stage-ordered twiddles of the warp FFT
   int dn_stage;              // weighted: dn rows may be staged with 16-byte cp.async
+  int col_block;             // 0: the library's rule; 8 or 16 columns per non-weighted block
 };
 
 template <int T>
@@ -1539,7 +1540,8 @@ struct ColK {
     // as many SMs share it (the columns' arithmetic is the same); so does every non-weighted
     // pass with 32 values per thread, whose 16-column blocks take half an SM's registers
     if constexpr (WHICH == 0) {
-      if (!p.scat && ((int)(g.x * g.y) < sm_count() || N / L >= 32)) {
+      const bool narrow = p.col_block == 8 || (p.col_block == 0 && ((int)(g.x * g.y) < sm_count() || N / L >= 32));
+      if (!p.scat && narrow) {
         BPM_CUDA_TRY(launch_dep(col_split_kernel<N, 0, 8, false, L>, dim3(g.x * 2, g.y), dim3(8 * L),
                                 split8_smem<L>(), s, p));
         BPM_LAUNCH_CHECK("col_split_kernel");
@@ -1675,6 +1677,12 @@ int check_request(const bpm_plan* pl, const bpm_request* r) {
   if (r->out_kind != BPM_OUT_NONE && !r->out) { set_error("out is NULL but out_kind is set"); return BPM_ERR_ARG; }
   if (r->scatter_g && !r->scatter_p) { set_error("scatter_g needs scatter_p"); return BPM_ERR_ARG; }
   if (r->group < 0) { set_error("group must be >= 0"); return BPM_ERR_ARG; }
+  if (r->conc < 0 || r->conc > kMaxConcurrentGroups) { set_error("conc must be in 0..8"); return BPM_ERR_ARG; }
+  if (r->col_block != 0 && r->col_block != 8 && r->col_block != 16) {
+    set_error("col_block must be 0, 8 or 16");
+    return BPM_ERR_ARG;
+  }
+  if (r->cluster < 0 || r->cluster > 2) { set_error("cluster must be 0, 1 or 2"); return BPM_ERR_ARG; }
   if (r->ckpt && r->ckpt_every < 1) { set_error("ckpt_every must be >= 1 with ckpt"); return BPM_ERR_ARG; }
   if (r->mask && (r->dn_dtype == BPM_DN_NONE || r->dn_batch_stride != 0 || ((uintptr_t)r->mask & 7))) {
     set_error("mask needs one shared dn volume and 8-byte alignment");
@@ -1800,6 +1808,7 @@ MarchCtx make_ctx(const bpm_plan* pl, const bpm_request* r, void* ws, int b0, in
                   ((size_t)r->dn_batch_stride * es) % 16 == 0 && ((size_t)nx * es) % 16 == 0;
   }
 
+  cp.col_block = r->col_block;
   c.grow = dim3(ny / 16, Gc);
   c.gcol = dim3(nx / 16, Gc);
   return c;
@@ -1949,7 +1958,8 @@ struct ClusterK {
 constexpr int kNotCluster = 1;
 int try_cluster_march(const bpm_plan* pl, const bpm_request* r, void* ws, cudaStream_t s) {
   const bpm_grid_desc& d = pl->d;
-  if (d.nx != d.ny || !cluster_enabled(d.nx) || r->scatter_p || r->ckpt || !pl->wtw_x || !pl->wtw_y) return kNotCluster;
+  const bool want = r->cluster == 1 || (r->cluster == 0 && cluster_enabled(d.nx));
+  if (d.nx != d.ny || !want || r->scatter_p || r->ckpt || !pl->wtw_x || !pl->wtw_y) return kNotCluster;
   switch (d.nx) {
     case 64: return ClusterK<64>::ready() ? ClusterK<64>::launch(pl, r, ws, s) : kNotCluster;
     case 128: return ClusterK<128>::ready() ? ClusterK<128>::launch(pl, r, ws, s) : kNotCluster;
@@ -1986,7 +1996,7 @@ int enqueue_march(bpm_plan* pl, const bpm_request* r, void* ws, size_t ws_bytes,
   const int ngroups = (r->batch + G - 1) / G;
   const size_t slot = ws_layout(pl, G).total;
   const int conc = std::max(
-      1, (int)std::min<size_t>({(size_t)ngroups, ws_bytes / slot, (size_t)conc_limit()}));
+      1, (int)std::min<size_t>({(size_t)ngroups, ws_bytes / slot, (size_t)(r->conc > 0 ? r->conc : conc_limit())}));
   cudaStream_t st[kMaxConcurrentGroups];
   for (int j = 0; j < conc; j++) st[j] = conc > 1 ? pl->aux[j] : s;
   if (conc > 1 || sink) BPM_CUDA_TRY(cudaEventRecord(pl->ev_fork, s));
@@ -2359,11 +2369,15 @@ extern "C" int bpm_group_size(const bpm_plan* pl, int batch, int group) {
   return group > 0 ? std::min(group, batch) : default_group(pl, batch);
 }
 
-extern "C" size_t bpm_workspace_bytes(const bpm_plan* pl, int batch, int group) {
-  if (!pl || batch < 1) return 0;
+extern "C" size_t bpm_workspace_bytes_conc(const bpm_plan* pl, int batch, int group, int conc) {
+  if (!pl || batch < 1 || conc < 0 || conc > kMaxConcurrentGroups) return 0;
   const int G = group > 0 ? std::min(group, batch) : default_group(pl, batch);
   const int ngroups = (batch + G - 1) / G;
-  return (size_t)std::min(ngroups, conc_limit()) * ws_layout(pl, G).total;
+  return (size_t)std::min(ngroups, conc > 0 ? conc : conc_limit()) * ws_layout(pl, G).total;
+}
+
+extern "C" size_t bpm_workspace_bytes(const bpm_plan* pl, int batch, int group) {
+  return bpm_workspace_bytes_conc(pl, batch, group, 0);
 }
 
 extern "C" int bpm_propagate(bpm_plan* pl, const bpm_request* r, void* ws, size_t ws_bytes, void* stream) {

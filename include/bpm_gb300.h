@@ -103,6 +103,14 @@ typedef struct {
   const void* mask;              /* device (nz, ny, nx) complex64 phase masks of the shared dn
                                     from bpm_mask_precompute, or NULL to form them on the fly
                                     (results are bit-identical either way)                     */
+  /* Launch shape (0 = the library's rule for each). None changes a result's bits, except
+   * cluster at 64x64, where the two families run FFTs of another radix order (FP32 rounding). */
+  int conc;                      /* groups marching at once on their own streams, 1..8
+                                    (default BPM_GB300_CONC, else 4)                            */
+  int col_block;                 /* columns per block of the non-weighted column passes, 8 or 16 */
+  int cluster;                   /* whole-march cluster kernel (square 64..256 grids without
+                                    scattering sums or checkpoints): 1 = use it, 2 = row/column
+                                    pass kernels (default: cluster at 64 and 128)               */
 } bpm_request;
 
 /* Library version (BPM_GB300_VERSION). */
@@ -150,6 +158,9 @@ int bpm_group_size(const bpm_plan* plan, int batch, int group);
  * to the caller's stream). Any workspace of at least one slot works; smaller ones march
  * the groups one after another. */
 size_t bpm_workspace_bytes(const bpm_plan* plan, int batch, int group);
+
+/* The same for `conc` groups marching at once (a request's conc; 0 = the default). */
+size_t bpm_workspace_bytes_conc(const bpm_plan* plan, int batch, int group, int conc);
 
 /* March every field of the request through all nz slices.
  * Replaces the hot loop of bpm/bpm/bpm_3d.py:_bpm_3d (:283-381, one fft / reduction /

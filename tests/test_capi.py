@@ -157,3 +157,16 @@ def test_serve_overlap_count():
     assert overlapped([(0., 1.), (1., 2.)]) == 0            # touching intervals do not overlap
     assert overlapped([(0., 2.), (1., 3.), (4., 5.)]) == 2
     assert overlapped([(0., 10.), (1., 2.), (3., 4.), (11., 12.)]) == 3
+
+
+def test_autotune_shape_choices():
+    """The launch-shape search: an option replaces the current choice only when more than 3 %
+    faster; the choices offered depend on the grid, the number of groups and the mode."""
+    from bpm_gb300.autotune import pick_option, shape_candidates
+    assert pick_option(0, 10., {1: 9.8, 2: 9.9}) == (0, 10.)          # within 3 %: keep
+    assert pick_option(0, 10., {1: 9.0, 8: 9.5}) == (1, 9.0)
+    c = shape_candidates((512, 512), 64, 8, "weighted")
+    assert c == {"conc": [1, 2, 4, 8]}                                 # weighted passes keep 16 columns
+    c = shape_candidates((256, 256), 4, 4, "ignore")
+    assert c == {"col_block": [8, 16], "cluster": [1, 2]}              # one group: no concurrency choice
+    assert "cluster" not in shape_candidates((512, 256), 8, 2, "ignore")
