@@ -29,7 +29,7 @@ PROP_FUNCTIONAL = 0
 PROP_CLASS = 1
 DN_NONE, DN_F32, DN_F16, DN_C64 = 0, 1, 2, 3
 OUT_NONE, OUT_FIELD, OUT_INTENSITY = 0, 1, 2
-PASS_FIRST_ROW, PASS_COLUMN, PASS_COLUMN_REDUCE, PASS_COLUMN_PROPAGATE, PASS_ROW = 0, 1, 2, 3, 4
+PASS_FIRST_ROW, PASS_COLUMN, PASS_COLUMN_REDUCE, PASS_COLUMN_PROPAGATE, PASS_ROW, PASS_COLUMN_FUSED = 0, 1, 2, 3, 4, 5
 
 
 class GridDesc(ctypes.Structure):
@@ -49,7 +49,7 @@ class Request(ctypes.Structure):
                 ("last_plane", c_vp), ("scatter_p", c_vp), ("scatter_g", c_vp),
                 ("scattering_plane_ind", c_int), ("group", c_int),
                 ("ckpt", c_vp), ("ckpt_every", c_int), ("mask", c_vp),
-                ("conc", c_int), ("col_block", c_int), ("cluster", c_int)]
+                ("conc", c_int), ("col_block", c_int), ("cluster", c_int), ("col_fuse", c_int)]
 
 
 class DebyeDesc(ctypes.Structure):

@@ -1,6 +1,6 @@
 """Autotuner for the launch shape of the batched march.
 
-A march's launch shape is four choices, none of which changes a result's bits (except the
+A march's launch shape is five choices, none of which changes a result's bits (except the
 cluster kernel at 64x64, whose FFT has another radix order; see bpm_request in
 include/bpm_gb300.h):
   group      fields advanced per kernel launch: larger groups fill more of the GPU per
@@ -12,7 +12,9 @@ include/bpm_gb300.h):
              spread a small pass over twice the SMs, 16-column blocks issue fewer
              instructions per column;
   cluster    the whole-march cluster kernel (the field in distributed shared memory, square
-             64..256 grids) against the row/column pass kernels.
+             64..256 grids) against the row/column pass kernels;
+  col_fuse   the weighted mode's one fused column pass (a thread-block cluster per field)
+             against its two column passes.
 The tuner times a short probe march for each candidate (the same kernels on the first few
 dn slices, captured as a CUDA graph, best of three trials): first the group (pick_group:
 the largest group within 3 % of the fastest), then each other choice in turn, which
@@ -30,7 +32,7 @@ from . import _native as N
 __all__ = ["tune_shape", "tune_group", "pick_group", "pick_option", "shape_candidates", "cache_path"]
 
 _cache = None
-_VERSION = 2  # cache entries of another layout are measured again
+_VERSION = 3  # cache entries of another layout are measured again
 
 
 def cache_path():
@@ -97,6 +99,8 @@ def shape_candidates(size, batch, group, mean_mode):
         out["col_block"] = [8, 16]    # the weighted passes keep 16-column blocks
     if Nx == Ny and Nx in (64, 128, 256):
         out["cluster"] = [1, 2]
+    if mean_mode == "weighted" and Ny in (128, 256, 512) and Nx % 32 == 0 and Nx <= 512:
+        out["col_fuse"] = [1, 2]
     return out
 
 
@@ -108,7 +112,7 @@ def _key(size, batch, mean_mode, dn_kind, out_kind, absorbing_width):
 
 def tune_shape(size, units, lam, n0, batch, dn, mean_mode="weighted", out_kind="intensity",
                absorbing_width=0, nz_probe=12, reps=3, trials=3, force=False):
-    """Launch shape {group, conc, col_block, cluster} that marches `batch` fields of grid
+    """Launch shape {group, conc, col_block, cluster, col_fuse} that marches `batch` fields of grid
     `size` fastest on this device. dn: the (Nz, Ny, Nx) volume of the real run (its first
     slices drive the probe)."""
     from .bpm3d import BatchedMarch, _dn_kind
@@ -139,7 +143,7 @@ def tune_shape(size, units, lam, n0, batch, dn, mean_mode="weighted", out_kind="
         del m
         return t
 
-    base = {"group": 0, "conc": 0, "col_block": 0, "cluster": 0}
+    base = {"group": 0, "conc": 0, "col_block": 0, "cluster": 0, "col_fuse": 0}
     log = {"group": {g: probe(dict(base, group=g)) for g in _candidates(batch)}}
     g = pick_group(log["group"])
     shape, t_best = dict(base, group=g), log["group"][g]

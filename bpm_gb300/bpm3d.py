@@ -216,11 +216,13 @@ def precompute_mask(plan, dn_t, dn_kind):
 
 def _apply_launch(req, launch):
     """Set the launch-shape fields of a request from a dict with keys conc, col_block,
-    cluster (absent or 0: the library's rule; see bpm_request in include/bpm_gb300.h)."""
+    cluster, col_fuse (absent or 0: the library's rule; see bpm_request in
+    include/bpm_gb300.h)."""
     if launch:
         req.conc = int(launch.get("conc", 0))
         req.col_block = int(launch.get("col_block", 0))
         req.cluster = int(launch.get("cluster", 0))
+        req.col_fuse = int(launch.get("col_fuse", 0))
     return req
 
 

@@ -439,6 +439,7 @@ struct ColParams {
   const float2* wtw;         // stage-ordered twiddles of the warp FFT
   int dn_stage;              // weighted: dn rows may be staged with 16-byte cp.async
   int col_block;             // 0: the library's rule; 8 or 16 columns per non-weighted block
+  int col_fuse;              // weighted: 1 one fused column pass where available, 0 or 2 two passes
 };
 
 template <int T>
@@ -1069,6 +1070,184 @@ col_split_kernel(ColParams p) {
 }
 
 // ---------------------------------------------------------------------------------------
+// Weighted column pass in one launch (Ny = N in {128, 256, 512}, no scattering sums): the
+// plane-wide sums sit between the forward column FFT and the propagator, so the two
+// column passes of the weighted mode (col_split_kernel<N, 1> and <N, 2>) become one kernel
+// whose blocks of a field form a thread-block cluster. A block is two 16-column tiles side
+// by side (two halves of 512 threads, each laid out and computing exactly as one block of
+// col_split_kernel: the same FFT stages, the same per-tile partial sums in the same order),
+// so a field of nx / 16 tiles is a cluster of nx / 32 blocks (16 at nx = 512). Each half
+// stores its tile's two partials in shared memory; after a cluster barrier (a hardware
+// barrier over blocks the launch co-schedules: no block waits on a block that has not
+// started), one warp per block reads all of the field's partials through distributed
+// shared memory in tile order and sums them as col_split_kernel<N, 2> does, so every block
+// gets the same n = n0 + dn0 bit for bit. The forward-transformed tile never leaves the
+// registers: propagator, inverse FFT and the coalesced store follow directly. A last
+// cluster barrier keeps each block's partials alive until every block has read them.
+// Results equal the two-pass march bit for bit. Opt-in (bpm_request.col_fuse = 1): a
+// cluster of 16 blocks that each fill an SM is placed on few GPCs at a time, and at
+// 512 x 512 (8 fields per launch, GB300) the fused pass took 41.2 us against 9.7 + 9.6 us
+// for the two passes.
+// ---------------------------------------------------------------------------------------
+template <int N>
+struct FusedCfg {
+  using Half = ColSplitCfg<N, kColWarps, 32>;
+  static constexpr int T = 2 * kColWarps * 32;                  // 1024 threads: two 16-column tiles
+  static constexpr int TW_F2 = Half::TW_F2;
+  static constexpr int BUFS_F2 = 2 * kColWarps * Half::STRIDE;  // two halves' column buffers
+  static constexpr int DN_F2 = (TW_F2 + BUFS_F2 + 1) & ~1;     // 16-byte aligned
+  static constexpr int KY_F = 2 * 16 * N;                       // ky^2 after the two dn tiles (floats)
+  static constexpr size_t SMEM = (size_t)DN_F2 * sizeof(float2) + (size_t)(KY_F + N) * sizeof(float);
+};
+
+template <int N>
+__global__ void __launch_bounds__(FusedCfg<N>::T, 1) col_fused_kernel(ColParams p) {
+  using Cfg = FusedCfg<N>;
+  using Half = typename Cfg::Half;
+  constexpr int L = 32;
+  constexpr int E = N / L;
+  constexpr int C = kColWarps;  // columns per half
+  constexpr int TH = C * L;     // threads per half
+  constexpr int T = Cfg::T;
+  extern __shared__ __align__(16) float2 smem[];
+  __shared__ float red[2][32];
+  __shared__ float part[2][2];  // this block's two tile partials (sum |u| dn, sum |u|)
+  __shared__ float s_n;
+  namespace cg = cooperative_groups;
+  cg::cluster_group cl = cg::this_cluster();
+  const int h = threadIdx.x / TH, ht = threadIdx.x % TH;
+  const int warp = threadIdx.x >> 5, t = threadIdx.x & 31;
+  const int r0 = ht / C, cc = ht % C;
+  const int gl = blockIdx.y;
+  const int x0 = (blockIdx.x * 2 + h) * C;
+  float2* tw = smem;
+  float2* bufs = smem + Cfg::TW_F2 + h * C * Half::STRIDE;
+  float2* Wp = p.W + (size_t)gl * p.nx * N;
+  const unsigned gstep = (unsigned)L * (unsigned)p.nx;
+  float2* colbuf = bufs + cc * Half::STRIDE;
+  float2* wbuf = bufs + (ht / L) * Half::STRIDE;
+  const int wt = ht % L;
+  float* dnbase = reinterpret_cast<float*>(smem + Cfg::DN_F2);
+  float* sky2 = dnbase + Cfg::KY_F;
+  // plan constants before the wait for the previous pass: twiddles and ky^2 to shared memory
+  for (int i = threadIdx.x; i < WarpFft<N, L>::TW; i += T) tw[i] = p.wtw[i];
+  for (int i = threadIdx.x; i < N; i += T) sky2[i] = __ldg(p.ky2 + i);
+  dep_wait();
+  dep_release();
+  const char* dn_stage = nullptr;
+  if (p.dn && p.dn_stage) {
+    const int lg = p.dn_dtype == BPM_DN_F16 ? 1 : 2;
+    const int es = 1 << lg;
+    char* dst = reinterpret_cast<char*>(dnbase + h * 16 * N);
+    const char* srcb = static_cast<const char*>(p.dn) + ((size_t)gl * p.dn_bstride + x0) * es;
+    const size_t rowb = (size_t)p.nx * es;
+    for (int ch = ht; ch < (N << lg); ch += TH)
+      cp_async16(dst + (size_t)ch * 16, srcb + (size_t)(ch >> lg) * rowb + (ch & (es - 1)) * 16);
+    cp_async_commit();
+    dn_stage = dst;
+  }
+  float2 v[E];
+  const unsigned gofs = (unsigned)r0 * (unsigned)p.nx + (unsigned)(x0 + cc);
+#pragma unroll
+  for (int i = 0; i < E; i++) v[i] = Wp[gofs + i * gstep];
+  __syncthreads();  // twiddles and ky^2 staged
+  // forward column FFT
+  colsplit_first<N, false, L>(v, colbuf, r0);
+  __syncthreads();
+  colsplit_middle<N, false, L>(wbuf, tw, wt);
+  __syncthreads();
+  colsplit_last<N, false, L>(v, colbuf, tw, r0);
+  // the tile's partial sums, each thread over its rows in order, then the half's tree
+  if (dn_stage) cp_async_wait<0>();
+  __syncthreads();  // the dn pieces other threads copied; every thread is past its last-stage reads
+  float sdn = 0.f, su = 0.f;
+  if (dn_stage && p.dn_dtype != BPM_DN_F16) {
+    const float* ds = reinterpret_cast<const float*>(dn_stage) + ht;
+#pragma unroll
+    for (int i = 0; i < E; i++) {
+      const float a = __fsqrt_rn(cabs2(v[i]));
+      su += a;
+      sdn = fmaf(a, ds[TH * i], sdn);
+    }
+  } else if (dn_stage) {
+    const __half* ds = reinterpret_cast<const __half*>(dn_stage) + ht;
+#pragma unroll
+    for (int i = 0; i < E; i++) {
+      const float a = __fsqrt_rn(cabs2(v[i]));
+      su += a;
+      sdn = fmaf(a, __half2float(ds[TH * i]), sdn);
+    }
+  } else {
+#pragma unroll
+    for (int i = 0; i < E; i++) {
+      const float a = __fsqrt_rn(cabs2(v[i]));
+      su += a;
+      if (p.dn) sdn = fmaf(a, load_dn_real(p.dn, p.dn_dtype, gl * p.dn_bstride + gofs + i * gstep), sdn);
+    }
+  }
+  // block_sum2<TH> of the half: warp trees, then the half's first thread over its warps in order
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) {
+    sdn += __shfl_xor_sync(0xffffffffu, sdn, o);
+    su += __shfl_xor_sync(0xffffffffu, su, o);
+  }
+  const int hw = ht >> 5;
+  if (t == 0) {
+    red[h][2 * hw] = sdn;
+    red[h][2 * hw + 1] = su;
+  }
+  __syncthreads();
+  if (ht == 0) {
+    float a = 0.f, b = 0.f;
+    for (int i = 0; i < TH / 32; i++) {
+      a += red[h][2 * i];
+      b += red[h][2 * i + 1];
+    }
+    part[h][0] = a;
+    part[h][1] = b;
+  }
+  cl.sync();  // every block's tile partials are visible across the cluster
+  if (warp == 0) {
+    // the field's partials in tile order (tile 2r + k in block rank r, half k), summed as
+    // col_split_kernel<N, 2> sums them
+    const int np = p.nx / 16;
+    float d0 = 0.f, u0 = 0.f, d1 = 0.f, u1 = 0.f;
+    if (t < np) {
+      const float* pr = cl.map_shared_rank(&part[0][0], t >> 1);
+      d0 = pr[2 * (t & 1)];
+      u0 = pr[2 * (t & 1) + 1];
+    }
+    if (t + 32 < np) {
+      const float* pr = cl.map_shared_rank(&part[0][0], (t + 32) >> 1);
+      d1 = pr[2 * (t & 1)];
+      u1 = pr[2 * (t & 1) + 1];
+    }
+    float dn_sum = 0.f, u_sum = 0.f;
+    for (int i = 0; i < np; i++) {
+      dn_sum += __shfl_sync(0xffffffffu, i < 32 ? d0 : d1, i & 31);
+      u_sum += __shfl_sync(0xffffffffu, i < 32 ? u0 : u1, i & 31);
+    }
+    if (t == 0) {
+      const float dn0 = dn_sum / u_sum;  // mult_dn_mean_buff, bpm_3d_kernels.cl:117
+      s_n = p.n00f + dn0;                // mult_propagator_buff, bpm_3d_kernels.cl:482
+      if (blockIdx.x == 0) p.dn0_field[gl] = dn0;
+    }
+  }
+  __syncthreads();  // s_n
+  float S = 0.f, G = 0.f;
+  propagate_rows<N, false, L>(p, v, x0 + cc, r0, s_n, __ldg(p.kx2 + x0 + cc), sky2, S, G);
+  // inverse column FFT, then the coalesced store
+  colsplit_first<N, true, L>(v, colbuf, r0);
+  __syncthreads();
+  colsplit_middle<N, true, L>(wbuf, tw, wt);
+  __syncthreads();
+  colsplit_last<N, true, L>(v, colbuf, tw, r0);
+#pragma unroll
+  for (int i = 0; i < E; i++) Wp[gofs + i * gstep] = v[i];
+  cl.sync();  // no block leaves while another may still read its partials
+}
+
+// ---------------------------------------------------------------------------------------
 // Whole-march cluster kernel for square grids N = 64, 128, 256: one thread-block cluster of
 // C = N/16 blocks per field (16 at 256, a non-portable cluster size) holds the field in
 // distributed shared memory for all nz steps. Block c owns rows [16c, 16c+16) (row slab R,
@@ -1578,6 +1757,57 @@ struct ColK {
   }
 };
 
+// The fused weighted column pass (col_fused_kernel<N>): a cluster of nx / 32 blocks per
+// field. state: -1 not checked yet, 0 this cluster size cannot be launched here, 1 ready
+template <int N>
+struct FusedK {
+  static int& state(int cl) {
+    static int st[17] = {-1, -1, -1, -1, -1, -1, -1, -1, -1, -1, -1, -1, -1, -1, -1, -1, -1};
+    return st[cl];
+  }
+  static cudaLaunchConfig_t config(dim3 g, int cl, cudaStream_t s, cudaLaunchAttribute* at, bool pdl) {
+    cudaLaunchConfig_t cfg = {};
+    cfg.gridDim = g;
+    cfg.blockDim = dim3(FusedCfg<N>::T);
+    cfg.dynamicSmemBytes = FusedCfg<N>::SMEM;
+    cfg.stream = s;
+    at[0].id = cudaLaunchAttributeClusterDimension;
+    at[0].val.clusterDim.x = cl;
+    at[0].val.clusterDim.y = 1;
+    at[0].val.clusterDim.z = 1;
+    at[1].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+    at[1].val.programmaticStreamSerializationAllowed = 1;
+    cfg.attrs = at;
+    cfg.numAttrs = pdl ? 2 : 1;
+    return cfg;
+  }
+  // the kernel fits and clusters of `cl` blocks can be co-scheduled on this device
+  static bool ready(int cl) {
+    int& st = state(cl);
+    if (st < 0) {
+      int ok = 0;
+      if (cl > 8) cudaFuncSetAttribute(col_fused_kernel<N>, cudaFuncAttributeNonPortableClusterSizeAllowed, 1);
+      if (cudaFuncSetAttribute(col_fused_kernel<N>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                               (int)FusedCfg<N>::SMEM) == cudaSuccess) {
+        cudaLaunchAttribute at[2];
+        cudaLaunchConfig_t cfg = config(dim3(cl, 1), cl, nullptr, at, false);
+        int clusters = 0;
+        if (cudaOccupancyMaxActiveClusters(&clusters, col_fused_kernel<N>, &cfg) == cudaSuccess) ok = clusters > 0;
+      }
+      cudaGetLastError();
+      st = ok;
+    }
+    return st == 1;
+  }
+  static int launch(dim3 g, int cl, cudaStream_t s, const ColParams& p) {
+    cudaLaunchAttribute at[2];
+    cudaLaunchConfig_t cfg = config(g, cl, s, at, true);
+    BPM_CUDA_TRY(cudaLaunchKernelEx(&cfg, col_fused_kernel<N>, p));
+    BPM_LAUNCH_CHECK("col_fused_kernel");
+    return BPM_OK;
+  }
+};
+
 int launch_row(int N, dim3 g, cudaStream_t s, const RowParams& p, bool adj = false) {
   switch (N) {
     case 16: return RowK<16>::launch(g, s, p, adj);
@@ -1683,6 +1913,7 @@ int check_request(const bpm_plan* pl, const bpm_request* r) {
     return BPM_ERR_ARG;
   }
   if (r->cluster < 0 || r->cluster > 2) { set_error("cluster must be 0, 1 or 2"); return BPM_ERR_ARG; }
+  if (r->col_fuse < 0 || r->col_fuse > 2) { set_error("col_fuse must be 0, 1 or 2"); return BPM_ERR_ARG; }
   if (r->ckpt && r->ckpt_every < 1) { set_error("ckpt_every must be >= 1 with ckpt"); return BPM_ERR_ARG; }
   if (r->mask && (r->dn_dtype == BPM_DN_NONE || r->dn_batch_stride != 0 || ((uintptr_t)r->mask & 7))) {
     set_error("mask needs one shared dn volume and 8-byte alignment");
@@ -1809,6 +2040,7 @@ MarchCtx make_ctx(const bpm_plan* pl, const bpm_request* r, void* ws, int b0, in
   }
 
   cp.col_block = r->col_block;
+  cp.col_fuse = r->col_fuse;
   c.grow = dim3(ny / 16, Gc);
   c.gcol = dim3(nx / 16, Gc);
   return c;
@@ -1825,10 +2057,37 @@ int launch_first_row(const bpm_plan* pl, const bpm_request* r, MarchCtx& c, int 
   return launch_row(pl->d.nx, c.grow, s, rp);
 }
 
-// the column pass(es) of step i (plane i -> plane i+1)
+// kNoFused when the fused column pass does not serve this request, else its launch status
+constexpr int kNoFused = 1;
+int try_fused_cols(const bpm_plan* pl, const MarchCtx& c, cudaStream_t s, bool force) {
+  const ColParams& p = c.cp;
+  const int nx = pl->d.nx, ny = pl->d.ny;
+  if (pl->d.mean_mode != BPM_MEAN_WEIGHTED || p.scat || (!force && p.col_fuse != 1) || nx % 32 || nx / 32 > 16)
+    return kNoFused;
+  const int cl = nx / 32;
+  const dim3 g(cl, c.gcol.y);
+  switch (ny) {
+    case 128: return FusedK<128>::ready(cl) ? FusedK<128>::launch(g, cl, s, p) : kNoFused;
+    case 256: return FusedK<256>::ready(cl) ? FusedK<256>::launch(g, cl, s, p) : kNoFused;
+    case 512: return FusedK<512>::ready(cl) ? FusedK<512>::launch(g, cl, s, p) : kNoFused;
+  }
+  return kNoFused;
+}
+
+// the column pass(es) of step i (plane i -> plane i+1): which = 0 the whole step (the fused
+// weighted pass where the request asks for it), 1 / 2 the weighted mode's first / second
+// pass, 3 the fused weighted pass
 int launch_cols(const bpm_plan* pl, MarchCtx& c, int i, int which, cudaStream_t s) {
   c.cp.z = i;
   if (pl->d.mean_mode == BPM_MEAN_WEIGHTED) {
+    if (which == 0 || which == 3) {
+      const int rc = try_fused_cols(pl, c, s, which == 3);
+      if (rc != kNoFused) return rc;
+      if (which == 3) {
+        set_error("the fused weighted column pass does not serve this grid or request");
+        return BPM_ERR_UNSUPPORTED;
+      }
+    }
     if (which != 2) {
       int rc = launch_col<1>(pl->d.ny, c.gcol, s, c.cp);
       if (rc || which == 1) return rc;
@@ -2428,11 +2687,15 @@ extern "C" int bpm_launch_pass(bpm_plan* pl, const bpm_request* r, void* ws, siz
       return launch_first_row(pl, r, c, 0, s);
     case BPM_PASS_COLUMN:
     case BPM_PASS_COLUMN_REDUCE:
-    case BPM_PASS_COLUMN_PROPAGATE: {
+    case BPM_PASS_COLUMN_PROPAGATE:
+    case BPM_PASS_COLUMN_FUSED: {
       if (z < 0 || z + 1 >= pl->d.nz) { set_error("column pass needs 0 <= z < nz-1"); return BPM_ERR_ARG; }
       const bool w = pl->d.mean_mode == BPM_MEAN_WEIGHTED;
       if (w == (pass == BPM_PASS_COLUMN)) { set_error("pass kind does not match the mean mode"); return BPM_ERR_ARG; }
-      return launch_cols(pl, c, z, pass == BPM_PASS_COLUMN ? 0 : (pass == BPM_PASS_COLUMN_REDUCE ? 1 : 2), s);
+      const int which = pass == BPM_PASS_COLUMN ? 0
+                        : pass == BPM_PASS_COLUMN_REDUCE ? 1
+                        : pass == BPM_PASS_COLUMN_PROPAGATE ? 2 : 3;
+      return launch_cols(pl, c, z, which, s);
     }
     case BPM_PASS_ROW:
       if (z < 1 || z >= pl->d.nz) { set_error("row pass needs 1 <= z < nz"); return BPM_ERR_ARG; }

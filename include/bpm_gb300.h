@@ -111,6 +111,11 @@ typedef struct {
   int cluster;                   /* whole-march cluster kernel (square 64..256 grids without
                                     scattering sums or checkpoints): 1 = use it, 2 = row/column
                                     pass kernels (default: cluster at 64 and 128)               */
+  int col_fuse;                  /* weighted mode: 1 = one column pass per step (forward FFT,
+                                    plane-wide sums across a thread-block cluster of the field's
+                                    blocks, propagator, inverse FFT) where ny <= 512, nx <= 512
+                                    and no scattering sums; 0 or 2 = the two column passes (the
+                                    default; same bits either way)                               */
 } bpm_request;
 
 /* Library version (BPM_GB300_VERSION). */
@@ -209,7 +214,8 @@ typedef enum {
   BPM_PASS_COLUMN = 1,            /* column FFT, propagator, inverse column FFT (ignore/simple) */
   BPM_PASS_COLUMN_REDUCE = 2,     /* weighted: forward column FFT + |u_hat| partial sums      */
   BPM_PASS_COLUMN_PROPAGATE = 3,  /* weighted: propagator + inverse column FFT                */
-  BPM_PASS_ROW = 4                /* inverse row FFT, mask, plane z output, forward row FFT   */
+  BPM_PASS_ROW = 4,               /* inverse row FFT, mask, plane z output, forward row FFT   */
+  BPM_PASS_COLUMN_FUSED = 5       /* weighted: both column passes in one launch (col_fuse)    */
 } bpm_pass_kind;
 
 /* Launch exactly one pass of the march for the first group of fields of the request, for

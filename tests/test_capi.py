@@ -166,7 +166,7 @@ def test_autotune_shape_choices():
     assert pick_option(0, 10., {1: 9.8, 2: 9.9}) == (0, 10.)          # within 3 %: keep
     assert pick_option(0, 10., {1: 9.0, 8: 9.5}) == (1, 9.0)
     c = shape_candidates((512, 512), 64, 8, "weighted")
-    assert c == {"conc": [1, 2, 4, 8]}                                 # weighted passes keep 16 columns
+    assert c == {"conc": [1, 2, 4, 8], "col_fuse": [1, 2]}             # weighted passes keep 16 columns
     c = shape_candidates((256, 256), 4, 4, "ignore")
     assert c == {"col_block": [8, 16], "cluster": [1, 2]}              # one group: no concurrency choice
     assert "cluster" not in shape_candidates((512, 256), 8, 2, "ignore")

@@ -1,5 +1,6 @@
 """Launch shapes of the march (fields per launch, concurrent groups, column-block width,
-cluster kernel or pass kernels; bpm_request in include/bpm_gb300.h) never change a result:
+cluster kernel or pass kernels, one fused or two weighted column passes; bpm_request in
+include/bpm_gb300.h) never change a result:
 every candidate the autotuner may pick gives the same bits as the library's default shape
 (the cluster kernel at 64x64, whose FFT has another radix order, to FP32 rounding), and the
 tuner's choice is valid, cached and applied by BatchedMarch(group="auto")."""
@@ -44,8 +45,8 @@ def test_every_launch_shape_gives_the_same_result(bpm, size, batch, mode, cplx):
     kw = dict(lam=.5, n0=1.33, dn=dn, mean_mode=mode, absorbing_width=3, return_field=True)
     ref = bpm.bpm_3d_batched(size, (.1, .1, .1), u0=u0, **kw)
     n = 0
-    for group, conc, col_block, cluster in itertools.product((1, 3, 0), (1, 2, 8), (8, 16), (1, 2)):
-        launch = {"group": group, "conc": conc, "col_block": col_block, "cluster": cluster}
+    for group, conc, col_block, cluster, fuse in itertools.product((1, 3, 0), (1, 2, 8), (8, 16), (1, 2), (1, 2)):
+        launch = {"group": group, "conc": conc, "col_block": col_block, "cluster": cluster, "col_fuse": fuse}
         got = bpm.bpm_3d_batched(size, (.1, .1, .1), u0=u0, launch=launch, **kw)
         if size[0] == 64 and cluster == 2:
             # the default at 64x64 is the cluster kernel (warp FFT); the pass kernels run the
@@ -54,7 +55,7 @@ def test_every_launch_shape_gives_the_same_result(bpm, size, batch, mode, cplx):
         else:
             assert np.array_equal(got, ref), launch
         n += 1
-    assert n == 36
+    assert n == 72
 
 
 def test_tuned_shape_is_applied(bpm, tmp_path, monkeypatch):
@@ -66,9 +67,9 @@ def test_tuned_shape_is_applied(bpm, tmp_path, monkeypatch):
     u0, dn = inputs(size, batch, 5)
     dn_t = torch.from_numpy(dn).cuda()
     shape = autotune.tune_shape(size, (.1, .1, .1), .5, 1.33, batch, dn_t, "weighted", "intensity")
-    assert set(shape) == {"group", "conc", "col_block", "cluster"}
+    assert set(shape) == {"group", "conc", "col_block", "cluster", "col_fuse"}
     assert 1 <= shape["group"] <= batch and shape["conc"] in (0, 1, 2, 4, 8)
-    assert shape["col_block"] in (0, 8, 16) and shape["cluster"] in (0, 1, 2)
+    assert shape["col_block"] in (0, 8, 16) and shape["cluster"] in (0, 1, 2) and shape["col_fuse"] in (0, 1, 2)
     assert (tmp_path / "tune.json").exists()
     assert autotune.tune_shape(size, (.1, .1, .1), .5, 1.33, batch, dn_t, "weighted", "intensity") == shape
     m = bpm.BatchedMarch(size, (.1, .1, .1), .5, 1.33, batch, dn=dn_t, group="auto")
