@@ -337,7 +337,10 @@ def bench_ours(args, rank, world, local_rank):
                        "per_launch_group_fields": grp, "sum_over_step_ms": t_step_sum},
         "roofline": {"bound": "hbm", "kernel": "row_shared_kernel<512, 1>", "achieved": row_gbs,
                      "peak": hbm_peak, "unit": "GB/s", "frac": row_gbs / hbm_peak,
-                     "traffic": traffic, "peak_kind": peak_kind + " (MEASURED_PEAKS.json hbm_gbs)",
+                     "traffic": traffic, "traffic_cold": profile_traffic(grp, "dram_bytes_per_launch_cold"),
+                     "traffic_note": "ncu DRAM bytes per launch: warm cache (L2 kept, as in the march) and with "
+                                     "L2 flushed before the launch",
+                     "peak_kind": peak_kind + " (MEASURED_PEAKS.json hbm_gbs)",
                      "algorithmic_bytes_per_launch": row_bytes,
                      "fp32": {"row_pass_tflops": row_flops / (t_row * 1e-3) / 1e12,
                               "col_pass_tflops": col_flops / ((t_cr + t_cp) * 1e-3) / 1e12,
@@ -686,16 +689,18 @@ def profile_run(args):
 
 
 
-def profile_traffic(fields):
+def profile_traffic(fields, key="dram_bytes_per_launch"):
     """DRAM bytes of one row-pass launch over `fields` fields: the committed ncu capture's
     per-field figure (dram__bytes_read.sum + dram__bytes_write.sum, captured on a smaller
-    batch of the same 512x512 kernel) scaled by the fields the bench's launch processes."""
+    batch of the same 512x512 kernel; `key` dram_bytes_per_launch: warm cache, as in the
+    timed march; dram_bytes_per_launch_cold: L2 flushed before the launch) scaled by the
+    fields the bench's launch processes."""
     p = os.path.join(ROOT, "profiles", "row_pass_512_traffic.json")
     if os.path.exists(p):
         try:
             d = json.load(open(p))
-            return float(d["dram_bytes_per_launch"]) / float(d["fields_per_launch"]) * fields
-        except (KeyError, ValueError, ZeroDivisionError):
+            return float(d[key]) / float(d["fields_per_launch"]) * fields
+        except (KeyError, ValueError, ZeroDivisionError, TypeError):
             return None
     return None
 

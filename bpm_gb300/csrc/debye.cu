@@ -602,41 +602,48 @@ __host__ __device__ constexpr uint32_t tc_a_bytes() { return TC_BM * TC_BK * 4; 
 __host__ __device__ constexpr uint32_t tc_b_bytes(int BN) { return (uint32_t)BN * TC_BK * 4; }
 __host__ __device__ constexpr uint32_t tc_stage_bytes(int BN) { return 2 * tc_a_bytes() + 2 * tc_b_bytes(BN); }
 __host__ __device__ constexpr size_t tc_smem_bytes(int BN, int S) {
-  return 1024 + (size_t)S * tc_stage_bytes(BN) + (2 * S + 1) * 8 + 16;
+  return 1024 + (size_t)S * tc_stage_bytes(BN) + (3 * S + 1) * 8 + 16;
 }
 
-// One 128-row x BN-column tile of the product per block of 4 warps. Thread 0 issues the TMA
-// loads (A, Bh, Bl of a 32-node slice per stage, S stages in flight) and the MMAs; every
-// thread splits the stage's A tile into its TF32 high part (in place) and the remainder
-// (next to it) before the MMAs of that stage are issued; a stage is refilled once the
-// MMAs that read it have completed (tcgen05.commit on its mbarrier). The accumulator is
-// one 128-lane x BN-column region of tensor memory; the 4 warps read their 32 lanes back
-// and store I. The products go to separate accumulators so that each adds fewer terms
-// (the tensor core rounds its FP32 sums with a bias that grows with the number of
-// accumulations): Ah Bh of even and of odd node slices to two accumulators and the small
-// cross terms to a third (with room for two only, Ah Bh to one and the cross terms to the
-// other); the epilogue adds them in FP32. Every wait is bounded in time: on expiry the
-// block records g_tc_status,
-// waits (bounded) for its own copies and products in flight, frees its tensor memory
-// and returns.
+// One 128-row x BN-column tile of the product per block of 4 warps, a three-role pipeline
+// over S shared-memory stages of one 32-node slice each (A, its TF32 remainder, Bh, Bl):
+//   warp 0 lane 0  loads: once the products of slice kt - S have released stage kt % S
+//                  (tcgen05.commit on empty[s]), TMA loads of A, Bh, Bl complete on full[s];
+//   warps 2 and 3  split: once full[s] has landed, A = Ah + Al, Ah (exact TF32) in place and
+//                  Al beside it, then an arrival on split[s] (64 arrivals);
+//   warp 1 lane 0  products: once split[s] is complete, the 3xTF32 MMAs of the slice, then
+//                  tcgen05.commit on empty[s].
+// So loads run up to S slices ahead and a slice's split overlaps the previous slice's
+// products. The products go to separate accumulators so that each adds fewer terms (the
+// tensor core rounds its FP32 sums with a bias that grows with the number of accumulations):
+// Ah Bh of even and of odd node slices to two accumulators and the small cross terms to a
+// third (with room for two only, Ah Bh to one and the cross terms to the other); the
+// epilogue (all 4 warps, 32 tensor-memory lanes each) adds them in FP32 and stores I. Every
+// wait is bounded in time: a role that gives up raises the block's abort flag, the others
+// stop at their next wait, the block records g_tc_status, waits (bounded) for its own loads
+// and products in flight, frees its tensor memory and returns.
 __global__ void __launch_bounds__(TC_THREADS, 1)
 debye_accum_tc_kernel(const __grid_constant__ CUtensorMap mapA, const __grid_constant__ CUtensorMap mapBh,
                       const __grid_constant__ CUtensorMap mapBl, TcArgs a) {
   extern __shared__ uint8_t tc_smem_raw[];
   uint8_t* sm = reinterpret_cast<uint8_t*>((reinterpret_cast<uintptr_t>(tc_smem_raw) + 1023) & ~uintptr_t(1023));
+  __shared__ int abort_flag;
   const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
   const int S = a.stages;
   const uint32_t AB = tc_a_bytes(), BB = tc_b_bytes(a.BN), SB = tc_stage_bytes(a.BN);
   uint64_t* full = reinterpret_cast<uint64_t*>(sm + (size_t)S * SB);
-  uint64_t* empty = full + S;
+  uint64_t* split = full + S;
+  uint64_t* empty = split + S;
   uint64_t* done = empty + S;
   uint32_t* tmem_slot = reinterpret_cast<uint32_t*>(done + 1);
   const int m0 = blockIdx.y * TC_BM, n0 = blockIdx.x * a.BN;
   const int KT = (a.T + TC_BK - 1) / TC_BK;
+  constexpr int SPLITTERS = 64;  // warps 2 and 3
 
   if (tid == 0) {
     for (int i = 0; i < S; i++) {
       tc::mbar_init(&full[i], 1);
+      tc::mbar_init(&split[i], SPLITTERS);
       tc::mbar_init(&empty[i], 1);
     }
     tc::mbar_init(done, 1);
@@ -644,6 +651,7 @@ debye_accum_tc_kernel(const __grid_constant__ CUtensorMap mapA, const __grid_con
     tc::tma_prefetch_map(&mapA);
     tc::tma_prefetch_map(&mapBh);
     tc::tma_prefetch_map(&mapBl);
+    abort_flag = 0;
   }
   if (warp == 0) {
     tc::tmem_alloc(tmem_slot, a.tmem_cols);
@@ -653,72 +661,77 @@ debye_accum_tc_kernel(const __grid_constant__ CUtensorMap mapA, const __grid_con
   __syncthreads();
   tc::fence_after_sync();
   const uint32_t tmem = *tmem_slot;
+  volatile int* abortv = &abort_flag;
+  int issued = 0;  // slices whose loads were issued (warp 0 lane 0)
 
-  auto issue = [&](int st, int kt) {
-    uint8_t* base = sm + (size_t)st * SB;
-    tc::mbar_expect_tx(&full[st], AB + 2 * BB);
-    tc::tma_load_2d(base, &mapA, &full[st], kt * TC_BK, m0);
-    tc::tma_load_2d(base + 2 * AB, &mapBh, &full[st], kt * TC_BK, n0);
-    tc::tma_load_2d(base + 2 * AB + BB, &mapBl, &full[st], kt * TC_BK, n0);
-  };
-  int issued = 0;  // slices whose loads thread 0 has issued
-  if (tid == 0)
-    for (; issued < S && issued < KT; issued++) issue(issued, issued);
-
-  const uint32_t idesc = tc::idesc_tf32(TC_BM, a.BN);
-  bool ok = true;
-  int consumed = 0;  // slices whose products were issued
-  for (int kt = 0; kt < KT; kt++) {
-    const int st = kt % S;
-    const bool landed = tc::mbar_wait(&full[st], (uint32_t)(kt / S) & 1u, TC_WAIT_NS);
-    if (!__syncthreads_and(landed && ok)) {
-      ok = false;
-      break;
+  if (warp == 0 && lane == 0) {
+    // ---- loads ----
+    for (int kt = 0; kt < KT && !*abortv; kt++) {
+      const int st = kt % S;
+      if (kt >= S && !tc::mbar_wait(&empty[st], (uint32_t)(kt / S - 1) & 1u, TC_WAIT_NS)) {
+        *abortv = 1;
+        break;
+      }
+      uint8_t* base = sm + (size_t)st * SB;
+      tc::mbar_expect_tx(&full[st], AB + 2 * BB);
+      tc::tma_load_2d(base, &mapA, &full[st], kt * TC_BK, m0);
+      tc::tma_load_2d(base + 2 * AB, &mapBh, &full[st], kt * TC_BK, n0);
+      tc::tma_load_2d(base + 2 * AB + BB, &mapBl, &full[st], kt * TC_BK, n0);
+      issued = kt + 1;
     }
-    // A = Ah + Al: Ah (exact TF32) in place, Al in the next 16 KB
-    uint8_t* base = sm + (size_t)st * SB;
-    float4* pa = reinterpret_cast<float4*>(base);
-    float4* pl = reinterpret_cast<float4*>(base + AB);
+  } else if (warp >= 2) {
+    // ---- TF32 split of A ----
+    const int sp = tid - 64;
+    for (int kt = 0; kt < KT; kt++) {
+      const int st = kt % S;
+      if (*abortv) break;
+      if (!tc::mbar_wait(&full[st], (uint32_t)(kt / S) & 1u, TC_WAIT_NS)) {
+        *abortv = 1;
+        break;
+      }
+      uint8_t* base = sm + (size_t)st * SB;
+      float4* pa = reinterpret_cast<float4*>(base);
+      float4* pl = reinterpret_cast<float4*>(base + AB);
 #pragma unroll 4
-    for (int i = tid; i < (int)(AB / 16); i += TC_THREADS) {
-      const float4 v = pa[i];
-      const float4 h = make_float4(tf32_hi(v.x), tf32_hi(v.y), tf32_hi(v.z), tf32_hi(v.w));
-      pl[i] = make_float4(v.x - h.x, v.y - h.y, v.z - h.z, v.w - h.w);
-      pa[i] = h;
+      for (int i = sp; i < (int)(AB / 16); i += SPLITTERS) {
+        const float4 v = pa[i];
+        const float4 h = make_float4(tf32_hi(v.x), tf32_hi(v.y), tf32_hi(v.z), tf32_hi(v.w));
+        pl[i] = make_float4(v.x - h.x, v.y - h.y, v.z - h.z, v.w - h.w);
+        pa[i] = h;
+      }
+      tc::fence_proxy_async();  // the split operands are visible to the tensor cores
+      tc::mbar_arrive(&split[st]);
     }
-    tc::fence_proxy_async();
-    __syncthreads();
-    if (tid == 0) {
+  } else if (warp == 1 && lane == 0) {
+    // ---- products ----
+    const uint32_t idesc = tc::idesc_tf32(TC_BM, a.BN);
+    for (int kt = 0; kt < KT; kt++) {
+      const int st = kt % S;
+      if (*abortv) break;
+      if (!tc::mbar_wait(&split[st], (uint32_t)(kt / S) & 1u, TC_WAIT_NS)) {
+        *abortv = 1;
+        break;
+      }
       tc::fence_after_sync();
-      const uint32_t sa = tc::smem_u32(base), sl = sa + AB, sbh = sa + 2 * AB, sbl = sbh + BB;
+      const uint32_t sa = tc::smem_u32(sm + (size_t)st * SB), sl = sa + AB, sbh = sa + 2 * AB, sbl = sbh + BB;
+      const uint32_t big = a.nacc == 3 ? tmem + (uint32_t)((kt & 1) * a.acc_stride) : tmem;
+      const uint32_t cross = tmem + (uint32_t)((a.nacc - 1) * a.acc_stride);
 #pragma unroll
       for (int k = 0; k < TC_BK / 8; k++) {  // 8 TF32 (32 bytes) of K per instruction
         const uint64_t dah = tc::desc_sw128_kmajor(sa + 32 * k), dal = tc::desc_sw128_kmajor(sl + 32 * k);
         const uint64_t dbh = tc::desc_sw128_kmajor(sbh + 32 * k), dbl = tc::desc_sw128_kmajor(sbl + 32 * k);
-        // accumulators: big (Ah Bh) and cross (Ah Bl + Al Bh)
-        const uint32_t big = a.nacc == 3 ? tmem + (uint32_t)((kt & 1) * a.acc_stride) : tmem;
-        const uint32_t cross = tmem + (uint32_t)((a.nacc - 1) * a.acc_stride);
-        const uint32_t first_big = a.nacc == 3 ? (kt < 2 && k == 0) : (kt == 0 && k == 0);
+        const bool first_big = a.nacc == 3 ? (kt < 2 && k == 0) : (kt == 0 && k == 0);
         tc::mma_tf32(big, dah, dbh, idesc, first_big ? 0u : 1u);
         tc::mma_tf32(cross, dah, dbl, idesc, (kt > 0 || k > 0) ? 1u : 0u);
         tc::mma_tf32(cross, dal, dbh, idesc, 1u);
       }
       tc::mma_commit(&empty[st]);
-      // refill the stage of the previous slice once its products have read it
-      if (kt >= 1 && issued < KT) {
-        const int sp = (kt - 1) % S;
-        if (tc::mbar_wait(&empty[sp], (uint32_t)((kt - 1) / S) & 1u, TC_WAIT_NS)) {
-          issue(sp, issued);
-          issued++;
-        } else {
-          ok = false;
-        }
-      }
     }
-    consumed = kt + 1;
+    tc::mma_commit(done);  // arrives once every product issued has completed
   }
-  ok = __syncthreads_and(ok);
-  if (tid == 0) tc::mma_commit(done);  // arrives once every product issued so far has completed
+  // every role has left its loop
+  __syncthreads();
+  bool ok = !*abortv;
   const bool fin = tc::mbar_wait(done, 0, TC_WAIT_NS);
   ok = __syncthreads_and(ok && fin);
   tc::fence_after_sync();
@@ -759,9 +772,10 @@ debye_accum_tc_kernel(const __grid_constant__ CUtensorMap mapA, const __grid_con
     }
   } else if (tid == 0) {
     atomicExch(&g_tc_status, 1);
-    // loads issued but never consumed still land in this block's shared memory: wait
-    // for them (bounded) before the block exits
-    for (int kt = consumed; kt < issued; kt++) tc::mbar_wait(&full[kt % S], (uint32_t)(kt / S) & 1u, TC_WAIT_NS);
+    // loads issued but never consumed still land in this block's shared memory: wait for
+    // each stage's latest issued load (bounded) before the block exits
+    for (int kt = issued > S ? issued - S : 0; kt < issued; kt++)
+      tc::mbar_wait(&full[kt % S], (uint32_t)(kt / S) & 1u, TC_WAIT_NS);
   }
   tc::fence_before_sync();
   __syncthreads();
