@@ -88,6 +88,7 @@ SIGNATURES = {
                                  c_double, c_double, c_double, c_double, c_vp, c_vp]),
     "bpm_host_ptr_mapped": (c_int, [c_vp]),
     "bpm_device_status": (c_int, [c_int]),
+    "debye_tc_timeout_selftest": (c_int, [c_double]),
     "debye_workspace_bytes": (c_size, [ctypes.POINTER(DebyeDesc)]),
     "debye_focus_field": (c_int, [ctypes.POINTER(DebyeDesc), c_vp, c_vp, c_vp, c_vp, c_vp, c_size, c_vp]),
     "debye_gauss_workspace_bytes": (c_size, [ctypes.POINTER(DebyeDesc)]),

@@ -584,6 +584,12 @@ __global__ void debye_phase_tc_kernel(int T, int Tp, int Zo, float z1, float z2,
 constexpr int TC_BM = 128, TC_BK = 32, TC_THREADS = 128;
 constexpr uint64_t TC_WAIT_NS = 2000000000ull;  // a wait gives up after 2 s
 
+// the dynamic shared-memory limit of debye_accum_tc_kernel, raised once to the opt-in
+// maximum (less the kernel's static shared memory) so every tile shape and the wait
+// self-test launch under it; tiles are sized to stay below TC_SMEM_MAX
+constexpr size_t TC_SMEM_MAX = 227 * 1024 - 256;
+cudaError_t tc_prepare();
+
 struct TcArgs {
   int T;           // quadrature nodes (the K extent)
   int rows;        // 3 Mr
@@ -596,6 +602,8 @@ struct TcArgs {
   int acc_stride;
   int nxo, M, sym; // octant columns per row, octant columns, radius rows deduplicated
   float2* I;       // (3, Zo, M): row r of the product goes to its octant column(s)
+  unsigned long long wait_ns;  // limit of every mbarrier wait
+  unsigned extra_tx;           // 0; debye_tc_timeout_selftest announces bytes that never arrive
 };
 
 __host__ __device__ constexpr uint32_t tc_a_bytes() { return TC_BM * TC_BK * 4; }
@@ -668,12 +676,12 @@ debye_accum_tc_kernel(const __grid_constant__ CUtensorMap mapA, const __grid_con
     // ---- loads ----
     for (int kt = 0; kt < KT && !*abortv; kt++) {
       const int st = kt % S;
-      if (kt >= S && !tc::mbar_wait(&empty[st], (uint32_t)(kt / S - 1) & 1u, TC_WAIT_NS)) {
+      if (kt >= S && !tc::mbar_wait(&empty[st], (uint32_t)(kt / S - 1) & 1u, a.wait_ns)) {
         *abortv = 1;
         break;
       }
       uint8_t* base = sm + (size_t)st * SB;
-      tc::mbar_expect_tx(&full[st], AB + 2 * BB);
+      tc::mbar_expect_tx(&full[st], AB + 2 * BB + a.extra_tx);
       tc::tma_load_2d(base, &mapA, &full[st], kt * TC_BK, m0);
       tc::tma_load_2d(base + 2 * AB, &mapBh, &full[st], kt * TC_BK, n0);
       tc::tma_load_2d(base + 2 * AB + BB, &mapBl, &full[st], kt * TC_BK, n0);
@@ -685,7 +693,7 @@ debye_accum_tc_kernel(const __grid_constant__ CUtensorMap mapA, const __grid_con
     for (int kt = 0; kt < KT; kt++) {
       const int st = kt % S;
       if (*abortv) break;
-      if (!tc::mbar_wait(&full[st], (uint32_t)(kt / S) & 1u, TC_WAIT_NS)) {
+      if (!tc::mbar_wait(&full[st], (uint32_t)(kt / S) & 1u, a.wait_ns)) {
         *abortv = 1;
         break;
       }
@@ -708,7 +716,7 @@ debye_accum_tc_kernel(const __grid_constant__ CUtensorMap mapA, const __grid_con
     for (int kt = 0; kt < KT; kt++) {
       const int st = kt % S;
       if (*abortv) break;
-      if (!tc::mbar_wait(&split[st], (uint32_t)(kt / S) & 1u, TC_WAIT_NS)) {
+      if (!tc::mbar_wait(&split[st], (uint32_t)(kt / S) & 1u, a.wait_ns)) {
         *abortv = 1;
         break;
       }
@@ -732,7 +740,7 @@ debye_accum_tc_kernel(const __grid_constant__ CUtensorMap mapA, const __grid_con
   // every role has left its loop
   __syncthreads();
   bool ok = !*abortv;
-  const bool fin = tc::mbar_wait(done, 0, TC_WAIT_NS);
+  const bool fin = tc::mbar_wait(done, 0, a.wait_ns);
   ok = __syncthreads_and(ok && fin);
   tc::fence_after_sync();
   if (ok) {
@@ -775,11 +783,27 @@ debye_accum_tc_kernel(const __grid_constant__ CUtensorMap mapA, const __grid_con
     // loads issued but never consumed still land in this block's shared memory: wait for
     // each stage's latest issued load (bounded) before the block exits
     for (int kt = issued > S ? issued - S : 0; kt < issued; kt++)
-      tc::mbar_wait(&full[kt % S], (uint32_t)(kt / S) & 1u, TC_WAIT_NS);
+      tc::mbar_wait(&full[kt % S], (uint32_t)(kt / S) & 1u, a.wait_ns);
   }
   tc::fence_before_sync();
   __syncthreads();
   if (warp == 0) tc::tmem_dealloc(tmem, a.tmem_cols);
+}
+
+cudaError_t tc_prepare() {
+  // the opt-in limit covers static and dynamic shared memory together
+  static const cudaError_t e = [] {
+    int dev = 0, optin = 0;
+    cudaFuncAttributes fa;
+    cudaError_t r;
+    if ((r = cudaGetDevice(&dev)) || (r = cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev)) ||
+        (r = cudaFuncGetAttributes(&fa, debye_accum_tc_kernel)))
+      return r;
+    const size_t room = (size_t)optin - fa.sharedSizeBytes;
+    return cudaFuncSetAttribute(debye_accum_tc_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                (int)std::min(room, TC_SMEM_MAX));
+  }();
+  return e;
 }
 
 enum Variant { V_STD = 0, V_GAUSS = 1, V_PLANE = 2, V_AT = 3 };
@@ -930,7 +954,7 @@ TcLayout tc_layout(const debye_desc* d, bool gauss) {
   const int cols = 2 * L.Zo;
   L.ntn = (cols + 255) / 256;
   L.BN = ((cols + L.ntn - 1) / L.ntn + 15) & ~15;
-  L.stages = tc_smem_bytes(L.BN, 3) <= 227 * 1024 ? 3 : 2;
+  L.stages = tc_smem_bytes(L.BN, 3) <= TC_SMEM_MAX ? 3 : 2;
   size_t off = 0;
   L.si = off; off += align256(sizeof(double) * L.T);
   L.ct = off; off += align256(sizeof(double) * L.T);
@@ -1009,12 +1033,11 @@ int run_octant_tc(const debye_desc* d, bool gauss, double sig, float* u, void* e
   ta.M = L.M;
   ta.sym = L.sym ? 1 : 0;
   ta.I = I;
+  ta.wait_ns = TC_WAIT_NS;
+  ta.extra_tx = 0;
   const size_t smem = tc_smem_bytes(L.BN, L.stages);
-  static size_t smem_set = 0;
-  if (smem > smem_set) {
-    BPM_CUDA_TRY(cudaFuncSetAttribute(debye_accum_tc_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-    smem_set = smem;
-  }
+  if (smem > TC_SMEM_MAX) { set_error("quadrature tile does not fit shared memory"); return BPM_ERR_SHAPE; }
+  BPM_CUDA_TRY(tc_prepare());
   const dim3 grid(L.ntn, (rows + TC_BM - 1) / TC_BM);
   debye_accum_tc_kernel<<<grid, TC_THREADS, smem, s>>>(mA, mBh, mBl, ta);
   BPM_LAUNCH_CHECK("debye_accum_tc_kernel");
@@ -1228,4 +1251,72 @@ extern "C" int bpm_device_status(int clear) {
     BPM_CUDA_TRY(cudaMemcpyToSymbol(g_tc_status, &zero, sizeof(int)));
   }
   return v;
+}
+
+// Self-test of the bounded waits of debye_accum_tc_kernel: one block on a small product whose
+// loads announce 16 bytes more than they deliver, so the slice never completes; every wait
+// gives up after wait_ms, the block records g_tc_status and leaves with its tensor memory
+// freed. Returns BPM_ERR_TIMEOUT when that happened (and clears the status), BPM_OK if the
+// product completed, a negative status on a CUDA error. Allocates and frees its own small
+// buffers; synchronises the device.
+extern "C" int debye_tc_timeout_selftest(double wait_ms) {
+  clear_error();
+  if (!(wait_ms > 0) || wait_ms > 1000.) { set_error("wait_ms must be in (0, 1000]"); return BPM_ERR_ARG; }
+  const int T = 64, Tp = 64, rows = 128, cols = 16;
+  float *A = nullptr, *Bh = nullptr, *Bl = nullptr;
+  float2* I = nullptr;
+  auto release = [&]() {
+    cudaFree(A);
+    cudaFree(Bh);
+    cudaFree(Bl);
+    cudaFree(I);
+  };
+  cudaError_t e;
+  if ((e = cudaMalloc(&A, sizeof(float) * rows * Tp)) || (e = cudaMalloc(&Bh, sizeof(float) * cols * Tp)) ||
+      (e = cudaMalloc(&Bl, sizeof(float) * cols * Tp)) || (e = cudaMalloc(&I, sizeof(float2) * rows * cols))) {
+    release();
+    return cuda_fail(e, "cudaMalloc");
+  }
+  cudaMemset(A, 0, sizeof(float) * rows * Tp);
+  cudaMemset(Bh, 0, sizeof(float) * cols * Tp);
+  cudaMemset(Bl, 0, sizeof(float) * cols * Tp);
+  CUtensorMap mA, mBh, mBl;
+  if (tc::encode_f32_kmajor(&mA, A, rows, T, Tp, TC_BM) || tc::encode_f32_kmajor(&mBh, Bh, cols, T, Tp, cols) ||
+      tc::encode_f32_kmajor(&mBl, Bl, cols, T, Tp, cols)) {
+    release();
+    set_error("cuTensorMapEncodeTiled failed");
+    return BPM_ERR_CUDA;
+  }
+  TcArgs ta;
+  memset(&ta, 0, sizeof(ta));
+  ta.T = T;
+  ta.rows = rows;
+  ta.Mr = rows / 3 + 1;
+  ta.Zo = cols / 2;
+  ta.BN = cols;
+  ta.stages = 2;
+  ta.acc_stride = 32;
+  ta.nacc = 3;
+  ta.tmem_cols = 128;
+  ta.nxo = rows;
+  ta.M = rows;
+  ta.sym = 0;
+  ta.I = I;
+  ta.wait_ns = (unsigned long long)(wait_ms * 1e6);
+  ta.extra_tx = 16;
+  const size_t smem = tc_smem_bytes(ta.BN, ta.stages);
+  if ((e = tc_prepare())) {
+    release();
+    return cuda_fail(e, "cudaFuncSetAttribute");
+  }
+  debye_accum_tc_kernel<<<dim3(1, 1), TC_THREADS, smem>>>(mA, mBh, mBl, ta);
+  if ((e = cudaGetLastError()) || (e = cudaDeviceSynchronize())) {
+    release();
+    return cuda_fail(e, "debye_accum_tc_kernel (wait self-test)");
+  }
+  count_launch();
+  release();
+  int st = bpm_device_status(1);
+  if (st < 0) return st;
+  return st ? BPM_ERR_TIMEOUT : BPM_OK;
 }

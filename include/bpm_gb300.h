@@ -308,6 +308,14 @@ size_t debye_workspace_bytes(const debye_desc* desc);
  * No counterpart in the reference (its OpenCL kernels have no such waits). */
 int bpm_device_status(int clear);
 
+/* Self-test of those bounded waits: runs the tensor-core quadrature kernel once on a small
+ * product whose loads announce more bytes than they deliver, so its waits give up after
+ * wait_ms (0 < wait_ms <= 1000) and it leaves with the status set and its tensor memory
+ * freed. Returns BPM_ERR_TIMEOUT when the waits gave up (the status is cleared again),
+ * BPM_OK if the product completed, another negative status on a CUDA error. Allocates its
+ * own small buffers and synchronises the device. No counterpart in the reference. */
+int debye_tc_timeout_selftest(double wait_ms);
+
 /* Compute the focus field on the full (nz, ny, nx) grid centred at index n/2.
  * Replaces bpm/psf/_focus_fields_debye.py:focus_field_debye (:48-146): the debye_wolf
  * octant launch (:102-109, kernel bpm/psf/kernels/psf_debye.cl:24-113) and the host-side

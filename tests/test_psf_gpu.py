@@ -239,3 +239,21 @@ def test_physical_quadrature_against_the_debye_integral(bpm, n_int):
     assert rel_l2(ref, u) > 1e-2          # the reference rule (no sin t) is another PSF
     with pytest.raises(ValueError):
         bpm.psf(shape, (dx,) * 3, lam, NA, 1., n_int, quadrature="midpoint")
+
+
+def test_tensor_core_wait_runs_out_and_reports(bpm):
+    """A bounded wait of the tensor-core quadrature that cannot be met (its loads announce 16
+    bytes that never arrive, debye_tc_timeout_selftest) gives up after 20 ms and reports
+    BPM_ERR_TIMEOUT through the device status; the context stays usable: a PSF afterwards
+    is correct and leaves the status clear."""
+    import time
+    from bpm_gb300 import _native as N
+    t0 = time.perf_counter()
+    assert N.lib().debye_tc_timeout_selftest(20.) == N.BPM_ERR_TIMEOUT
+    assert time.perf_counter() - t0 < 30
+    assert N.lib().bpm_device_status(0) == 0
+    shape = (32, 32, 32)
+    u = bpm.psf(shape, (.1, .1, .1), .5, 1.1, 1.33, 100)
+    o = debye_ref.psf(shape, (.1, .1, .1), .5, 1.1, 1.33, 100)
+    assert rel_l2(u, o) < TOL
+    assert N.lib().bpm_device_status(0) == 0
