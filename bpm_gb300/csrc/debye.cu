@@ -30,6 +30,7 @@
 #include <cstdlib>
 #include <cstring>
 #include <algorithm>
+#include <atomic>
 #include <vector>
 
 #include "common.cuh"
@@ -380,15 +381,16 @@ __device__ __forceinline__ int mirror_gauss(int p, int N0, int N) {
   return p >= N0 - N ? p - (N0 - N) : N - 1 - p;
 }
 
-// full-volume assembly fused with the octant mirroring
+// One voxel of the full volume from its octant sample: the fields (conjugated where the
+// mirroring asks for it) and the intensity, psf_debye.cl:90-101
+struct Voxel {
+  float u;
+  float2 ex, ey, ez;
+};
 template <int MIR>
-__global__ void debye_assemble_kernel(int nx, int ny, int nz, OctGeom g, int M, int Zo, float ex0, float ey0,
-                                      const float2* __restrict__ I, const float* __restrict__ trig,
-                                      float* __restrict__ u, float2* __restrict__ ex, float2* __restrict__ ey,
-                                      float2* __restrict__ ez) {
-  const int x = blockIdx.x * blockDim.x + threadIdx.x;
-  const int y = blockIdx.y, z = blockIdx.z;
-  if (x >= nx) return;
+__device__ __forceinline__ Voxel assemble_point(int x, int y, int z, int nx, int ny, int nz, const OctGeom& g, int M,
+                                                int Zo, float ex0, float ey0, const float2* __restrict__ I,
+                                                const float* __restrict__ trig) {
   int ix, jy, kz;
   bool conj;
   if (MIR == MIR_STD) {
@@ -403,21 +405,76 @@ __global__ void debye_assemble_kernel(int nx, int ny, int nz, OctGeom g, int M, 
   const float2 I0 = __ldg(I + o), I1 = __ldg(I + ZM + o), I2 = __ldg(I + 2 * ZM + o);
   const float c1 = __ldg(trig + m), s1 = __ldg(trig + M + m);
   const float c2 = __ldg(trig + 2 * M + m), s2 = __ldg(trig + 3 * M + m);
-  // psf_debye.cl:90-101
-  float2 vx = make_float2(ex0 * (I0.x + I2.x * c2) + (ey0 * s2) * I2.x, ex0 * (I0.y + I2.y * c2) + (ey0 * s2) * I2.y);
-  float2 vy = make_float2(ey0 * (I0.x - I2.x * c2) + (ex0 * s2) * I2.x, ey0 * (I0.y - I2.y * c2) + (ex0 * s2) * I2.y);
+  Voxel r;
+  r.ex = make_float2(ex0 * (I0.x + I2.x * c2) + (ey0 * s2) * I2.x, ex0 * (I0.y + I2.y * c2) + (ey0 * s2) * I2.y);
+  r.ey = make_float2(ey0 * (I0.x - I2.x * c2) + (ex0 * s2) * I2.x, ey0 * (I0.y - I2.y * c2) + (ex0 * s2) * I2.y);
   const float pz = ex0 * c1 + ey0 * s1;
-  float2 vz = make_float2(2.f * I1.y * pz, -2.f * I1.x * pz);
-  const size_t v = ((size_t)z * ny + y) * nx + x;
-  if (u) __stcs(u + v, cabs2(vx) + cabs2(vy) + cabs2(vz));
+  r.ez = make_float2(2.f * I1.y * pz, -2.f * I1.x * pz);
+  r.u = cabs2(r.ex) + cabs2(r.ey) + cabs2(r.ez);
   if (conj) {
-    vx.y = -vx.y;
-    vy.y = -vy.y;
-    vz.y = -vz.y;
+    r.ex.y = -r.ex.y;
+    r.ey.y = -r.ey.y;
+    r.ez.y = -r.ez.y;
   }
-  if (ex) __stcs(ex + v, vx);
-  if (ey) __stcs(ey + v, vy);
-  if (ez) __stcs(ez + v, vz);
+  return r;
+}
+
+// full-volume assembly fused with the octant mirroring; PAIR: two neighbouring voxels per
+// thread (even nx), stored as 8- and 16-byte vectors
+template <int MIR, bool PAIR>
+__global__ void debye_assemble_kernel(int nx, int ny, int nz, OctGeom g, int M, int Zo, float ex0, float ey0,
+                                      const float2* __restrict__ I, const float* __restrict__ trig,
+                                      float* __restrict__ u, float2* __restrict__ ex, float2* __restrict__ ey,
+                                      float2* __restrict__ ez) {
+  const int y = blockIdx.y, z = blockIdx.z;
+  if constexpr (PAIR) {
+    const int x = 2 * (blockIdx.x * blockDim.x + threadIdx.x);
+    if (x >= nx) return;
+    const Voxel a = assemble_point<MIR>(x, y, z, nx, ny, nz, g, M, Zo, ex0, ey0, I, trig);
+    const Voxel b = assemble_point<MIR>(x + 1, y, z, nx, ny, nz, g, M, Zo, ex0, ey0, I, trig);
+    const size_t v = ((size_t)z * ny + y) * nx + x;  // even: 8-byte u pairs, 16-byte field pairs
+    if (u) __stcs(reinterpret_cast<float2*>(u + v), make_float2(a.u, b.u));
+    if (ex) __stcs(reinterpret_cast<float4*>(ex + v), make_float4(a.ex.x, a.ex.y, b.ex.x, b.ex.y));
+    if (ey) __stcs(reinterpret_cast<float4*>(ey + v), make_float4(a.ey.x, a.ey.y, b.ey.x, b.ey.y));
+    if (ez) __stcs(reinterpret_cast<float4*>(ez + v), make_float4(a.ez.x, a.ez.y, b.ez.x, b.ez.y));
+  } else {
+    const int x = blockIdx.x * blockDim.x + threadIdx.x;
+    if (x >= nx) return;
+    const Voxel a = assemble_point<MIR>(x, y, z, nx, ny, nz, g, M, Zo, ex0, ey0, I, trig);
+    const size_t v = ((size_t)z * ny + y) * nx + x;
+    if (u) __stcs(u + v, a.u);
+    if (ex) __stcs(ex + v, a.ex);
+    if (ey) __stcs(ey + v, a.ey);
+    if (ez) __stcs(ez + v, a.ez);
+  }
+}
+
+// launch the assembly: pairs of voxels when nx is even and the outputs allow vector stores
+int launch_assemble(const debye_desc* d, bool gauss, const OctGeom& g, int M, int Zo, const float2* I,
+                    const float* trig, float* u, void* ex, void* ey, void* ez, cudaStream_t s) {
+  float2 *pex = static_cast<float2*>(ex), *pey = static_cast<float2*>(ey), *pez = static_cast<float2*>(ez);
+  const bool pair = d->nx % 2 == 0 && ((uintptr_t)u & 7) == 0 && ((uintptr_t)ex & 15) == 0 &&
+                    ((uintptr_t)ey & 15) == 0 && ((uintptr_t)ez & 15) == 0;
+  const int xs = pair ? d->nx / 2 : d->nx;
+  const dim3 grid((xs + 127) / 128, d->ny, d->nz);
+  const float e0 = (float)d->ex0, e1 = (float)d->ey0;
+  if (gauss) {
+    if (pair)
+      debye_assemble_kernel<MIR_GAUSS, true><<<grid, 128, 0, s>>>(d->nx, d->ny, d->nz, g, M, Zo, e0, e1, I, trig, u,
+                                                                   pex, pey, pez);
+    else
+      debye_assemble_kernel<MIR_GAUSS, false><<<grid, 128, 0, s>>>(d->nx, d->ny, d->nz, g, M, Zo, e0, e1, I, trig, u,
+                                                                    pex, pey, pez);
+  } else {
+    if (pair)
+      debye_assemble_kernel<MIR_STD, true><<<grid, 128, 0, s>>>(d->nx, d->ny, d->nz, g, M, Zo, e0, e1, I, trig, u,
+                                                                 pex, pey, pez);
+    else
+      debye_assemble_kernel<MIR_STD, false><<<grid, 128, 0, s>>>(d->nx, d->ny, d->nz, g, M, Zo, e0, e1, I, trig, u,
+                                                                  pex, pey, pez);
+  }
+  BPM_LAUNCH_CHECK("debye_assemble_kernel");
+  return BPM_OK;
 }
 
 // Fields at arbitrary points (debye_wolf_at, psf_debye.cl:187-269) or on one z plane
@@ -790,20 +847,24 @@ debye_accum_tc_kernel(const __grid_constant__ CUtensorMap mapA, const __grid_con
   if (warp == 0) tc::tmem_dealloc(tmem, a.tmem_cols);
 }
 
+// once per device (the attribute belongs to the current device's context); the opt-in
+// limit covers static and dynamic shared memory together
 cudaError_t tc_prepare() {
-  // the opt-in limit covers static and dynamic shared memory together
-  static const cudaError_t e = [] {
-    int dev = 0, optin = 0;
-    cudaFuncAttributes fa;
-    cudaError_t r;
-    if ((r = cudaGetDevice(&dev)) || (r = cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev)) ||
-        (r = cudaFuncGetAttributes(&fa, debye_accum_tc_kernel)))
-      return r;
-    const size_t room = (size_t)optin - fa.sharedSizeBytes;
-    return cudaFuncSetAttribute(debye_accum_tc_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                (int)std::min(room, TC_SMEM_MAX));
-  }();
-  return e;
+  constexpr int kDevices = 64;
+  static std::atomic<bool> done[kDevices];
+  int dev = 0, optin = 0;
+  cudaError_t r;
+  if ((r = cudaGetDevice(&dev))) return r;
+  if (dev >= 0 && dev < kDevices && done[dev].load(std::memory_order_acquire)) return cudaSuccess;
+  cudaFuncAttributes fa;
+  if ((r = cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev)) ||
+      (r = cudaFuncGetAttributes(&fa, debye_accum_tc_kernel)))
+    return r;
+  const size_t room = (size_t)optin - fa.sharedSizeBytes;
+  r = cudaFuncSetAttribute(debye_accum_tc_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                           (int)std::min(room, TC_SMEM_MAX));
+  if (r == cudaSuccess && dev >= 0 && dev < kDevices) done[dev].store(true, std::memory_order_release);
+  return r;
 }
 
 enum Variant { V_STD = 0, V_GAUSS = 1, V_PLANE = 2, V_AT = 3 };
@@ -1041,17 +1102,7 @@ int run_octant_tc(const debye_desc* d, bool gauss, double sig, float* u, void* e
   const dim3 grid(L.ntn, (rows + TC_BM - 1) / TC_BM);
   debye_accum_tc_kernel<<<grid, TC_THREADS, smem, s>>>(mA, mBh, mBl, ta);
   BPM_LAUNCH_CHECK("debye_accum_tc_kernel");
-  if (u || ex || ey || ez) {
-    const dim3 ag((d->nx + 127) / 128, d->ny, d->nz);
-    float2 *pex = static_cast<float2*>(ex), *pey = static_cast<float2*>(ey), *pez = static_cast<float2*>(ez);
-    if (gauss)
-      debye_assemble_kernel<MIR_GAUSS><<<ag, 128, 0, s>>>(d->nx, d->ny, d->nz, g, L.M, L.Zo, (float)d->ex0,
-                                                          (float)d->ey0, I, trig, u, pex, pey, pez);
-    else
-      debye_assemble_kernel<MIR_STD><<<ag, 128, 0, s>>>(d->nx, d->ny, d->nz, g, L.M, L.Zo, (float)d->ex0,
-                                                        (float)d->ey0, I, trig, u, pex, pey, pez);
-    BPM_LAUNCH_CHECK("debye_assemble_kernel");
-  }
+  if (u || ex || ey || ez) return launch_assemble(d, gauss, g, L.M, L.Zo, I, trig, u, ex, ey, ez, s);
   return BPM_OK;
 }
 
@@ -1104,19 +1155,7 @@ int run_octant(const debye_desc* d, bool gauss, double sig, float* u, void* ex, 
     debye_accum_rem_kernel<1><<<rtiles, 256, 0, s>>>(L.T, L.M, L.Mp, L.Zo, L.Zp, nrz, J, E, I);
     BPM_LAUNCH_CHECK("debye_accum_rem_kernel");
   }
-  if (u || ex || ey || ez) {
-    const dim3 grid((d->nx + 127) / 128, d->ny, d->nz);
-    float2 *pex = static_cast<float2*>(ex), *pey = static_cast<float2*>(ey), *pez = static_cast<float2*>(ez);
-    if (gauss)
-      debye_assemble_kernel<MIR_GAUSS><<<grid, 128, 0, s>>>(d->nx, d->ny, d->nz, g, L.M, L.Zo,
-                                                            (float)d->ex0, (float)d->ey0, I, trig, u, pex, pey,
-                                                            pez);
-    else
-      debye_assemble_kernel<MIR_STD><<<grid, 128, 0, s>>>(d->nx, d->ny, d->nz, g, L.M, L.Zo,
-                                                          (float)d->ex0, (float)d->ey0, I, trig, u, pex, pey,
-                                                          pez);
-    BPM_LAUNCH_CHECK("debye_assemble_kernel");
-  }
+  if (u || ex || ey || ez) return launch_assemble(d, gauss, g, L.M, L.Zo, I, trig, u, ex, ey, ez, s);
   return BPM_OK;
 }
 
