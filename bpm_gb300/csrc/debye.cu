@@ -177,6 +177,45 @@ __global__ void debye_phase_kernel(int Zo, int Zp, float z1, float z2, double k,
   E[idx] = make_float2((float)c, (float)s);
 }
 
+// Coefficients of Hankel's asymptotic expansion (Abramowitz & Stegun 9.2.5, 9.2.9, 9.2.10):
+// a_k(n) = prod_{j=1..k} (4 n^2 - (2j - 1)^2) / (8 j), so that for large x
+//   J_n(x) = sqrt(2 / (pi x)) (P_n cos chi_n - Q_n sin chi_n), chi_n = x - (n/2 + 1/4) pi,
+//   P_n = sum_k (-1)^k a_2k x^-2k,  Q_n = sum_k (-1)^k a_2k+1 x^-(2k+1).
+__host__ __device__ constexpr double hankel_a(int n, int k) {
+  double a = 1.;
+  for (int j = 1; j <= k; j++) a *= (4. * n * n - (2. * j - 1.) * (2. * j - 1.)) / (8. * j);
+  return a;
+}
+
+// J0 and J1 together. From x = 16 on, the expansion above truncated after x^-7 (its error,
+// below 2e-9 of the envelope sqrt(2 / (pi x)), is under FP32 rounding), with one sincosf of x
+// for both orders: chi_0 = x - pi/4 and chi_1 = chi_0 - pi/2, so cos chi_0 = (cos x + sin x)
+// / sqrt 2, sin chi_0 = (sin x - cos x) / sqrt 2, cos chi_1 = sin chi_0, sin chi_1 = -cos chi_0.
+// Below 16, CUDA's j0f and j1f.
+__device__ __forceinline__ void bessel_j01(float x, float& j0, float& j1) {
+  const float ax = fabsf(x);
+  if (ax < 16.f) {
+    j0 = j0f(x);
+    j1 = j1f(x);
+    return;
+  }
+  const float r = __frcp_rn(ax), y = r * r;
+  const float P0 = fmaf(fmaf(fmaf((float)-hankel_a(0, 6), y, (float)hankel_a(0, 4)), y, (float)-hankel_a(0, 2)), y, 1.f);
+  const float Q0 = r * fmaf(fmaf(fmaf((float)-hankel_a(0, 7), y, (float)hankel_a(0, 5)), y, (float)-hankel_a(0, 3)), y,
+                            (float)hankel_a(0, 1));
+  const float P1 = fmaf(fmaf(fmaf((float)-hankel_a(1, 6), y, (float)hankel_a(1, 4)), y, (float)-hankel_a(1, 2)), y, 1.f);
+  const float Q1 = r * fmaf(fmaf(fmaf((float)-hankel_a(1, 7), y, (float)hankel_a(1, 5)), y, (float)-hankel_a(1, 3)), y,
+                            (float)hankel_a(1, 1));
+  float s, c;
+  sincosf(ax, &s, &c);
+  constexpr float kInvSqrt2 = 0.70710678118654752f;
+  const float c0 = (c + s) * kInvSqrt2, s0 = (s - c) * kInvSqrt2;   // cos, sin of x - pi/4
+  const float env = sqrtf(0.63661977236758134f * r);                // sqrt(2 / (pi x))
+  j0 = env * fmaf(P0, c0, -(Q0 * s0));
+  const float j1a = env * fmaf(P1, s0, Q1 * c0);                    // P1 cos chi_1 - Q1 sin chi_1
+  j1 = x < 0.f ? -j1a : j1a;                                        // J1 is odd
+}
+
 // J2 from J0, J1: ascending series for small x, the three-term recurrence J2 = 2 J1/x - J0
 // otherwise (stable for n = 2 < x).
 __device__ __forceinline__ float bessel_j2(float x, float j0, float j1) {
@@ -208,7 +247,8 @@ __global__ void debye_bessel_kernel(int T, int M, int Mp, const double* si, cons
     return;
   }
   const float x = (float)(kr[m] * si[t]);
-  const float j0 = j0f(x), j1 = j1f(x);
+  float j0, j1;
+  bessel_j01(x, j0, j1);
   const float j2 = bessel_j2(x, j0, j1);
   J[o] = wf[t] * j0;
   J[TM + o] = wf[T + t] * j1;
@@ -540,7 +580,8 @@ __global__ void __launch_bounds__(PT_THREADS) debye_points_kernel(
     if (!active) continue;
     for (int tt = 0; tt < nt; tt++) {
       const float xb = kr * s_si[tt];
-      const float j0 = j0f(xb), j1 = j1f(xb);
+      float j0, j1;
+      bessel_j01(xb, j0, j1);
       const float j2 = bessel_j2(xb, j0, j1);
       float2 e;
       if (GRID) {
@@ -611,7 +652,8 @@ __global__ void debye_bessel_tc_kernel(int T, int Tp, int Mr, int nxo, int sym, 
   if (t >= T) return;
   const int m = radius_column(r, nxo, sym != 0);
   const float x = (float)(kr[m] * si[t]);
-  const float j0 = j0f(x), j1 = j1f(x);
+  float j0, j1;
+  bessel_j01(x, j0, j1);
   const float j2 = bessel_j2(x, j0, j1);
   const size_t o = (size_t)r * Tp + t, RT = (size_t)Mr * Tp;
   A[o] = wf[t] * j0;
