@@ -221,7 +221,8 @@ class Server:
         except Exception as e:  # pragma: no cover - surfaced through the futures
             self.error = e
             for en in self._pending:
-                en.fut.set_exception(e)
+                if not en.fut.done():
+                    en.fut.set_exception(e)
             for la in self._inflight:
                 for en in la.entries:
                     if not en.fut.done():
@@ -257,7 +258,14 @@ class Server:
                 still.append(la)
         self._inflight = still
 
+    def _drop_cancelled(self):
+        """Requests whose future the caller cancelled while they waited are dropped; a
+        request admitted to a launch is running and can no longer be cancelled
+        (Future.set_running_or_notify_cancel)."""
+        self._pending = [en for en in self._pending if not en.fut.cancelled()]
+
     def _admit(self):
+        self._drop_cancelled()
         while self._pending and self._free_streams:
             head = self._pending[0]
             if self._used + head.req.footprint() > self.budget:
@@ -275,7 +283,10 @@ class Server:
                         fp += en.req.footprint()
             for en in group:
                 self._pending.remove(en)
-            self._launch(group)
+            # claim the futures; one cancelled since _drop_cancelled leaves the group
+            group = [en for en in group if en.fut.set_running_or_notify_cancel()]
+            if group:
+                self._launch(group)
 
     def _launch(self, group):
         stream = self._free_streams.pop()

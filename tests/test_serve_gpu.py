@@ -116,6 +116,34 @@ def test_launches_overlap_on_the_device(env):
         assert np.array_equal(o.cpu().numpy(), want)
 
 
+def test_cancelled_requests_are_dropped(env):
+    """Futures cancelled while their requests wait are dropped by the scheduler; the other
+    requests complete with the same results as alone, and the server keeps serving."""
+    torch, bpm, BpmRequest, PsfRequest, Server = env
+    side, nz = 64, 12
+    reqs = [BpmRequest((side, side, nz), (.1, .1, .1), n0=1.33, mean_mode="ignore",
+                       u0=np.exp(1j * .04 * k * np.arange(side))[None].repeat(side, 0).astype(np.complex64))
+            for k in range(16)]
+    # a budget of one request at a time keeps the later ones waiting long enough to cancel
+    srv = Server(hbm_budget=int(1.5 * reqs[0].footprint()), max_inflight=1, max_batch=1)
+    futs = [srv.submit(r) for r in reqs]
+    cancelled = [f.cancel() for f in futs[8:]]
+    done = [f.result(timeout=60) for f in futs[:8]]
+    for f, c in zip(futs[8:], cancelled):
+        if c:
+            assert f.cancelled()
+        else:   # admitted before the cancel arrived: it runs to the end
+            f.result(timeout=60)
+    assert any(cancelled)
+    late = srv.submit(reqs[0]).result(timeout=60)
+    srv.close()
+    assert srv.error is None
+    for r, o in zip(reqs[:8], done):
+        want = bpm.bpm_3d(r.size, r.units, lam=r.lam, n0=r.n0, u0=r.u0, mean_mode="ignore", return_field=False)
+        assert np.array_equal(o.cpu().numpy(), want)
+    assert np.array_equal(late.cpu().numpy(), done[0].cpu().numpy())
+
+
 def test_oversized_request_is_refused(env):
     torch, bpm, BpmRequest, PsfRequest, Server = env
     srv = Server(hbm_budget=1 << 20)
