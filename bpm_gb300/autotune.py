@@ -8,8 +8,8 @@ include/bpm_gb300.h):
              every concurrent group's planes inside L2;
   conc       groups marching at once on their own streams (1, 2, 4, 8), so one group's
              kernels fill the SMs another group's tail wave leaves idle;
-  col_block  columns per block of the non-weighted column passes (8 or 16): 8-column blocks
-             spread a small pass over twice the SMs, 16-column blocks issue fewer
+  col_block  columns per block of the non-weighted column passes (4, 8 or 16): narrower
+             blocks spread a small pass over more SMs, 16-column blocks issue fewer
              instructions per column;
   cluster    the whole-march cluster kernel (the field in distributed shared memory, square
              64..256 grids) against the row/column pass kernels;
@@ -32,7 +32,7 @@ from . import _native as N
 __all__ = ["tune_shape", "tune_group", "pick_group", "pick_option", "shape_candidates", "cache_path"]
 
 _cache = None
-_VERSION = 3  # cache entries of another layout are measured again
+_VERSION = 4  # cache entries of another layout are measured again
 
 
 def cache_path():
@@ -96,7 +96,7 @@ def shape_candidates(size, batch, group, mean_mode):
     if ngroups > 1:
         out["conc"] = [1, 2, 4, 8]
     if mean_mode != "weighted" and Ny >= 128:
-        out["col_block"] = [8, 16]    # the weighted passes keep 16-column blocks
+        out["col_block"] = [4, 8, 16]    # the weighted passes keep 16-column blocks
     if Nx == Ny and Nx in (64, 128, 256):
         out["cluster"] = [1, 2]
     if mean_mode == "weighted" and Ny in (128, 256, 512) and Nx % 32 == 0 and Nx <= 512:

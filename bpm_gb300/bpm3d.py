@@ -194,11 +194,14 @@ def _slice_tables(dn, n0, dev):
 def mask_pays(batch, Nx, Ny):
     """Whether a march of `batch` fields through one shared dn volume computes its phase
     masks once up front (precompute_mask) instead of per element in every row pass. The
-    results are the same bits either way. It pays for several fields, and for one field
-    from 512x512 up, where the row pass is bound by its per-element exp/sincos (GB300, one
-    field, Nz 128, precompute included: 1024^2 5.9 -> 4.6 ms ignore / 8.1 -> 7.0 ms
-    weighted, 512^2 2.5 -> 2.3 / 3.7 -> 3.2 ms; at 256^2 the weighted march slows down)."""
-    return batch >= 2 or Nx * Ny >= 512 * 512
+    results are the same bits either way. It pays for several fields, and for one field on
+    every grid measured, where the row pass stages one mask row instead of evaluating
+    exp/sincos per element (GB300, one field, precompute included, per-element -> mask:
+    Nz 128 ignore with complex dn 1024^2 4.74 -> 3.55 ms, 512^2 1.70 -> 1.23, 256^2 0.84 ->
+    0.74, 128^2 0.89 -> 0.81; weighted 1024^2 6.04 -> 5.01, 512^2 (Nz 256) 5.78 -> 4.57,
+    256^2 1.51 -> 1.38, 128^2 1.20 -> 1.13, 64^2 (Nz 64) 0.419 -> 0.405). Below 64x64 it
+    stays per element (not measured)."""
+    return batch >= 2 or Nx * Ny >= 64 * 64
 
 
 def precompute_mask(plan, dn_t, dn_kind):

@@ -438,7 +438,7 @@ struct ColParams {
   const float2* tw;
   const float2* wtw;         // stage-ordered twiddles of the warp FFT
   int dn_stage;              // weighted: dn rows may be staged with 16-byte cp.async
-  int col_block;             // 0: the library's rule; 8 or 16 columns per non-weighted block
+  int col_block;             // 0: the library's rule; 4, 8 or 16 columns per non-weighted block
   int col_fuse;              // weighted: 1 one fused column pass where available, 0 or 2 two passes
 };
 
@@ -840,11 +840,14 @@ row_shared_kernel(RowParams p, int nfields, int fw_rt) {
 // Column buffers are STRIDE float2 apart: with 16 columns an odd stride puts a half-warp's
 // 16 columns on 16 different bank pairs; with 8 columns a half-warp spans two rows of 8
 // columns, conflict-free at N = 512 and 1024 for stride BUF + 2, 2-way on some accesses at
-// 128 and 256.
+// 128 and 256; with 4 columns four rows of 4, conflict-free at 512 and 1024 for BUF + 4
+// (BUF is a multiple of 16 there), 2-way at best at 128 and 256 (BUF + 2). Checked for every
+// first-stage store and last-stage load of each half-warp by brute force on the CPU.
 template <int N, int C = kColWarps, int L = 32>
 struct ColSplitCfg {
   static constexpr int BUF = WarpFft<N, L>::BUF;
-  static constexpr int STRIDE = (C == 8 && N / L >= 16) ? BUF + 2 : (BUF | 1);
+  static constexpr int STRIDE = C == 4 ? (N / L >= 16 ? BUF + 4 : BUF + 2)
+                                       : ((C == 8 && N / L >= 16) ? BUF + 2 : (BUF | 1));
   static constexpr int TW_F2 = (WarpFft<N, L>::TW + 1) & ~1;
   static constexpr int DN_F2 = (TW_F2 + C * STRIDE + 1) & ~1;  // 16-byte aligned
   static constexpr size_t SMEM = (size_t)DN_F2 * sizeof(float2);
@@ -915,7 +918,7 @@ col_split_kernel(ColParams p) {
   using Cfg = ColSplitCfg<N, C, L>;
   constexpr int E = N / L;
   constexpr int T = C * L;
-  static_assert(C == 16 || (C == 8 && WHICH == 0), "weighted passes keep 16-column blocks");
+  static_assert(C == 16 || ((C == 8 || C == 4) && WHICH == 0), "weighted passes keep 16-column blocks");
   static_assert(!SCAT || (C == 16 && WHICH != 1), "scattering partials per 16-column tile");
   extern __shared__ __align__(16) float2 smem[];
   float2* tw = smem;
@@ -1614,11 +1617,12 @@ struct RowK {
     }
   }
   // all fields of the group share the slice-z mask row: the precomputed mask, or one dn
-  // volume (dn_batch_stride 0); the row is staged with 16-byte cp.async
-  static bool shared_ok(const RowParams& p) {
+  // volume (dn_batch_stride 0, or a group of one field); the row is staged with 16-byte
+  // cp.async
+  static bool shared_ok(const RowParams& p, int nfields) {
     if (!p.do_mask) return false;
     if (p.mask) return aligned16(p.mask);
-    return p.dn_bstride == 0 && aligned16(p.dn);
+    return (p.dn_bstride == 0 || nfields == 1) && aligned16(p.dn);
   }
   // g.x counts 16-row tiles
   static int launch(dim3 g, cudaStream_t s, const RowParams& p, bool adj) {
@@ -1643,7 +1647,11 @@ struct RowK {
   static int launch_warp(dim3 g, cudaStream_t s, const RowParams& p, bool adj) {
     if constexpr (WARP) {
       constexpr int BUF = WarpFft<N, L>::BUF;
-      if (!adj && shared_ok(p) && g.y >= 2) {
+      // a single field takes this kernel too (one-warp blocks): its mask or dn row is staged
+      // by cp.async at block start, so the row's DRAM read overlaps the inverse row FFT
+      // instead of following it as in row_warp_kernel (GB300, one field, Nz 128, same bits:
+      // 1024^2 ignore 3.63 -> 2.55 ms, 512^2 2.04 -> 1.14 ms, 512^2 weighted 3.00 -> 2.05 ms)
+      if (!adj && shared_ok(p, (int)g.y)) {
         // fields per block: the group split evenly over ceil(G / 8) blocks per row
         const int nb = ((int)g.y + kRowWarps - 1) / kRowWarps;
         const int fw = ((int)g.y + nb - 1) / nb;
@@ -1655,8 +1663,9 @@ struct RowK {
         BPM_LAUNCH_CHECK("row_shared_kernel");
         return BPM_OK;
       }
-      // with fewer 8-row blocks than twice the SMs (a single field, small per-field-dn
-      // groups), blocks of 2 rows spread the pass over 4 times as many SMs
+      // with fewer 8-row blocks than twice the SMs (a single field's adjoint or unaligned
+      // mask, small per-field-dn groups), blocks of 2 rows spread the pass over 4 times as
+      // many SMs
       const int rows = (int)(g.x * 16) * (int)g.y;
       if (rows / kRowWarps < 2 * sm_count()) {
         const dim3 gw(g.x * 16 / 2, g.y);
@@ -1695,12 +1704,17 @@ struct ColK {
   template <int L>
   static constexpr size_t split8_smem() { return ColSplitCfg<N, 8, L>::SMEM_KY; }
   template <int L>
+  static constexpr size_t split4_smem() { return ColSplitCfg<N, 4, L>::SMEM_KY; }
+  template <int L>
   static void prepare_l() {
     cudaFuncSetAttribute(col_split_kernel<N, WHICH, kColWarps, false, L>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                          (int)split_smem<L>());
-    if constexpr (WHICH == 0)
+    if constexpr (WHICH == 0) {
       cudaFuncSetAttribute(col_split_kernel<N, 0, 8, false, L>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                            (int)split8_smem<L>());
+      cudaFuncSetAttribute(col_split_kernel<N, 0, 4, false, L>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                           (int)split4_smem<L>());
+    }
     if constexpr (WHICH != 1)
       cudaFuncSetAttribute(col_split_kernel<N, WHICH, kColWarps, true, L>,
                            cudaFuncAttributeMaxDynamicSharedMemorySize, (int)split_smem<L>());
@@ -1717,8 +1731,19 @@ struct ColK {
   static int launch_split(dim3 g, cudaStream_t s, const ColParams& p) {
     // a non-weighted pass with fewer 16-column blocks than SMs runs 8-column blocks, so twice
     // as many SMs share it (the columns' arithmetic is the same); so does every non-weighted
-    // pass with 32 values per thread, whose 16-column blocks take half an SM's registers
+    // pass with 32 values per thread, whose 16-column blocks take half an SM's registers; and
+    // with fewer 8-column blocks than SMs and up to 16 values per thread (a single field of
+    // 256 or 512 rows), 4-column blocks (GB300, one field, Nz 128: 512^2 ignore 1.12 -> 1.03
+    // ms, 256^2 0.68 -> 0.62 ms; at 1024 rows they measured slower, 2.53 -> 2.94 ms)
     if constexpr (WHICH == 0) {
+      const bool quarter =
+          p.col_block == 4 || (p.col_block == 0 && N / L < 32 && (int)(g.x * 2 * g.y) < sm_count());
+      if (!p.scat && quarter) {
+        BPM_CUDA_TRY(launch_dep(col_split_kernel<N, 0, 4, false, L>, dim3(g.x * 4, g.y), dim3(4 * L),
+                                split4_smem<L>(), s, p));
+        BPM_LAUNCH_CHECK("col_split_kernel");
+        return BPM_OK;
+      }
       const bool narrow = p.col_block == 8 || (p.col_block == 0 && ((int)(g.x * g.y) < sm_count() || N / L >= 32));
       if (!p.scat && narrow) {
         BPM_CUDA_TRY(launch_dep(col_split_kernel<N, 0, 8, false, L>, dim3(g.x * 2, g.y), dim3(8 * L),
@@ -1908,8 +1933,8 @@ int check_request(const bpm_plan* pl, const bpm_request* r) {
   if (r->scatter_g && !r->scatter_p) { set_error("scatter_g needs scatter_p"); return BPM_ERR_ARG; }
   if (r->group < 0) { set_error("group must be >= 0"); return BPM_ERR_ARG; }
   if (r->conc < 0 || r->conc > kMaxConcurrentGroups) { set_error("conc must be in 0..8"); return BPM_ERR_ARG; }
-  if (r->col_block != 0 && r->col_block != 8 && r->col_block != 16) {
-    set_error("col_block must be 0, 8 or 16");
+  if (r->col_block != 0 && r->col_block != 4 && r->col_block != 8 && r->col_block != 16) {
+    set_error("col_block must be 0, 4, 8 or 16");
     return BPM_ERR_ARG;
   }
   if (r->cluster < 0 || r->cluster > 2) { set_error("cluster must be 0, 1 or 2"); return BPM_ERR_ARG; }

@@ -107,7 +107,7 @@ typedef struct {
    * cluster at 64x64, where the two families run FFTs of another radix order (FP32 rounding). */
   int conc;                      /* groups marching at once on their own streams, 1..8
                                     (default BPM_GB300_CONC, else 4)                            */
-  int col_block;                 /* columns per block of the non-weighted column passes, 8 or 16 */
+  int col_block;                 /* columns per block of the non-weighted column passes, 4, 8 or 16 */
   int cluster;                   /* whole-march cluster kernel (square 64..256 grids without
                                     scattering sums or checkpoints): 1 = use it, 2 = row/column
                                     pass kernels (default: cluster at 64 and 128)               */

@@ -120,11 +120,12 @@ def test_psf_request_footprint_covers_the_workspace(native):
 
 def test_mask_policy():
     """Phase masks are precomputed for several fields through one dn, and for one field
-    from 512 x 512 points up."""
+    from 64 x 64 points up."""
     from bpm_gb300.bpm3d import mask_pays
-    assert mask_pays(2, 64, 32) and mask_pays(64, 512, 512)
+    assert mask_pays(2, 64, 32) and mask_pays(2, 16, 16) and mask_pays(64, 512, 512)
     assert mask_pays(1, 512, 512) and mask_pays(1, 1024, 256) and mask_pays(1, 1024, 1024)
-    assert not mask_pays(1, 256, 256) and not mask_pays(1, 512, 256) and not mask_pays(1, 16, 16)
+    assert mask_pays(1, 256, 256) and mask_pays(1, 512, 256) and mask_pays(1, 64, 64)
+    assert not mask_pays(1, 32, 64) and not mask_pays(1, 16, 16)
 
 
 def test_serve_request_keys_and_footprint():
@@ -168,5 +169,5 @@ def test_autotune_shape_choices():
     c = shape_candidates((512, 512), 64, 8, "weighted")
     assert c == {"conc": [1, 2, 4, 8], "col_fuse": [1, 2]}             # weighted passes keep 16 columns
     c = shape_candidates((256, 256), 4, 4, "ignore")
-    assert c == {"col_block": [8, 16], "cluster": [1, 2]}              # one group: no concurrency choice
+    assert c == {"col_block": [4, 8, 16], "cluster": [1, 2]}              # one group: no concurrency choice
     assert "cluster" not in shape_candidates((512, 256), 8, 2, "ignore")

@@ -45,7 +45,7 @@ def test_every_launch_shape_gives_the_same_result(bpm, size, batch, mode, cplx):
     kw = dict(lam=.5, n0=1.33, dn=dn, mean_mode=mode, absorbing_width=3, return_field=True)
     ref = bpm.bpm_3d_batched(size, (.1, .1, .1), u0=u0, **kw)
     n = 0
-    for group, conc, col_block, cluster, fuse in itertools.product((1, 3, 0), (1, 2, 8), (8, 16), (1, 2), (1, 2)):
+    for group, conc, col_block, cluster, fuse in itertools.product((1, 3, 0), (1, 2, 8), (4, 8, 16), (1, 2), (1, 2)):
         launch = {"group": group, "conc": conc, "col_block": col_block, "cluster": cluster, "col_fuse": fuse}
         got = bpm.bpm_3d_batched(size, (.1, .1, .1), u0=u0, launch=launch, **kw)
         if size[0] == 64 and cluster == 2:
@@ -55,7 +55,7 @@ def test_every_launch_shape_gives_the_same_result(bpm, size, batch, mode, cplx):
         else:
             assert np.array_equal(got, ref), launch
         n += 1
-    assert n == 72
+    assert n == 108
 
 
 def test_tuned_shape_is_applied(bpm, tmp_path, monkeypatch):
@@ -69,7 +69,7 @@ def test_tuned_shape_is_applied(bpm, tmp_path, monkeypatch):
     shape = autotune.tune_shape(size, (.1, .1, .1), .5, 1.33, batch, dn_t, "weighted", "intensity")
     assert set(shape) == {"group", "conc", "col_block", "cluster", "col_fuse"}
     assert 1 <= shape["group"] <= batch and shape["conc"] in (0, 1, 2, 4, 8)
-    assert shape["col_block"] in (0, 8, 16) and shape["cluster"] in (0, 1, 2) and shape["col_fuse"] in (0, 1, 2)
+    assert shape["col_block"] in (0, 4, 8, 16) and shape["cluster"] in (0, 1, 2) and shape["col_fuse"] in (0, 1, 2)
     assert (tmp_path / "tune.json").exists()
     assert autotune.tune_shape(size, (.1, .1, .1), .5, 1.33, batch, dn_t, "weighted", "intensity") == shape
     m = bpm.BatchedMarch(size, (.1, .1, .1), .5, 1.33, batch, dn=dn_t, group="auto")
