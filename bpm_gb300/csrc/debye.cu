@@ -113,18 +113,17 @@ __device__ __forceinline__ float coord_f32(int i, float x1, float x2, int N) {
   return __fadd_rn(x1, __fdiv_rn(__fmul_rn((float)i, __fsub_rn(x2, x1)), __fsub_rn((float)N, 1.f)));
 }
 
-// trapezoid nodes and weights per annulus (psf_debye.cl:62-78), FP64
-__global__ void debye_nodes_kernel(NodeArgs a, double* si, double* ct, float* wf, int T) {
-  int idx = blockIdx.x * blockDim.x + threadIdx.x;
-  if (idx >= T) return;
+constexpr double kTwoPi = 6.283185307179586, kInvTwoPi = 0.15915494309189535;
+
+// trapezoid node idx of its annulus (psf_debye.cl:62-78), FP64: sin t, cos t and the pupil
+// weight w
+__device__ __forceinline__ void node_values(const NodeArgs& a, int idx, double& s, double& c, double& w) {
   const int per = a.steps + 1;
   const int ann = idx / per, i = idx - ann * per;
   const double a1 = a.alpha[2 * ann], a2 = a.alpha[2 * ann + 1];
   const double dt = (a2 - a1) / (a.steps - 1.);
   const double t = a1 + i * dt;
-  double s, c;
   sincos(t, &s, &c);
-  double w;
   if (a.kind == W_STD) {
     w = ((i == 0 || i == a.steps) ? .5 : 1.) * dt * sqrt(c);
   } else if (a.kind == W_PHYS) {
@@ -137,28 +136,55 @@ __global__ void debye_nodes_kernel(NodeArgs a, double* si, double* ct, float* wf
     w = ((tf == a1f || tf == a2f) ? .5 : 1.) * dt * sqrt(c) * s;
     if (a.kind == W_GAUSS) w *= exp(t * t * a.gauss_prefac);
   }
-  si[idx] = s;
-  ct[idx] = c;
+}
+
+// the per-order node factors p_0 = w (cos t + 1), p_1 = w sin t, p_2 = w (cos t - 1)
+__device__ __forceinline__ void node_store(float* wf, int T, int idx, double s, double c, double w) {
   wf[idx] = (float)(w * (c + 1.));
   wf[T + idx] = (float)(w * s);
   wf[2 * T + idx] = (float)(w * (c - 1.));
+}
+
+__global__ void debye_nodes_kernel(NodeArgs a, double* si, double* ct, float* wf, int T) {
+  int idx = blockIdx.x * blockDim.x + threadIdx.x;
+  if (idx >= T) return;
+  double s, c, w;
+  node_values(a, idx, s, c, w);
+  si[idx] = s;
+  ct[idx] = c;
+  node_store(wf, T, idx, s, c, w);
+}
+
+// k r of octant column m in FP64, and (cos phi, sin phi, cos 2 phi, sin 2 phi) of its azimuth
+// from the coordinates: x / r, y / r, (x - y)(x + y) / r^2, 2 x y / r^2 (phi = 0 at the origin,
+// as atan2(0, 0))
+__device__ __forceinline__ double radius_values(const OctGeom& g, double k, int m, float4& trig) {
+  const int jy = m / g.nxo, ix = m - jy * g.nxo;
+  const double x = coord_f32(ix, g.x1, g.x2, g.nxo), y = coord_f32(jy, g.y1, g.y2, g.nyo);
+  const double r2 = x * x + y * y;
+  if (r2 == 0.) {
+    trig = make_float4(1.f, 0.f, 1.f, 0.f);
+    return 0.;
+  }
+  const double r = sqrt(r2), ir = 1. / r, ir2 = ir * ir;
+  trig = make_float4((float)(x * ir), (float)(y * ir), (float)((x - y) * (x + y) * ir2), (float)(2. * x * y * ir2));
+  return k * r;
+}
+
+__device__ __forceinline__ void trig_store(float* trig, int M, int m, float4 v) {
+  trig[m] = v.x;
+  trig[M + m] = v.y;
+  trig[2 * M + m] = v.z;
+  trig[3 * M + m] = v.w;
 }
 
 // radius and azimuth per octant column (ix, jy)
 __global__ void debye_radii_kernel(OctGeom g, double k, double* kr, float* trig, int M) {
   int m = blockIdx.x * blockDim.x + threadIdx.x;
   if (m >= M) return;
-  const int jy = m / g.nxo, ix = m - jy * g.nxo;
-  const double x = coord_f32(ix, g.x1, g.x2, g.nxo), y = coord_f32(jy, g.y1, g.y2, g.nyo);
-  kr[m] = k * sqrt(x * x + y * y);
-  const double phi = atan2(y, x);
-  double s1, c1, s2, c2;
-  sincos(phi, &s1, &c1);
-  sincos(2. * phi, &s2, &c2);
-  trig[m] = (float)c1;
-  trig[M + m] = (float)s1;
-  trig[2 * M + m] = (float)c2;
-  trig[3 * M + m] = (float)s2;
+  float4 tv;
+  kr[m] = radius_values(g, k, m, tv);
+  trig_store(trig, M, m, tv);
 }
 
 // E(t, z) = exp(i kz cos t), phase formed and reduced in FP64
@@ -227,7 +253,7 @@ __device__ __forceinline__ float bessel_j2(float x, float j0, float j1) {
     float sum = term;
 #pragma unroll
     for (int k = 1; k < 12; k++) {
-      term *= -q / (float)(k * (k + 2));
+      term *= -q * (1.f / (float)(k * (k + 2)));  // the reciprocal folds to a constant
       sum += term;
     }
     return sum;
@@ -533,7 +559,6 @@ struct PointArgs {
 };
 
 constexpr int PT_THREADS = 128, PT_CHUNK = 256;
-constexpr double kTwoPi = 6.283185307179586, kInvTwoPi = 0.15915494309189535;
 
 template <bool GRID>
 __global__ void __launch_bounds__(PT_THREADS) debye_points_kernel(
@@ -642,16 +667,80 @@ __device__ __forceinline__ int radius_column(int r, int nxo, bool sym) {
   return b * nxo + a;
 }
 
-// A(n Mr + r, t) = p_n(t) J_n(kr sin t): the same values as debye_bessel_kernel's tables
-__global__ void debye_bessel_tc_kernel(int T, int Tp, int Mr, int nxo, int sym, const double* __restrict__ si,
-                                       const double* __restrict__ kr, const float* __restrict__ wf,
-                                       float* __restrict__ A) {
+// An FP64 value v as a float pair (hi, lo): hi = v rounded to FP32, lo = v - hi rounded to FP32,
+// so hi + lo is v to about 2^-48 relative.
+__device__ __forceinline__ float2 split_pair(double v) {
+  const float hi = (float)v;
+  return make_float2(hi, (float)(v - (double)hi));
+}
+
+// a * b of two float pairs, rounded once to FP32: the exact rounding error of a.hi b.hi (an
+// FMA) plus the cross terms, added to the rounded product (a.lo b.lo is below 2^-48). The
+// result is the FP32 rounding of the FP64 product except where that product lies within
+// about 2^-46 of a rounding boundary; it takes FP32 instructions instead of two of the FP64
+// pipe, which runs at 1/64 of the FP32 rate on this GPU.
+__device__ __forceinline__ float mul_pair(float2 a, float2 b) {
+  const float p = __fmul_rn(a.x, b.x);
+  const float e = fmaf(a.x, b.x, -p);
+  return __fadd_rn(p, fmaf(a.x, b.y, fmaf(a.y, b.x, e)));
+}
+
+// Nodes and radii of the tensor-core path in one launch: blocks [0, nbn) one quadrature node
+// per thread (as debye_nodes_kernel: cos t in FP64 for the phases, the three node factors,
+// sin t as a float pair), the others one octant column per thread (as debye_radii_kernel,
+// k r as a float pair). 32-thread blocks spread the FP64 chains over the SMs.
+__global__ void debye_setup_tc_kernel(NodeArgs a, OctGeom g, double k, int T, int M, int nbn, double* ct,
+                                      float* wf, float2* si2, float2* kr2, float* trig) {
+  if ((int)blockIdx.x < nbn) {
+    const int idx = blockIdx.x * blockDim.x + threadIdx.x;
+    if (idx >= T) return;
+    double sn, c, w;
+    node_values(a, idx, sn, c, w);
+    ct[idx] = c;
+    si2[idx] = split_pair(sn);
+    node_store(wf, T, idx, sn, c, w);
+  } else {
+    const int m = (blockIdx.x - nbn) * blockDim.x + threadIdx.x;
+    if (m >= M) return;
+    float4 tv;
+    kr2[m] = split_pair(radius_values(g, k, m, tv));
+    trig_store(trig, M, m, tv);
+  }
+}
+
+// The operand tables of the product in one launch of 128-thread blocks, each over 128 nodes
+// (tb blocks per row):
+//   blocks [0, nph): Bh/Bl(2z + {0, 1}, t) = high/low parts of (cos, sin)(kz_z cos t), the
+//     phase formed and reduced modulo 2 pi in FP64, its sine and cosine in FP32;
+//   the rest: A(n Mr + r, t) = p_n(t) J_n(kr sin t) (debye_bessel_kernel's values, x = kr sin t
+//     rounded to FP32 from the pair product).
+__global__ void debye_tables_tc_kernel(int T, int Tp, int Mr, int nxo, int sym, int Zo, int nph, float z1, float z2,
+                                       double k, const double* __restrict__ ct, const float2* __restrict__ si2,
+                                       const float2* __restrict__ kr2, const float* __restrict__ wf,
+                                       float* __restrict__ A, float* __restrict__ Bh, float* __restrict__ Bl) {
   const int tb = (T + 127) / 128;
-  const int r = blockIdx.x / tb;
-  const int t = (blockIdx.x - r * tb) * 128 + threadIdx.x;
+  if ((int)blockIdx.x < nph) {
+    const int z = blockIdx.x / tb;
+    const int t = (blockIdx.x - z * tb) * 128 + threadIdx.x;
+    if (t >= T) return;
+    const double kz = k * (double)(Zo == 1 ? z1 : coord_f32(z, z1, z2, Zo));
+    const double arg = kz * ct[t];
+    const double q = rint(arg * kInvTwoPi);
+    float c, sn;
+    sincosf((float)fma(-q, kTwoPi, arg), &sn, &c);
+    const size_t o = (size_t)(2 * z) * Tp + t;
+    Bh[o] = tf32_hi(c);
+    Bl[o] = c - tf32_hi(c);
+    Bh[o + Tp] = tf32_hi(sn);
+    Bl[o + Tp] = sn - tf32_hi(sn);
+    return;
+  }
+  const int b = blockIdx.x - nph;
+  const int r = b / tb;
+  const int t = (b - r * tb) * 128 + threadIdx.x;
   if (t >= T) return;
   const int m = radius_column(r, nxo, sym != 0);
-  const float x = (float)(kr[m] * si[t]);
+  const float x = mul_pair(kr2[m], si2[t]);
   float j0, j1;
   bessel_j01(x, j0, j1);
   const float j2 = bessel_j2(x, j0, j1);
@@ -659,25 +748,6 @@ __global__ void debye_bessel_tc_kernel(int T, int Tp, int Mr, int nxo, int sym, 
   A[o] = wf[t] * j0;
   A[RT + o] = wf[T + t] * j1;
   A[2 * RT + o] = wf[2 * T + t] * j2;
-}
-
-// Bh/Bl(2z + {0, 1}, t) = high/low parts of (cos, sin)(kz_z cos t), phase formed and
-// reduced in FP64 as debye_phase_kernel's
-__global__ void debye_phase_tc_kernel(int T, int Tp, int Zo, float z1, float z2, double k, const double* ct,
-                                      float* __restrict__ Bh, float* __restrict__ Bl) {
-  const int tb = (T + 127) / 128;
-  const int z = blockIdx.x / tb;
-  const int t = (blockIdx.x - z * tb) * 128 + threadIdx.x;
-  if (t >= T) return;
-  const double kz = k * (double)(Zo == 1 ? z1 : coord_f32(z, z1, z2, Zo));
-  double sd, cd;
-  sincos(kz * ct[t], &sd, &cd);
-  const float c = (float)cd, sn = (float)sd;
-  const size_t o = (size_t)(2 * z) * Tp + t;
-  Bh[o] = tf32_hi(c);
-  Bl[o] = c - tf32_hi(c);
-  Bh[o + Tp] = tf32_hi(sn);
-  Bl[o + Tp] = sn - tf32_hi(sn);
 }
 
 constexpr int TC_BM = 128, TC_BK = 32, TC_THREADS = 128;
@@ -1028,7 +1098,7 @@ void octant_setup(const debye_desc* d, bool gauss, double sig, int nxo, int nyo,
 }
 
 struct TcLayout {
-  size_t si, ct, wf, kr, trig, A, Bh, Bl, I, total;
+  size_t si2, ct, wf, kr2, trig, A, Bh, Bl, I, total;
   int T, Tp, M, Mr, Zo, nxo, nyo, nzo, BN, ntn, stages;
   bool sym;
 };
@@ -1059,10 +1129,10 @@ TcLayout tc_layout(const debye_desc* d, bool gauss) {
   L.BN = ((cols + L.ntn - 1) / L.ntn + 15) & ~15;
   L.stages = tc_smem_bytes(L.BN, 3) <= TC_SMEM_MAX ? 3 : 2;
   size_t off = 0;
-  L.si = off; off += align256(sizeof(double) * L.T);
+  L.si2 = off; off += align256(sizeof(float2) * L.T);
   L.ct = off; off += align256(sizeof(double) * L.T);
   L.wf = off; off += align256(sizeof(float) * 3 * L.T);
-  L.kr = off; off += align256(sizeof(double) * L.M);
+  L.kr2 = off; off += align256(sizeof(float2) * L.M);
   L.trig = off; off += align256(sizeof(float) * 4 * L.M);
   L.A = off; off += align256(sizeof(float) * 3 * (size_t)L.Mr * L.Tp);
   L.Bh = off; off += align256(sizeof(float) * 2 * (size_t)L.Zo * L.Tp);
@@ -1085,10 +1155,10 @@ int run_octant_tc(const debye_desc* d, bool gauss, double sig, float* u, void* e
   }
   if (!aligned16(ws)) { set_error("workspace must be 16-byte aligned"); return BPM_ERR_ARG; }
   char* w = static_cast<char*>(ws);
-  double* si = reinterpret_cast<double*>(w + L.si);
+  float2* si2 = reinterpret_cast<float2*>(w + L.si2);
   double* ct = reinterpret_cast<double*>(w + L.ct);
   float* wf = reinterpret_cast<float*>(w + L.wf);
-  double* kr = reinterpret_cast<double*>(w + L.kr);
+  float2* kr2 = reinterpret_cast<float2*>(w + L.kr2);
   float* trig = reinterpret_cast<float*>(w + L.trig);
   float* A = reinterpret_cast<float*>(w + L.A);
   float* Bh = reinterpret_cast<float*>(w + L.Bh);
@@ -1108,15 +1178,14 @@ int run_octant_tc(const debye_desc* d, bool gauss, double sig, float* u, void* e
     return BPM_ERR_CUDA;
   }
   const int tb = (L.T + 127) / 128;
-  debye_nodes_kernel<<<(L.T + 127) / 128, 128, 0, s>>>(na, si, ct, wf, L.T);
-  BPM_LAUNCH_CHECK("debye_nodes_kernel");
-  debye_radii_kernel<<<(L.M + 127) / 128, 128, 0, s>>>(g, k, kr, trig, L.M);
-  BPM_LAUNCH_CHECK("debye_radii_kernel");
-  debye_phase_tc_kernel<<<(unsigned)(tb * L.Zo), 128, 0, s>>>(L.T, L.Tp, L.Zo, g.z1, g.z2, k, ct, Bh, Bl);
-  BPM_LAUNCH_CHECK("debye_phase_tc_kernel");
-  debye_bessel_tc_kernel<<<(unsigned)((size_t)tb * L.Mr), 128, 0, s>>>(L.T, L.Tp, L.Mr, L.nxo, L.sym ? 1 : 0, si,
-                                                                      kr, wf, A);
-  BPM_LAUNCH_CHECK("debye_bessel_tc_kernel");
+  const int nbn = (L.T + 31) / 32;
+  debye_setup_tc_kernel<<<(unsigned)(nbn + (L.M + 31) / 32), 32, 0, s>>>(na, g, k, L.T, L.M, nbn, ct, wf, si2, kr2,
+                                                                          trig);
+  BPM_LAUNCH_CHECK("debye_setup_tc_kernel");
+  const int nph = tb * L.Zo;
+  debye_tables_tc_kernel<<<(unsigned)(nph + (size_t)tb * L.Mr), 128, 0, s>>>(
+      L.T, L.Tp, L.Mr, L.nxo, L.sym ? 1 : 0, L.Zo, nph, g.z1, g.z2, k, ct, si2, kr2, wf, A, Bh, Bl);
+  BPM_LAUNCH_CHECK("debye_tables_tc_kernel");
   TcArgs ta;
   ta.T = L.T;
   ta.rows = rows;
