@@ -443,30 +443,14 @@ __global__ void __launch_bounds__(256) debye_accum_rem_kernel(int T, int M, int 
     }
 }
 
-__device__ __forceinline__ int mirror_gauss(int p, int N0, int N) {
-  return p >= N0 - N ? p - (N0 - N) : N - 1 - p;
-}
-
-// One voxel of the full volume from its octant sample: the fields (conjugated where the
-// mirroring asks for it) and the intensity, psf_debye.cl:90-101
+// The fields and intensity of octant sample (ix, jy, kz), psf_debye.cl:90-101, unconjugated
 struct Voxel {
   float u;
   float2 ex, ey, ez;
 };
-template <int MIR>
-__device__ __forceinline__ Voxel assemble_point(int x, int y, int z, int nx, int ny, int nz, const OctGeom& g, int M,
-                                                int Zo, float ex0, float ey0, const float2* __restrict__ I,
-                                                const float* __restrict__ trig) {
-  int ix, jy, kz;
-  bool conj;
-  if (MIR == MIR_STD) {
-    ix = abs(x - nx / 2), jy = abs(y - ny / 2), kz = abs(z - nz / 2);
-    conj = z <= nz / 2;
-  } else {
-    ix = mirror_gauss(x, nx, g.nxo), jy = mirror_gauss(y, ny, g.nyo), kz = mirror_gauss(z, nz, g.nzo);
-    conj = false;
-  }
-  const int m = jy * g.nxo + ix;
+__device__ __forceinline__ Voxel octant_sample(int ix, int jy, int kz, int nxo, int M, int Zo, float ex0, float ey0,
+                                               const float2* __restrict__ I, const float* __restrict__ trig) {
+  const int m = jy * nxo + ix;
   const size_t ZM = (size_t)Zo * M, o = (size_t)kz * M + m;
   const float2 I0 = __ldg(I + o), I1 = __ldg(I + ZM + o), I2 = __ldg(I + 2 * ZM + o);
   const float c1 = __ldg(trig + m), s1 = __ldg(trig + M + m);
@@ -477,6 +461,27 @@ __device__ __forceinline__ Voxel assemble_point(int x, int y, int z, int nx, int
   const float pz = ex0 * c1 + ey0 * s1;
   r.ez = make_float2(2.f * I1.y * pz, -2.f * I1.x * pz);
   r.u = cabs2(r.ex) + cabs2(r.ey) + cabs2(r.ez);
+  return r;
+}
+
+// Gather form: the voxel (x, y, z) of the full volume from the octant sample it mirrors onto
+// (conjugated fields where MIR_STD asks for it)
+template <int MIR>
+__device__ __forceinline__ Voxel assemble_point(int x, int y, int z, int nx, int ny, int nz, const OctGeom& g, int M,
+                                                int Zo, float ex0, float ey0, const float2* __restrict__ I,
+                                                const float* __restrict__ trig) {
+  int ix, jy, kz;
+  bool conj;
+  if (MIR == MIR_STD) {
+    ix = abs(x - nx / 2), jy = abs(y - ny / 2), kz = abs(z - nz / 2);
+    conj = z <= nz / 2;
+  } else {
+    ix = x >= nx - g.nxo ? x - (nx - g.nxo) : g.nxo - 1 - x;
+    jy = y >= ny - g.nyo ? y - (ny - g.nyo) : g.nyo - 1 - y;
+    kz = z >= nz - g.nzo ? z - (nz - g.nzo) : g.nzo - 1 - z;
+    conj = false;
+  }
+  Voxel r = octant_sample(ix, jy, kz, g.nxo, M, Zo, ex0, ey0, I, trig);
   if (conj) {
     r.ex.y = -r.ex.y;
     r.ey.y = -r.ey.y;
@@ -485,61 +490,114 @@ __device__ __forceinline__ Voxel assemble_point(int x, int y, int z, int nx, int
   return r;
 }
 
-// full-volume assembly fused with the octant mirroring; PAIR: two neighbouring voxels per
-// thread (even nx), stored as 8- and 16-byte vectors
-template <int MIR, bool PAIR>
+// Gather assembly, two neighbouring voxels per thread (even nx) stored as 8- and 16-byte
+// vectors: the faster form when the fields are written (470 MB at 256^3), since its paired
+// stores beat the scatter form's single ones; each sample is read by every voxel mirroring
+// onto it
+template <int MIR>
 __global__ void debye_assemble_kernel(int nx, int ny, int nz, OctGeom g, int M, int Zo, float ex0, float ey0,
                                       const float2* __restrict__ I, const float* __restrict__ trig,
                                       float* __restrict__ u, float2* __restrict__ ex, float2* __restrict__ ey,
                                       float2* __restrict__ ez) {
   const int y = blockIdx.y, z = blockIdx.z;
-  if constexpr (PAIR) {
-    const int x = 2 * (blockIdx.x * blockDim.x + threadIdx.x);
-    if (x >= nx) return;
-    const Voxel a = assemble_point<MIR>(x, y, z, nx, ny, nz, g, M, Zo, ex0, ey0, I, trig);
-    const Voxel b = assemble_point<MIR>(x + 1, y, z, nx, ny, nz, g, M, Zo, ex0, ey0, I, trig);
-    const size_t v = ((size_t)z * ny + y) * nx + x;  // even: 8-byte u pairs, 16-byte field pairs
-    if (u) __stcs(reinterpret_cast<float2*>(u + v), make_float2(a.u, b.u));
-    if (ex) __stcs(reinterpret_cast<float4*>(ex + v), make_float4(a.ex.x, a.ex.y, b.ex.x, b.ex.y));
-    if (ey) __stcs(reinterpret_cast<float4*>(ey + v), make_float4(a.ey.x, a.ey.y, b.ey.x, b.ey.y));
-    if (ez) __stcs(reinterpret_cast<float4*>(ez + v), make_float4(a.ez.x, a.ez.y, b.ez.x, b.ez.y));
+  const int x = 2 * (blockIdx.x * blockDim.x + threadIdx.x);
+  if (x >= nx) return;
+  const Voxel a = assemble_point<MIR>(x, y, z, nx, ny, nz, g, M, Zo, ex0, ey0, I, trig);
+  const Voxel b = assemble_point<MIR>(x + 1, y, z, nx, ny, nz, g, M, Zo, ex0, ey0, I, trig);
+  const size_t v = ((size_t)z * ny + y) * nx + x;  // even: 8-byte u pairs, 16-byte field pairs
+  if (u) __stcs(reinterpret_cast<float2*>(u + v), make_float2(a.u, b.u));
+  if (ex) __stcs(reinterpret_cast<float4*>(ex + v), make_float4(a.ex.x, a.ex.y, b.ex.x, b.ex.y));
+  if (ey) __stcs(reinterpret_cast<float4*>(ey + v), make_float4(a.ey.x, a.ey.y, b.ey.x, b.ey.y));
+  if (ez) __stcs(reinterpret_cast<float4*>(ez + v), make_float4(a.ez.x, a.ez.y, b.ez.x, b.ez.y));
+}
+
+// The full-volume positions of octant index q along one axis of N0 points: the inverse of
+// the mirroring maps (MIR_STD: q = |p - N0/2|; MIR_GAUSS: q = p - (N0 - N) for p >= N0 - N,
+// else N - 1 - q), at most two, in p[0..n)
+template <int MIR>
+__device__ __forceinline__ int mirror_positions(int q, int N0, int N, int (&p)[2]) {
+  int n = 0;
+  if (MIR == MIR_STD) {
+    const int a = N0 / 2 + q, b = N0 / 2 - q;
+    if (a < N0) p[n++] = a;
+    if (b >= 0 && b != a) p[n++] = b;
   } else {
-    const int x = blockIdx.x * blockDim.x + threadIdx.x;
-    if (x >= nx) return;
-    const Voxel a = assemble_point<MIR>(x, y, z, nx, ny, nz, g, M, Zo, ex0, ey0, I, trig);
-    const size_t v = ((size_t)z * ny + y) * nx + x;
-    if (u) __stcs(u + v, a.u);
-    if (ex) __stcs(ex + v, a.ex);
-    if (ey) __stcs(ey + v, a.ey);
-    if (ez) __stcs(ez + v, a.ez);
+    const int a = q + (N0 - N), b = N - 1 - q;
+    if (a < N0) p[n++] = a;
+    if (b < N0 - N && b >= 0) p[n++] = b;
+  }
+  return n;
+}
+
+// Full-volume assembly fused with the octant mirroring, one octant sample per thread: the
+// fields and intensity are formed once (octant_sample) and stored to every
+// voxel that mirrors onto the sample (up to 8; conjugated fields where z <= Nz/2 for
+// MIR_STD). A warp's 32 consecutive ix store 32 consecutive x on either side of the centre,
+// so every store stays coalesced, and the integrals and azimuth tables are read once per
+// sample instead of once per voxel (an 8-fold cut of the reads, the whole cost of an
+// intensity-only call).
+template <int MIR>
+__global__ void debye_scatter_kernel(int nx, int ny, int nz, OctGeom g, int M, int Zo, float ex0, float ey0,
+                                     const float2* __restrict__ I, const float* __restrict__ trig,
+                                     float* __restrict__ u, float2* __restrict__ ex, float2* __restrict__ ey,
+                                     float2* __restrict__ ez) {
+  const int ix = blockIdx.x * blockDim.x + threadIdx.x, jy = blockIdx.y, kz = blockIdx.z;
+  if (ix >= g.nxo) return;
+  int px[2], py[2], pz[2];
+  const int nxp = mirror_positions<MIR>(ix, nx, g.nxo, px);
+  const int nyp = mirror_positions<MIR>(jy, ny, g.nyo, py);
+  const int nzp = mirror_positions<MIR>(kz, nz, g.nzo, pz);
+  if (nxp == 0 || nyp == 0 || nzp == 0) return;
+  const Voxel v = octant_sample(ix, jy, kz, g.nxo, M, Zo, ex0, ey0, I, trig);
+  for (int c = 0; c < nzp; c++) {
+    const int z = pz[c];
+    const bool cj = MIR == MIR_STD && z <= nz / 2;
+    const float2 fx = cj ? make_float2(v.ex.x, -v.ex.y) : v.ex;
+    const float2 fy = cj ? make_float2(v.ey.x, -v.ey.y) : v.ey;
+    const float2 fz = cj ? make_float2(v.ez.x, -v.ez.y) : v.ez;
+    for (int b = 0; b < nyp; b++) {
+      const size_t row = ((size_t)z * ny + py[b]) * nx;
+      for (int a = 0; a < nxp; a++) {
+        const size_t o = row + px[a];
+        if (u) __stcs(u + o, v.u);
+        if (ex) __stcs(ex + o, fx);
+        if (ey) __stcs(ey + o, fy);
+        if (ez) __stcs(ez + o, fz);
+      }
+    }
   }
 }
 
-// launch the assembly: pairs of voxels when nx is even and the outputs allow vector stores
+// launch the assembly: the paired gather form when fields are written to 16-byte aligned
+// buffers of even nx (GB300, 256^3 with all four outputs: gather 82 us against 90 us for the
+// scatter form), else one thread per octant sample (intensity only: 0.172 -> 0.151 ms for the
+// whole 256^3 PSF)
 int launch_assemble(const debye_desc* d, bool gauss, const OctGeom& g, int M, int Zo, const float2* I,
                     const float* trig, float* u, void* ex, void* ey, void* ez, cudaStream_t s) {
   float2 *pex = static_cast<float2*>(ex), *pey = static_cast<float2*>(ey), *pez = static_cast<float2*>(ez);
+  const float e0 = (float)d->ex0, e1 = (float)d->ey0;
+  const bool fields = ex || ey || ez;
   const bool pair = d->nx % 2 == 0 && ((uintptr_t)u & 7) == 0 && ((uintptr_t)ex & 15) == 0 &&
                     ((uintptr_t)ey & 15) == 0 && ((uintptr_t)ez & 15) == 0;
-  const int xs = pair ? d->nx / 2 : d->nx;
-  const dim3 grid((xs + 127) / 128, d->ny, d->nz);
-  const float e0 = (float)d->ex0, e1 = (float)d->ey0;
-  if (gauss) {
-    if (pair)
-      debye_assemble_kernel<MIR_GAUSS, true><<<grid, 128, 0, s>>>(d->nx, d->ny, d->nz, g, M, Zo, e0, e1, I, trig, u,
-                                                                   pex, pey, pez);
+  if (fields && pair) {
+    const dim3 grid((d->nx / 2 + 127) / 128, d->ny, d->nz);
+    if (gauss)
+      debye_assemble_kernel<MIR_GAUSS><<<grid, 128, 0, s>>>(d->nx, d->ny, d->nz, g, M, Zo, e0, e1, I, trig, u, pex,
+                                                            pey, pez);
     else
-      debye_assemble_kernel<MIR_GAUSS, false><<<grid, 128, 0, s>>>(d->nx, d->ny, d->nz, g, M, Zo, e0, e1, I, trig, u,
-                                                                    pex, pey, pez);
-  } else {
-    if (pair)
-      debye_assemble_kernel<MIR_STD, true><<<grid, 128, 0, s>>>(d->nx, d->ny, d->nz, g, M, Zo, e0, e1, I, trig, u,
-                                                                 pex, pey, pez);
-    else
-      debye_assemble_kernel<MIR_STD, false><<<grid, 128, 0, s>>>(d->nx, d->ny, d->nz, g, M, Zo, e0, e1, I, trig, u,
-                                                                  pex, pey, pez);
+      debye_assemble_kernel<MIR_STD><<<grid, 128, 0, s>>>(d->nx, d->ny, d->nz, g, M, Zo, e0, e1, I, trig, u, pex,
+                                                          pey, pez);
+    BPM_LAUNCH_CHECK("debye_assemble_kernel");
+    return BPM_OK;
   }
-  BPM_LAUNCH_CHECK("debye_assemble_kernel");
+  const dim3 grid((g.nxo + 127) / 128, g.nyo, g.nzo);
+  if (gauss)
+    debye_scatter_kernel<MIR_GAUSS><<<grid, 128, 0, s>>>(d->nx, d->ny, d->nz, g, M, Zo, e0, e1, I, trig, u, pex,
+                                                         pey, pez);
+  else
+    debye_scatter_kernel<MIR_STD><<<grid, 128, 0, s>>>(d->nx, d->ny, d->nz, g, M, Zo, e0, e1, I, trig, u, pex, pey,
+                                                       pez);
+  BPM_LAUNCH_CHECK("debye_scatter_kernel");
   return BPM_OK;
 }
 
