@@ -643,7 +643,8 @@ def profile_kernels():
     ncu captures: tile kernels (1024^2, 64x32), narrow single-field kernels (256^2), the
     adjoint, the scattering column pass, the mask precompute, the coated-sphere fill, the
     Debye-Wolf plane / free-point / Gaussian-pupil variants (the last through the tensor-core
-    quadrature) and the fused weighted column pass."""
+    quadrature), an intensity-only PSF (the scatter assembly) and the fused weighted column
+    pass."""
     import torch
     import bpm_gb300
     from bpm_gb300.adjoint import propagate_exit
@@ -665,6 +666,8 @@ def profile_kernels():
     pts = np.linspace(-2, 2, 4096).astype(np.float32)
     bpm_gb300.focus_field_debye_at(pts, pts[::-1].copy(), .5 * pts, LAM, 1.1, n0=N0)
     bpm_gb300.focus_field_debye_gauss((128, 128, 128), (.1, .1, .1), LAM, [0, .9])
+    # the intensity alone: the scatter form of the assembly
+    bpm_gb300.psf((128, 128, 128), (.1, .1, .1), LAM, 1.1, N0, 512)
     # the weighted column passes fused into one cluster launch per step (opt-in launch shape)
     dnw = torch.from_numpy((.02 * rng.standard_normal((6, 256, 256))).astype(np.float32)).cuda()
     bpm_gb300.bpm_3d_batched((256, 256, 6), UNITS, lam=LAM, n0=N0, u0=make_u0(4, 256, 256, 3), dn=dnw,
