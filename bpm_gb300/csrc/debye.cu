@@ -213,35 +213,6 @@ __host__ __device__ constexpr double hankel_a(int n, int k) {
   return a;
 }
 
-// J0 and J1 together. From x = 16 on, the expansion above truncated after x^-7 (its error,
-// below 2e-9 of the envelope sqrt(2 / (pi x)), is under FP32 rounding), with one sincosf of x
-// for both orders: chi_0 = x - pi/4 and chi_1 = chi_0 - pi/2, so cos chi_0 = (cos x + sin x)
-// / sqrt 2, sin chi_0 = (sin x - cos x) / sqrt 2, cos chi_1 = sin chi_0, sin chi_1 = -cos chi_0.
-// Below 16, CUDA's j0f and j1f.
-__device__ __forceinline__ void bessel_j01(float x, float& j0, float& j1) {
-  const float ax = fabsf(x);
-  if (ax < 16.f) {
-    j0 = j0f(x);
-    j1 = j1f(x);
-    return;
-  }
-  const float r = __frcp_rn(ax), y = r * r;
-  const float P0 = fmaf(fmaf(fmaf((float)-hankel_a(0, 6), y, (float)hankel_a(0, 4)), y, (float)-hankel_a(0, 2)), y, 1.f);
-  const float Q0 = r * fmaf(fmaf(fmaf((float)-hankel_a(0, 7), y, (float)hankel_a(0, 5)), y, (float)-hankel_a(0, 3)), y,
-                            (float)hankel_a(0, 1));
-  const float P1 = fmaf(fmaf(fmaf((float)-hankel_a(1, 6), y, (float)hankel_a(1, 4)), y, (float)-hankel_a(1, 2)), y, 1.f);
-  const float Q1 = r * fmaf(fmaf(fmaf((float)-hankel_a(1, 7), y, (float)hankel_a(1, 5)), y, (float)-hankel_a(1, 3)), y,
-                            (float)hankel_a(1, 1));
-  float s, c;
-  sincosf(ax, &s, &c);
-  constexpr float kInvSqrt2 = 0.70710678118654752f;
-  const float c0 = (c + s) * kInvSqrt2, s0 = (s - c) * kInvSqrt2;   // cos, sin of x - pi/4
-  const float env = sqrtf(0.63661977236758134f * r);                // sqrt(2 / (pi x))
-  j0 = env * fmaf(P0, c0, -(Q0 * s0));
-  const float j1a = env * fmaf(P1, s0, Q1 * c0);                    // P1 cos chi_1 - Q1 sin chi_1
-  j1 = x < 0.f ? -j1a : j1a;                                        // J1 is odd
-}
-
 // J2 from J0, J1: ascending series for small x, the three-term recurrence J2 = 2 J1/x - J0
 // otherwise (stable for n = 2 < x).
 __device__ __forceinline__ float bessel_j2(float x, float j0, float j1) {
@@ -261,6 +232,40 @@ __device__ __forceinline__ float bessel_j2(float x, float j0, float j1) {
   return 2.f * j1 / x - j0;
 }
 
+// J0, J1 and J2 together. From x = 16 on, the expansion above truncated after x^-7 (its
+// error, below 2e-9 of the envelope sqrt(2 / (pi x)), is under FP32 rounding), with one
+// sincosf of x for both orders: chi_0 = x - pi/4 and chi_1 = chi_0 - pi/2, so cos chi_0 =
+// (cos x + sin x) / sqrt 2, sin chi_0 = (sin x - cos x) / sqrt 2, cos chi_1 = sin chi_0,
+// sin chi_1 = -cos chi_0; 1/x and the envelope come from the approximate reciprocal and
+// reciprocal square root (2 ulp, far below what the truncated series resolves), and J2 from
+// the recurrence 2 J1/x - J0 with that reciprocal. Below 16: CUDA's j0f and j1f, J2 by
+// bessel_j2.
+__device__ __forceinline__ void bessel_j012(float x, float& j0, float& j1, float& j2) {
+  const float ax = fabsf(x);
+  if (ax < 16.f) {
+    j0 = j0f(x);
+    j1 = j1f(x);
+    j2 = bessel_j2(x, j0, j1);
+    return;
+  }
+  const float r = __fdividef(1.f, ax), y = r * r;
+  const float P0 = fmaf(fmaf(fmaf((float)-hankel_a(0, 6), y, (float)hankel_a(0, 4)), y, (float)-hankel_a(0, 2)), y, 1.f);
+  const float Q0 = r * fmaf(fmaf(fmaf((float)-hankel_a(0, 7), y, (float)hankel_a(0, 5)), y, (float)-hankel_a(0, 3)), y,
+                            (float)hankel_a(0, 1));
+  const float P1 = fmaf(fmaf(fmaf((float)-hankel_a(1, 6), y, (float)hankel_a(1, 4)), y, (float)-hankel_a(1, 2)), y, 1.f);
+  const float Q1 = r * fmaf(fmaf(fmaf((float)-hankel_a(1, 7), y, (float)hankel_a(1, 5)), y, (float)-hankel_a(1, 3)), y,
+                            (float)hankel_a(1, 1));
+  float s, c;
+  sincosf(ax, &s, &c);
+  constexpr float kInvSqrt2 = 0.70710678118654752f;
+  const float c0 = (c + s) * kInvSqrt2, s0 = (s - c) * kInvSqrt2;   // cos, sin of x - pi/4
+  const float env = 0.79788456080286536f * rsqrtf(ax);              // sqrt(2 / (pi x))
+  j0 = env * fmaf(P0, c0, -(Q0 * s0));
+  const float j1a = env * fmaf(P1, s0, Q1 * c0);                    // P1 cos chi_1 - Q1 sin chi_1
+  j1 = x < 0.f ? -j1a : j1a;                                        // J1 is odd
+  j2 = fmaf(2.f * r, j1a, -j0);                                     // J2 is even
+}
+
 // A_n(t, m) = p_n(t) J_n(kr_m sin t_t)
 __global__ void debye_bessel_kernel(int T, int M, int Mp, const double* si, const double* kr, const float* wf,
                                     float* J) {
@@ -274,8 +279,8 @@ __global__ void debye_bessel_kernel(int T, int M, int Mp, const double* si, cons
   }
   const float x = (float)(kr[m] * si[t]);
   float j0, j1;
-  bessel_j01(x, j0, j1);
-  const float j2 = bessel_j2(x, j0, j1);
+  float j2;
+  bessel_j012(x, j0, j1, j2);
   J[o] = wf[t] * j0;
   J[TM + o] = wf[T + t] * j1;
   J[2 * TM + o] = wf[2 * T + t] * j2;
@@ -664,8 +669,8 @@ __global__ void __launch_bounds__(PT_THREADS) debye_points_kernel(
     for (int tt = 0; tt < nt; tt++) {
       const float xb = kr * s_si[tt];
       float j0, j1;
-      bessel_j01(xb, j0, j1);
-      const float j2 = bessel_j2(xb, j0, j1);
+      float j2;
+      bessel_j012(xb, j0, j1, j2);
       float2 e;
       if (GRID) {
         e = s_E[tt];
@@ -766,21 +771,21 @@ __global__ void debye_setup_tc_kernel(NodeArgs a, OctGeom g, double k, int T, in
   }
 }
 
-// The operand tables of the product in one launch of 128-thread blocks, each over 128 nodes
-// (tb blocks per row):
-//   blocks [0, nph): Bh/Bl(2z + {0, 1}, t) = high/low parts of (cos, sin)(kz_z cos t), the
-//     phase formed and reduced modulo 2 pi in FP64, its sine and cosine in FP32;
-//   the rest: A(n Mr + r, t) = p_n(t) J_n(kr sin t) (debye_bessel_kernel's values, x = kr sin t
-//     rounded to FP32 from the pair product).
-__global__ void debye_tables_tc_kernel(int T, int Tp, int Mr, int nxo, int sym, int Zo, int nph, float z1, float z2,
-                                       double k, const double* __restrict__ ct, const float2* __restrict__ si2,
+// The operand tables of the product in one launch of 128-thread blocks: block (row, chunk)
+// takes nodes chunk*128 .. +127 of one row,
+//   rows [0, Zo): Bh/Bl(2z + {0, 1}, t) = high/low parts of (cos, sin)(kz_z cos t), the phase
+//     formed and reduced modulo 2 pi in FP64, its sine and cosine in FP32;
+//   rows Zo + r: A(n Mr + r, t) = p_n(t) J_n(kr sin t) for n = 0, 1, 2 (debye_bessel_kernel's
+//     values, x = kr sin t rounded to FP32 from the pair product).
+__global__ void debye_tables_tc_kernel(int T, int Tp, int Mr, int nxo, int sym, int Zo, float z1, float z2, double k,
+                                       const double* __restrict__ ct, const float2* __restrict__ si2,
                                        const float2* __restrict__ kr2, const float* __restrict__ wf,
                                        float* __restrict__ A, float* __restrict__ Bh, float* __restrict__ Bl) {
-  const int tb = (T + 127) / 128;
-  if ((int)blockIdx.x < nph) {
-    const int z = blockIdx.x / tb;
-    const int t = (blockIdx.x - z * tb) * 128 + threadIdx.x;
-    if (t >= T) return;
+  const int row = blockIdx.x;
+  const int t = blockIdx.y * 128 + threadIdx.x;
+  if (t >= T) return;
+  if (row < Zo) {
+    const int z = row;
     const double kz = k * (double)(Zo == 1 ? z1 : coord_f32(z, z1, z2, Zo));
     const double arg = kz * ct[t];
     const double q = rint(arg * kInvTwoPi);
@@ -793,15 +798,11 @@ __global__ void debye_tables_tc_kernel(int T, int Tp, int Mr, int nxo, int sym, 
     Bl[o + Tp] = sn - tf32_hi(sn);
     return;
   }
-  const int b = blockIdx.x - nph;
-  const int r = b / tb;
-  const int t = (b - r * tb) * 128 + threadIdx.x;
-  if (t >= T) return;
+  const int r = row - Zo;
   const int m = radius_column(r, nxo, sym != 0);
   const float x = mul_pair(kr2[m], si2[t]);
-  float j0, j1;
-  bessel_j01(x, j0, j1);
-  const float j2 = bessel_j2(x, j0, j1);
+  float j0, j1, j2;
+  bessel_j012(x, j0, j1, j2);
   const size_t o = (size_t)r * Tp + t, RT = (size_t)Mr * Tp;
   A[o] = wf[t] * j0;
   A[RT + o] = wf[T + t] * j1;
@@ -1240,9 +1241,8 @@ int run_octant_tc(const debye_desc* d, bool gauss, double sig, float* u, void* e
   debye_setup_tc_kernel<<<(unsigned)(nbn + (L.M + 31) / 32), 32, 0, s>>>(na, g, k, L.T, L.M, nbn, ct, wf, si2, kr2,
                                                                           trig);
   BPM_LAUNCH_CHECK("debye_setup_tc_kernel");
-  const int nph = tb * L.Zo;
-  debye_tables_tc_kernel<<<(unsigned)(nph + (size_t)tb * L.Mr), 128, 0, s>>>(
-      L.T, L.Tp, L.Mr, L.nxo, L.sym ? 1 : 0, L.Zo, nph, g.z1, g.z2, k, ct, si2, kr2, wf, A, Bh, Bl);
+  debye_tables_tc_kernel<<<dim3((unsigned)(L.Zo + L.Mr), (unsigned)tb), 128, 0, s>>>(
+      L.T, L.Tp, L.Mr, L.nxo, L.sym ? 1 : 0, L.Zo, g.z1, g.z2, k, ct, si2, kr2, wf, A, Bh, Bl);
   BPM_LAUNCH_CHECK("debye_tables_tc_kernel");
   TcArgs ta;
   ta.T = L.T;
