@@ -49,7 +49,8 @@ class Request(ctypes.Structure):
                 ("last_plane", c_vp), ("scatter_p", c_vp), ("scatter_g", c_vp),
                 ("scattering_plane_ind", c_int), ("group", c_int),
                 ("ckpt", c_vp), ("ckpt_every", c_int), ("mask", c_vp),
-                ("conc", c_int), ("col_block", c_int), ("cluster", c_int), ("col_fuse", c_int)]
+                ("conc", c_int), ("col_block", c_int), ("cluster", c_int), ("col_fuse", c_int),
+                ("grad_sum", c_int)]
 
 
 class DebyeDesc(ctypes.Structure):

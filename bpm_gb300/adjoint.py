@@ -15,7 +15,7 @@ import ctypes
 import torch
 
 from . import _native as N
-from .bpm3d import _ptr, _stream_ptr, get_plan
+from .bpm3d import _ptr, _stream_ptr, get_plan, mask_pays, precompute_mask
 
 __all__ = ["propagate_exit"]
 
@@ -34,13 +34,19 @@ class _ExitMarch(torch.autograd.Function):
         last = torch.empty((B, Ny, Nx), dtype=torch.complex64, device=dev)
         kind = N.DN_F32 if dnc is not None else N.DN_NONE
         bstride = Nz * Ny * Nx if (dnc is not None and dnc.dim() == 4) else 0
+        # the phase masks of a shared dn, formed once for the forward march and its adjoint
+        # (the same bits as forming them per element)
+        mask = precompute_mask(plan, dnc, kind) if (dnc is not None and bstride == 0 and mask_pays(B, Nx, Ny)) \
+            else None
         req = N.Request(B, _ptr(u0c), _ptr(dnc), kind, bstride, None, None, None, N.OUT_NONE, 0,
-                        _ptr(last), None, None, 0, int(group), _ptr(ckpt), int(ckpt_every))
+                        _ptr(last), None, None, 0, int(group), _ptr(ckpt), int(ckpt_every), _ptr(mask))
         wsb = plan.workspace_bytes(B, group)
         ws = torch.empty(wsb, dtype=torch.uint8, device=dev)
         N.check(N.lib().bpm_propagate(plan.handle, ctypes.byref(req), _ptr(ws), wsb, _stream_ptr()),
                 "bpm_propagate")
-        ctx.save_for_backward(u0c, dnc if dnc is not None else torch.empty(0, device=dev), ckpt)
+        ctx.save_for_backward(u0c, dnc if dnc is not None else torch.empty(0, device=dev), ckpt,
+                              mask if mask is not None else torch.empty(0, device=dev))
+        ctx.has_mask = mask is not None
         ctx.plan = plan
         ctx.k = ckpt_every
         ctx.group = group
@@ -51,7 +57,7 @@ class _ExitMarch(torch.autograd.Function):
 
     @staticmethod
     def backward(ctx, grad_last):
-        u0c, dnc, ckpt = ctx.saved_tensors
+        u0c, dnc, ckpt, mask = ctx.saved_tensors
         plan = ctx.plan
         B, Ny, Nx = u0c.shape
         Nz = plan.size[2]
@@ -59,8 +65,18 @@ class _ExitMarch(torch.autograd.Function):
         g = grad_last.to(torch.complex64).contiguous()
         kind = N.DN_F32 if ctx.has_dn else N.DN_NONE
         req = N.Request(B, _ptr(u0c), _ptr(dnc) if ctx.has_dn else None, kind, ctx.bstride, None, None,
-                        None, N.OUT_NONE, 0, None, None, None, 0, int(ctx.group), _ptr(ckpt), int(ctx.k))
-        grad_dn = torch.zeros((B, Nz, Ny, Nx), dtype=torch.float32, device=dev) if ctx.has_dn else None
+                        None, N.OUT_NONE, 0, None, None, None, 0, int(ctx.group), _ptr(ckpt), int(ctx.k),
+                        _ptr(mask) if ctx.has_mask else None)
+        # a shared dn: the library sums the gradient over the fields (fixed order), so only
+        # one (Nz, Ny, Nx) volume is written; plane 0 (u0, which dn does not reach) stays zero
+        shared = ctx.has_dn and not ctx.bstride and 128 <= Nx <= 1024 and dnc.data_ptr() % 16 == 0
+        req.grad_sum = 1 if shared else 0
+        grad_dn = None
+        if shared:
+            grad_dn = torch.empty((Nz, Ny, Nx), dtype=torch.float32, device=dev)
+            grad_dn[0].zero_()
+        elif ctx.has_dn:
+            grad_dn = torch.zeros((B, Nz, Ny, Nx), dtype=torch.float32, device=dev)
         grad_u0 = torch.empty((B, Ny, Nx), dtype=torch.complex64, device=dev) if ctx.needs_input_grad[1] else None
         wsb = int(N.lib().bpm_backward_workspace_bytes(plan.handle, B, int(ctx.group), int(ctx.k)))
         ws = torch.empty(wsb, dtype=torch.uint8, device=dev)
@@ -68,7 +84,7 @@ class _ExitMarch(torch.autograd.Function):
                                      _ptr(ws), wsb, _stream_ptr()), "bpm_backward")
         gdn = None
         if ctx.has_dn and ctx.needs_input_grad[0]:
-            gdn = grad_dn if ctx.bstride else grad_dn.sum(dim=0)
+            gdn = grad_dn if (shared or ctx.bstride) else grad_dn.sum(dim=0)
             gdn = gdn.to(ctx.dn_dtype)
         return gdn, grad_u0, None, None, None
 

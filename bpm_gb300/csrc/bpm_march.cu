@@ -208,6 +208,14 @@ struct RowParams {
   float* grad_dn;           // group's (nz, ny, nx) dn gradients
   float2* grad_u0;          // group's (ny, nx) u0 gradients or NULL
   const float2* mask;       // precomputed masks of the shared dn, (nz, ny, nx), or NULL
+  // adjoint with the dn gradient summed over the fields (row_adj_shared_kernel, grad_sum 1):
+  // block 0 of a row writes its fields' sum to grad_dn, block b >= 1 to grad_part + (b - 1) *
+  // grad_part_stride, stored (grad_acc 0, the first group of the request) or added (grad_acc
+  // 1, the later groups)
+  int grad_sum;
+  float* grad_part;
+  long long grad_part_stride;
+  int grad_acc;
 };
 
 __device__ __forceinline__ float load_dn_real(const void* dn, int dtype, size_t idx) {
@@ -680,6 +688,11 @@ struct WarpCfg {
   }
   static constexpr size_t ROW_SMEM = row_smem(kRowWarps);
   static constexpr size_t ROW_SMEM_SHARED = ROW_SMEM + (size_t)N * sizeof(float2);  // + the staged row
+  // row_adj_shared_kernel with `slots` sequences: + a forward-field row and a row of
+  // gradient terms per sequence
+  static constexpr size_t adj_smem(int slots) {
+    return row_smem(slots) + (size_t)N * sizeof(float2) + (size_t)slots * N * (sizeof(float2) + sizeof(float));
+  }
 };
 
 // blocks per SM a row kernel of RW sequences of L lanes must fit: 32 values per lane need
@@ -826,8 +839,102 @@ row_shared_kernel(RowParams p, int nfields, int fw_rt) {
   for (int m = 0; m < E; m++) dst[t + L * m] = v[m];
 }
 
+// Adjoint row pass for fields sharing one dn with the dn gradient summed over them (plane z
+// >= 1, do_mask): block (y, b) takes row y of fields fw*b .. fw*b + fw-1, one warp each (fw <=
+// 8). At block start cp.async stages the slice-z mask row (precomputed mask, or dn row) and
+// every warp's row of the forward field at plane z (from the recomputed segment), so their
+// reads overlap the inverse row FFT (the per-element reads of row_warp_kernel follow it);
+// each warp leaves its gradient terms k0 dz Im(conj(G) u) in shared memory, and the block adds
+// them over its fields in warp order, so the sum is the same in every run. The arithmetic per
+// element is row_point's.
+template <int N, int PRE, int L = 32>
+__global__ void __launch_bounds__(kRowWarps * 32, 2)
+row_adj_shared_kernel(RowParams p, int nfields, int fw) {
+  constexpr int E = N / L;
+  const int T = blockDim.x;
+  const int slots = T / L;
+  extern __shared__ __align__(16) float2 smem[];
+  float2* tw = smem;
+  const int seq = threadIdx.x / L, t = threadIdx.x % L;
+  float2* buf = smem + N + seq * WarpFft<N, L>::BUF;
+  float2* mrow = smem + N + slots * WarpFft<N, L>::BUF;  // N float2: the staged mask or dn row
+  float2* srow = mrow + N;                                // slots x N float2: forward-field rows
+  float* grow = reinterpret_cast<float*>(srow + (size_t)slots * N);  // slots x N gradient terms
+  const int y = blockIdx.x;
+  const int gl = blockIdx.y * fw + seq;
+  const bool active = seq < fw && gl < nfields;
+  const size_t plane = (size_t)N * p.ny;
+  const size_t zoff = (size_t)p.z * plane;
+  for (int k = threadIdx.x; k < WarpFft<N, L>::TW; k += T) tw[k] = p.wtw[k];  // plan constant
+  dep_wait();
+  dep_release();
+  {
+    const int es = PRE ? 8 : (p.dn_dtype == BPM_DN_F16 ? 2 : 4);
+    const char* srcm = PRE ? reinterpret_cast<const char*>(p.mask + zoff + (size_t)y * N)
+                           : static_cast<const char*>(p.dn) + (zoff + (size_t)y * N) * es;
+    char* dstm = reinterpret_cast<char*>(mrow);
+    for (int o = threadIdx.x * 16; o < N * es; o += T * 16) cp_async16(dstm + o, srcm + o);
+    if (active) {
+      const char* srcs = reinterpret_cast<const char*>(p.seg + gl * p.seg_bstride +
+                                                       (size_t)(p.z - p.seg_z0) * plane + (size_t)y * N);
+      char* dsts = reinterpret_cast<char*>(srow + (size_t)seq * N);
+      for (int o = t * 16; o < N * 8; o += L * 16) cp_async16(dsts + o, srcs + o);
+    }
+    cp_async_commit();
+  }
+  float2 v[E];
+  if (active) {
+    const float2* src = p.src + gl * p.src_bstride + (size_t)y * N;
+#pragma unroll
+    for (int m = 0; m < E; m++) v[m] = src[t + L * m];
+  }
+  __syncthreads();
+  if (active && p.do_inv) warp_fft<N, true, L>(v, buf, tw, t);
+  cp_async_wait<0>();
+  __syncthreads();  // the staged rows are visible to every warp
+  if (active) {
+    const float2* us = srow + (size_t)seq * N;
+    float* gw = grow + (size_t)seq * N;
+#pragma unroll
+    for (int m = 0; m < E; m++) {
+      const int x = t + L * m;
+      const float2 u = us[x];
+      gw[x] = p.unit_k * fmaf(v[m].x, u.y, -(v[m].y * u.x));
+      const float2 M = staged_mask<PRE>(p, mrow, x, y);
+      v[m] = cmul(v[m], make_float2(M.x, -M.y));
+    }
+  }
+  __syncthreads();  // every warp's gradient terms are in shared memory
+  {
+    const int nf = min(fw, nfields - (int)blockIdx.y * fw);
+    float* gp = (blockIdx.y == 0 ? p.grad_dn : p.grad_part + (size_t)(blockIdx.y - 1) * p.grad_part_stride) + zoff +
+                (size_t)y * N;
+    for (int x = threadIdx.x; x < N; x += T) {
+      float sacc = grow[x];
+      for (int w = 1; w < nf; w++) sacc += grow[(size_t)w * N + x];
+      gp[x] = p.grad_acc ? gp[x] + sacc : sacc;
+    }
+  }
+  if (!active || !p.do_fwd) return;
+  warp_fft<N, false, L>(v, buf, tw, t);
+  float2* dst = p.W + gl * plane + (size_t)y * N;
+#pragma unroll
+  for (int m = 0; m < E; m++) dst[t + L * m] = v[m];
+}
+
+// Sum of the adjoint's per-block gradient partials: grad += part[1] + part[2] + ... in block
+// order (part[0] is grad itself), planes 1 .. nz-1
+__global__ void grad_parts_sum_kernel(float* grad, const float* part, long long stride, int nparts, size_t n0,
+                                      size_t n) {
+  const size_t i = n0 + (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  float sacc = grad[i];
+  for (int b = 1; b < nparts; b++) sacc += part[(size_t)(b - 1) * stride + i];
+  grad[i] = sacc;
+}
+
 // Column pass without the tile transposition (128 <= N <= 1024, with or without scattering sums). The
-// block's 32*C threads load C columns (16, or 8 for small non-weighted passes) in the
+// block's 32*C threads load C columns (16, or 8 or 4 for small non-weighted passes) in the
 // coalesced tile mapping — thread (r0, cc) = (tid / C, tid % C) holds rows r0 + 32 i of column
 // x0 + cc — and keep that mapping for every pointwise step (the propagator from the
 // row-major table or the FP32 recipe, the weighted partial sums, the loads and stores); the
@@ -1584,6 +1691,10 @@ struct RowK {
   template <int L>
   static void prepare_l() {
     using W = WarpCfg<N, L>;
+    cudaFuncSetAttribute(row_adj_shared_kernel<N, 0, L>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                         (int)W::adj_smem(kRowWarps));
+    cudaFuncSetAttribute(row_adj_shared_kernel<N, 1, L>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                         (int)W::adj_smem(kRowWarps));
     cudaFuncSetAttribute(row_shared_kernel<N, 0, L>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                          (int)W::ROW_SMEM_SHARED);
     cudaFuncSetAttribute(row_shared_kernel<N, 1, L>, cudaFuncAttributeMaxDynamicSharedMemorySize,
@@ -1651,6 +1762,17 @@ struct RowK {
       // by cp.async at block start, so the row's DRAM read overlaps the inverse row FFT
       // instead of following it as in row_warp_kernel (GB300, one field, Nz 128, same bits:
       // 1024^2 ignore 3.63 -> 2.55 ms, 512^2 2.04 -> 1.14 ms, 512^2 weighted 3.00 -> 2.05 ms)
+      if (adj && p.grad_sum && p.do_mask && p.z > 0 && (p.mask ? aligned16(p.mask) : aligned16(p.dn))) {
+        // the dn gradient summed over the group's fields, a block per row and up to 8 fields
+        const int nb = ((int)g.y + kRowWarps - 1) / kRowWarps;
+        const int fw = ((int)g.y + nb - 1) / nb;
+        const int threads = (fw * L + 31) / 32 * 32;
+        const size_t sm = WarpCfg<N, L>::adj_smem(threads / L);
+        auto fn = p.mask ? row_adj_shared_kernel<N, 1, L> : row_adj_shared_kernel<N, 0, L>;
+        BPM_CUDA_TRY(launch_dep(fn, dim3(p.ny, nb), dim3(threads), sm, s, p, (int)g.y, fw));
+        BPM_LAUNCH_CHECK("row_adj_shared_kernel");
+        return BPM_OK;
+      }
       if (!adj && shared_ok(p, (int)g.y)) {
         // fields per block: the group split evenly over ceil(G / 8) blocks per row
         const int nb = ((int)g.y + kRowWarps - 1) / kRowWarps;
@@ -2334,8 +2456,12 @@ int enqueue_march(bpm_plan* pl, const bpm_request* r, void* ws, size_t ws_bytes,
 // adjoint march
 // ---------------------------------------------------------------------------------------
 struct BwLayout {
-  size_t fwd, adj, seg, total;
+  size_t fwd, adj, seg, part, total;
 };
+
+// gradient partial volumes of a summed-gradient adjoint (grad_sum): one per row block past
+// the first, ceil(G / 8) blocks per row
+inline int bw_grad_parts(int G) { return (G + kRowWarps - 1) / kRowWarps - 1; }
 
 BwLayout bw_layout(const bpm_plan* pl, int G, int k) {
   BwLayout L;
@@ -2347,6 +2473,8 @@ BwLayout bw_layout(const bpm_plan* pl, int G, int k) {
   off += ws_layout(pl, G).total;
   L.seg = off;
   off += align256((size_t)G * (k + 1) * plane * sizeof(float2));
+  L.part = off;
+  off += align256((size_t)bw_grad_parts(G) * pl->d.nz * plane * sizeof(float));
   L.total = off;
   return L;
 }
@@ -2369,6 +2497,17 @@ int check_backward(const bpm_plan* pl, const bpm_request* r, const void* grad_la
     set_error("grad_dn must be a 16-byte aligned pointer");
     return BPM_ERR_ARG;
   }
+  if (r->grad_sum != 0 && r->grad_sum != 1) { set_error("grad_sum must be 0 or 1"); return BPM_ERR_ARG; }
+  if (r->grad_sum && (r->dn_dtype == BPM_DN_NONE || r->dn_batch_stride != 0)) {
+    set_error("grad_sum needs one dn volume shared by the fields (dn_batch_stride 0)");
+    return BPM_ERR_ARG;
+  }
+  // the summed gradient comes from row_adj_shared_kernel: warp-FFT rows, staged 16-byte rows
+  if (r->grad_sum && (pl->d.nx < 128 || pl->d.nx > 1024 || (pl->d.nx == 1024 && !warp1024_enabled()) ||
+                      !aligned16(r->dn) || (r->mask && !aligned16(r->mask)))) {
+    set_error("grad_sum needs 128 <= nx <= 1024 (warp-FFT rows) and 16-byte aligned dn and mask");
+    return BPM_ERR_ARG;
+  }
   return BPM_OK;
 }
 
@@ -2387,6 +2526,8 @@ int enqueue_backward(bpm_plan* pl, const bpm_request* r, const void* grad_last, 
   const int n_ckpt = (nz - 1) / k + 1;
   const int nseg = (nz - 1 + k - 1) / k;  // segments (s*k, min(s*k+k, nz-1)]
   float2* seg = reinterpret_cast<float2*>(wsb + L.seg);
+  float* part = reinterpret_cast<float*>(wsb + L.part);
+  const bool gsum = r->grad_sum && grad_dn;
   int rc;
   for (int b0 = 0; b0 < r->batch; b0 += G) {
     const int Gc = std::min(G, r->batch - b0);
@@ -2408,7 +2549,11 @@ int enqueue_backward(bpm_plan* pl, const bpm_request* r, const void* grad_last, 
     ca.rp.scat_p = ca.rp.scat_g = nullptr;
     ca.rp.seg = seg;
     ca.rp.seg_bstride = (long long)(k + 1) * plane;
-    ca.rp.grad_dn = grad_dn ? grad_dn + (size_t)b0 * nz * plane : nullptr;
+    ca.rp.grad_dn = grad_dn ? (gsum ? grad_dn : grad_dn + (size_t)b0 * nz * plane) : nullptr;
+    ca.rp.grad_sum = gsum ? 1 : 0;
+    ca.rp.grad_part = part;
+    ca.rp.grad_part_stride = (long long)nz * plane;
+    ca.rp.grad_acc = b0 > 0 ? 1 : 0;
     ca.rp.grad_u0 = grad_u0 ? static_cast<float2*>(grad_u0) + (size_t)b0 * plane : nullptr;
     ca.cp.scat = 0;
     ca.cp.conj_h = 1;
@@ -2469,6 +2614,14 @@ int enqueue_backward(bpm_plan* pl, const bpm_request* r, const void* grad_last, 
       ra.do_inv = 1;
     }
     if ((rc = launch_row(d.nx, ca.grow, s, ra, true))) return rc;
+  }
+  const int nparts = bw_grad_parts(G) + 1;
+  if (gsum && nparts > 1 && nz > 1) {
+    // the row blocks' partial sums, added in block order (planes 1 .. nz-1)
+    const size_t n0 = plane, n = (size_t)nz * plane;
+    grad_parts_sum_kernel<<<(unsigned)((n - n0 + 255) / 256), 256, 0, s>>>(grad_dn, part, (long long)nz * plane,
+                                                                           nparts, n0, n);
+    BPM_LAUNCH_CHECK("grad_parts_sum_kernel");
   }
   return BPM_OK;
 }

@@ -116,6 +116,9 @@ typedef struct {
                                     blocks, propagator, inverse FFT) where ny <= 512, nx <= 512
                                     and no scattering sums; 0 or 2 = the two column passes (the
                                     default; same bits either way)                               */
+  int grad_sum;                  /* bpm_backward only: 1 = the fields share one dn volume
+                                    (dn_batch_stride 0) and grad_dn is (nz, ny, nx), the dn
+                                    gradient summed over the request's fields; 0 = per field   */
 } bpm_request;
 
 /* Library version (BPM_GB300_VERSION). */
@@ -249,7 +252,9 @@ size_t bpm_backward_workspace_bytes(const bpm_plan* plan, int batch, int group, 
  * grad_last = dL/dRe(u_last) + i dL/dIm(u_last) for the exit planes, (batch, ny, nx)
  * complex64, write the gradient of L with respect to each field's dn into grad_dn
  * (batch, nz, ny, nx) float32 (plane z >= 1 written; plane 0 left untouched: plane 0 of
- * the march is u0, which dn does not reach) and, if grad_u0 is not NULL, the gradient
+ * the march is u0, which dn does not reach) -- or, with req->grad_sum = 1 and one shared
+ * dn, the gradient with respect to that dn, summed over the fields in a fixed order, into
+ * grad_dn (nz, ny, nx) -- and, if grad_u0 is not NULL, the gradient
  * with respect to u0 into grad_u0 (batch, ny, nx) complex64. The request must be the one
  * the forward bpm_propagate ran with, including its checkpoints (req->ckpt,
  * req->ckpt_every): each segment between checkpoints is recomputed forward, then marched

@@ -153,3 +153,31 @@ def test_config4_inversion_gradient(torch_bpm):
     err = rel_l2(dn.grad.cpu().numpy(), dn64.grad.cpu().numpy())
     print("config 4 gradient at 0.5 dn_true: rel-L2 %.3e against FP64 autograd" % err)
     assert err < 1e-4, err
+
+
+@pytest.mark.parametrize("group", [0, 5, 12])
+def test_summed_gradient_matches_per_field_sum(torch_bpm, group):
+    """Fields sharing one dn: the library sums the dn gradient over them (bpm_request.grad_sum,
+    row_adj_shared_kernel, per-block partials added in block order when a group spans more
+    than 8 fields). Same result as the per-field gradients summed (a per-field dn volume per
+    field), to FP32 rounding, and bit-identical from run to run; groups of 5 (three
+    sequential groups added in order) and of 12 (two row blocks per row)."""
+    torch, bpm, propagate_exit = torch_bpm
+    size, units, lam, n0 = (256, 128, 12), (.1, .1, .1), .5, 1.33
+    Nx, Ny, Nz = size
+    B = 12
+    u0 = torch.as_tensor(tilted_waves(B, Nx, Ny, .1, lam, .6, 21), device="cuda")
+    dn0 = torch.tensor(spheres(Nx, Ny, Nz, 3, 22), dtype=torch.float32, device="cuda")
+    I_t = torch.as_tensor(np.random.default_rng(1).uniform(.5, 1.5, (B, Ny, Nx)), device="cuda")
+
+    def grad_of(dn):
+        d = dn.clone().requires_grad_(True)
+        out = propagate_exit(d, u0, size, units, lam, n0, ckpt_every=4, group=group)
+        ((out.abs() ** 2 - I_t) ** 2).sum().backward()
+        return d.grad
+
+    g1, g2 = grad_of(dn0), grad_of(dn0)
+    assert torch.equal(g1, g2)
+    per_field = grad_of(dn0.expand(B, Nz, Ny, Nx).contiguous()).double().sum(dim=0)
+    assert torch.all(g1[0] == 0)
+    assert rel_l2(g1.double().cpu().numpy(), per_field.cpu().numpy()) < 1e-6
