@@ -15,7 +15,7 @@ import ctypes
 import torch
 
 from . import _native as N
-from .bpm3d import _ptr, _stream_ptr, get_plan, mask_pays, precompute_mask
+from .bpm3d import _apply_launch, _ptr, _stream_ptr, get_plan, mask_pays, precompute_mask
 
 __all__ = ["propagate_exit"]
 
@@ -23,7 +23,7 @@ __all__ = ["propagate_exit"]
 class _ExitMarch(torch.autograd.Function):
 
     @staticmethod
-    def forward(ctx, dn, u0, plan, ckpt_every, group):
+    def forward(ctx, dn, u0, plan, ckpt_every, group, launch):
         B, Ny, Nx = u0.shape
         Nz = plan.size[2]
         dev = u0.device
@@ -40,6 +40,7 @@ class _ExitMarch(torch.autograd.Function):
             else None
         req = N.Request(B, _ptr(u0c), _ptr(dnc), kind, bstride, None, None, None, N.OUT_NONE, 0,
                         _ptr(last), None, None, 0, int(group), _ptr(ckpt), int(ckpt_every), _ptr(mask))
+        _apply_launch(req, launch)
         wsb = plan.workspace_bytes(B, group)
         ws = torch.empty(wsb, dtype=torch.uint8, device=dev)
         N.check(N.lib().bpm_propagate(plan.handle, ctypes.byref(req), _ptr(ws), wsb, _stream_ptr()),
@@ -50,6 +51,7 @@ class _ExitMarch(torch.autograd.Function):
         ctx.plan = plan
         ctx.k = ckpt_every
         ctx.group = group
+        ctx.launch = launch
         ctx.has_dn = dnc is not None
         ctx.bstride = bstride
         ctx.dn_dtype = dn.dtype if dn is not None else None
@@ -67,6 +69,7 @@ class _ExitMarch(torch.autograd.Function):
         req = N.Request(B, _ptr(u0c), _ptr(dnc) if ctx.has_dn else None, kind, ctx.bstride, None, None,
                         None, N.OUT_NONE, 0, None, None, None, 0, int(ctx.group), _ptr(ckpt), int(ctx.k),
                         _ptr(mask) if ctx.has_mask else None)
+        _apply_launch(req, ctx.launch)
         # a shared dn: the library sums the gradient over the fields (fixed order), so only
         # one (Nz, Ny, Nx) volume is written; plane 0 (u0, which dn does not reach) stays zero
         shared = ctx.has_dn and not ctx.bstride and 128 <= Nx <= 1024 and dnc.data_ptr() % 16 == 0
@@ -86,15 +89,17 @@ class _ExitMarch(torch.autograd.Function):
         if ctx.has_dn and ctx.needs_input_grad[0]:
             gdn = grad_dn if (shared or ctx.bstride) else grad_dn.sum(dim=0)
             gdn = gdn.to(ctx.dn_dtype)
-        return gdn, grad_u0, None, None, None
+        return gdn, grad_u0, None, None, None, None
 
 
 def propagate_exit(dn, u0, size, units, lam=.5, n0=1., absorbing_width=0, ckpt_every=16,
-                   prop="functional", group=0):
+                   prop="functional", group=0, launch=None):
     """Exit planes (B, Ny, Nx) complex64 of the fields u0 (B, Ny, Nx) marched through dn
     (Nz, Ny, Nx) real, shared by all fields, or (B, Nz, Ny, Nx) per field. Differentiable
     in dn and u0 (torch autograd). prop = "functional" (bpm_3d, mean_mode="ignore") or
-    "class" (Bpm3d's FP64 propagator)."""
+    "class" (Bpm3d's FP64 propagator). group and launch (keys conc, col_block; see
+    bpm_gb300.autotune) set the launch shape of the forward and adjoint marches; they
+    change no result."""
     kind = {"functional": N.PROP_FUNCTIONAL, "class": N.PROP_CLASS}[prop]
     plan = get_plan(size, units, lam, n0, absorbing_width, "ignore", kind)
     if u0.dim() == 2:
@@ -106,4 +111,4 @@ def propagate_exit(dn, u0, size, units, lam=.5, n0=1., absorbing_width=0, ckpt_e
         raise ValueError("dn must have shape (..., %d, %d, %d)" % (Nz, Ny, Nx))
     if dn is not None and dn.is_complex():
         raise NotImplementedError("the adjoint needs real dn")
-    return _ExitMarch.apply(dn, u0, plan, int(ckpt_every), int(group))
+    return _ExitMarch.apply(dn, u0, plan, int(ckpt_every), int(group), dict(launch or {}))
