@@ -541,7 +541,7 @@ __device__ __forceinline__ int mirror_positions(int q, int N0, int N, int (&p)[2
 // so every store stays coalesced, and the integrals and azimuth tables are read once per
 // sample instead of once per voxel (an 8-fold cut of the reads, the whole cost of an
 // intensity-only call).
-template <int MIR>
+template <int MIR, bool FIELDS>
 __global__ void debye_scatter_kernel(int nx, int ny, int nz, OctGeom g, int M, int Zo, float ex0, float ey0,
                                      const float2* __restrict__ I, const float* __restrict__ trig,
                                      float* __restrict__ u, float2* __restrict__ ex, float2* __restrict__ ey,
@@ -554,20 +554,31 @@ __global__ void debye_scatter_kernel(int nx, int ny, int nz, OctGeom g, int M, i
   const int nzp = mirror_positions<MIR>(kz, nz, g.nzo, pz);
   if (nxp == 0 || nyp == 0 || nzp == 0) return;
   const Voxel v = octant_sample(ix, jy, kz, g.nxo, M, Zo, ex0, ey0, I, trig);
-  for (int c = 0; c < nzp; c++) {
+#pragma unroll
+  for (int c = 0; c < 2; c++) {
+    if (c >= nzp) break;
     const int z = pz[c];
-    const bool cj = MIR == MIR_STD && z <= nz / 2;
-    const float2 fx = cj ? make_float2(v.ex.x, -v.ex.y) : v.ex;
-    const float2 fy = cj ? make_float2(v.ey.x, -v.ey.y) : v.ey;
-    const float2 fz = cj ? make_float2(v.ez.x, -v.ez.y) : v.ez;
-    for (int b = 0; b < nyp; b++) {
-      const size_t row = ((size_t)z * ny + py[b]) * nx;
-      for (int a = 0; a < nxp; a++) {
+    const size_t zb = (size_t)z * ny;
+    float2 fx = v.ex, fy = v.ey, fz = v.ez;
+    if (FIELDS && MIR == MIR_STD && z <= nz / 2) {
+      fx.y = -fx.y;
+      fy.y = -fy.y;
+      fz.y = -fz.y;
+    }
+#pragma unroll
+    for (int b = 0; b < 2; b++) {
+      if (b >= nyp) break;
+      const size_t row = (zb + py[b]) * nx;
+#pragma unroll
+      for (int a = 0; a < 2; a++) {
+        if (a >= nxp) break;
         const size_t o = row + px[a];
         if (u) __stcs(u + o, v.u);
-        if (ex) __stcs(ex + o, fx);
-        if (ey) __stcs(ey + o, fy);
-        if (ez) __stcs(ez + o, fz);
+        if (FIELDS) {
+          if (ex) __stcs(ex + o, fx);
+          if (ey) __stcs(ey + o, fy);
+          if (ez) __stcs(ez + o, fz);
+        }
       }
     }
   }
@@ -596,12 +607,9 @@ int launch_assemble(const debye_desc* d, bool gauss, const OctGeom& g, int M, in
     return BPM_OK;
   }
   const dim3 grid((g.nxo + 127) / 128, g.nyo, g.nzo);
-  if (gauss)
-    debye_scatter_kernel<MIR_GAUSS><<<grid, 128, 0, s>>>(d->nx, d->ny, d->nz, g, M, Zo, e0, e1, I, trig, u, pex,
-                                                         pey, pez);
-  else
-    debye_scatter_kernel<MIR_STD><<<grid, 128, 0, s>>>(d->nx, d->ny, d->nz, g, M, Zo, e0, e1, I, trig, u, pex, pey,
-                                                       pez);
+  auto fn = gauss ? (fields ? debye_scatter_kernel<MIR_GAUSS, true> : debye_scatter_kernel<MIR_GAUSS, false>)
+                  : (fields ? debye_scatter_kernel<MIR_STD, true> : debye_scatter_kernel<MIR_STD, false>);
+  fn<<<grid, 128, 0, s>>>(d->nx, d->ny, d->nz, g, M, Zo, e0, e1, I, trig, u, pex, pey, pez);
   BPM_LAUNCH_CHECK("debye_scatter_kernel");
   return BPM_OK;
 }
