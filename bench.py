@@ -657,7 +657,8 @@ def profile_kernels():
     bpm_gb300.bpm_3d_batched((256, 128, 6), UNITS, lam=LAM, n0=N0, u0=make_u0(2, 256, 128, 1), dn=dn[:, :128].contiguous(),
                              return_field=False)
     dng = dn.clone().requires_grad_(True)
-    out = propagate_exit(dng, torch.from_numpy(make_u0(2, 256, 256, 2)).cuda(), (256, 256, 6), UNITS, LAM, N0,
+    # 10 fields: two row blocks per row in the summed-gradient adjoint, so the partial sum runs too
+    out = propagate_exit(dng, torch.from_numpy(make_u0(10, 256, 256, 2)).cuda(), (256, 256, 6), UNITS, LAM, N0,
                          ckpt_every=2)
     (out.abs() ** 2).sum().backward()
     bpm_gb300.bpm_3d_spheres((256, 256, 64), UNITS, points=[[12.8, 12.8, 3.2], [6.4, 19.2, 2.]], dn_outer=.05,
