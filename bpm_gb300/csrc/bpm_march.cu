@@ -1713,8 +1713,8 @@ struct RowK {
                          (int)W::ROW_SMEM);
   }
   static void prepare() {
-    static bool attr = false;
-    if (!attr) {
+    static PerDevice once;
+    once.get([] {
       if constexpr (WARP) {
         prepare_l<32>();
       }
@@ -1724,8 +1724,8 @@ struct RowK {
         cudaFuncSetAttribute(row_pass_kernel<N, true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                              (int)TileCfg<N>::SMEM);
       }
-      attr = true;
-    }
+      return 1;
+    });
   }
   // all fields of the group share the slice-z mask row: the precomputed mask, or one dn
   // volume (dn_batch_stride 0, or a group of one field); the row is staged with 16-byte
@@ -1842,12 +1842,12 @@ struct ColK {
                            cudaFuncAttributeMaxDynamicSharedMemorySize, (int)split_smem<L>());
   }
   static void prepare() {
-    static bool attr = false;
-    if (!attr) {
+    static PerDevice once;
+    once.get([] {
       if constexpr (TILE) cudaFuncSetAttribute(fn(), cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem());
       if constexpr (SPLIT) prepare_l<32>();
-      attr = true;
-    }
+      return 1;
+    });
   }
   template <int L>
   static int launch_split(dim3 g, cudaStream_t s, const ColParams& p) {
@@ -1908,8 +1908,8 @@ struct ColK {
 // field. state: -1 not checked yet, 0 this cluster size cannot be launched here, 1 ready
 template <int N>
 struct FusedK {
-  static int& state(int cl) {
-    static int st[17] = {-1, -1, -1, -1, -1, -1, -1, -1, -1, -1, -1, -1, -1, -1, -1, -1, -1};
+  static PerDevice& state(int cl) {
+    static PerDevice st[17];
     return st[cl];
   }
   static cudaLaunchConfig_t config(dim3 g, int cl, cudaStream_t s, cudaLaunchAttribute* at, bool pdl) {
@@ -1930,8 +1930,7 @@ struct FusedK {
   }
   // the kernel fits and clusters of `cl` blocks can be co-scheduled on this device
   static bool ready(int cl) {
-    int& st = state(cl);
-    if (st < 0) {
+    return state(cl).get([cl] {
       int ok = 0;
       if (cl > 8) cudaFuncSetAttribute(col_fused_kernel<N>, cudaFuncAttributeNonPortableClusterSizeAllowed, 1);
       if (cudaFuncSetAttribute(col_fused_kernel<N>, cudaFuncAttributeMaxDynamicSharedMemorySize,
@@ -1942,9 +1941,8 @@ struct FusedK {
         if (cudaOccupancyMaxActiveClusters(&clusters, col_fused_kernel<N>, &cfg) == cudaSuccess) ok = clusters > 0;
       }
       cudaGetLastError();
-      st = ok;
-    }
-    return st == 1;
+      return ok;
+    }) == 1;
   }
   static int launch(dim3 g, int cl, cudaStream_t s, const ColParams& p) {
     cudaLaunchAttribute at[2];
@@ -2316,13 +2314,10 @@ struct ClusterK {
     cfg.numAttrs = 1;
     return cfg;
   }
-  // -1: not checked yet; 0: no cluster of this shape fits on the device; 1: launchable
-  static int& state() {
-    static int st = -1;
-    return st;
-  }
+  // per device: 0 = no cluster of this shape fits, 1 = launchable
   static bool ready() {
-    if (state() < 0) {
+    static PerDevice state;
+    return state.get([] {
       int ok = 0;
       if (ClusterCfg<N>::C > 8)
         cudaFuncSetAttribute(cluster_march_kernel<N>, cudaFuncAttributeNonPortableClusterSizeAllowed, 1);
@@ -2335,9 +2330,8 @@ struct ClusterK {
           ok = clusters > 0;
       }
       cudaGetLastError();
-      state() = ok;
-    }
-    return state() == 1;
+      return ok;
+    }) == 1;
   }
   static int launch(const bpm_plan* pl, const bpm_request* r, void* ws, cudaStream_t s) {
     MarchCtx c = make_ctx(pl, r, ws, 0, r->batch);

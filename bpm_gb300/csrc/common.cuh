@@ -6,6 +6,7 @@
 #include <cuda_fp16.h>
 #include <stdint.h>
 #include <atomic>
+#include <mutex>
 #include <string>
 #include <utility>
 
@@ -114,6 +115,28 @@ inline cudaError_t launch_dep(void (*kernel)(KArgs...), dim3 grid, dim3 block, s
   cfg.numAttrs = 1;
   return cudaLaunchKernelEx(&cfg, kernel, std::forward<Args>(args)...);
 }
+
+// One-time setup per device: kernel attributes (dynamic shared-memory limits, cluster
+// sizes) and occupancy checks belong to the current device's context, so get(f) runs f the
+// first time it is called with each device current, under a lock (no caller on that device
+// launches before the setup is complete), and returns what f returned for that device.
+struct PerDevice {
+  static constexpr int kMax = 64;
+  std::mutex m;
+  int val[kMax] = {};
+  bool done[kMax] = {};
+  template <class F>
+  int get(F&& f) {
+    int dev = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= kMax) return f();
+    std::lock_guard<std::mutex> g(m);
+    if (!done[dev]) {
+      val[dev] = f();
+      done[dev] = true;
+    }
+    return val[dev];
+  }
+};
 
 inline bool is_pow2(int n) { return n > 0 && (n & (n - 1)) == 0; }
 inline bool aligned16(const void* p) { return ((uintptr_t)p & 15) == 0; }

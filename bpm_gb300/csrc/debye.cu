@@ -1314,11 +1314,11 @@ int run_octant(const debye_desc* d, bool gauss, double sig, float* u, void* ex, 
   BPM_LAUNCH_CHECK("debye_phase_kernel");
   debye_bessel_kernel<<<dim3((L.Mp + 127) / 128, L.T), 128, 0, s>>>(L.T, L.M, L.Mp, si, kr, wf, J);
   BPM_LAUNCH_CHECK("debye_bessel_kernel");
-  static bool attr = false;
-  if (!attr) {
+  static PerDevice attr;
+  attr.get([] {
     cudaFuncSetAttribute(debye_accum_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)ACC_SMEM);
-    attr = true;
-  }
+    return 1;
+  });
   // whole 32-plane tiles in the tile kernel; a single plane past them (the octant's
   // Nz/2 + 1 planes of a power-of-two shape) in the matrix-vector kernel; other
   // remainders stay a partial tile of the tile kernel
