@@ -2283,18 +2283,22 @@ int sink_copy(bpm_plan* pl, const bpm_request* r, const HostSink& h, int b0, int
 }
 
 // The whole-march cluster kernel serves square grids without scattering sums or
-// checkpoints. Measured on GB300 (one field, Nz 128): at 128^2 it beats the pass kernels
-// (one 128^3 weighted request 1.26 vs 1.51 ms), at 256^2 it does not (1.60 vs 1.38 ms per
-// march), so by default it takes N = 64 and 128. BPM_GB300_CLUSTER=1 extends it to 256,
-// =0 turns it off.
+// checkpoints. Measured on GB300, one field: at 64^2 it beats the pass kernels (Nz 64
+// weighted 0.40 vs 0.82 ms); at 128^2 the pass kernels are faster since a single field's row
+// pass stages its mask row (Nz 128 weighted 1.08 vs 1.14 ms, ignore 0.59 vs 0.81 ms, the
+// same bits), and at 256^2 too (Nz 256 ignore 1.47 vs 2.70 ms). So by default it takes
+// N = 64; BPM_GB300_CLUSTER=1 extends it to 128 and 256, =0 turns it off, and a side
+// length (64, 128 or 256) makes it the default up to that side.
 bool cluster_enabled(int n) {
-  static const int mode = [] {
+  static const int max_side = [] {
     const char* e = getenv("BPM_GB300_CLUSTER");
-    if (e && strcmp(e, "0") == 0) return 0;
-    if (e && strcmp(e, "1") == 0) return 2;
-    return 1;
+    if (!e) return 64;
+    if (strcmp(e, "0") == 0) return 0;
+    if (strcmp(e, "1") == 0) return 256;
+    const int v = atoi(e);
+    return v >= 64 ? v : 64;
   }();
-  return mode == 2 || (mode == 1 && n <= 128);
+  return n <= max_side;
 }
 
 template <int N>

@@ -110,7 +110,7 @@ typedef struct {
   int col_block;                 /* columns per block of the non-weighted column passes, 4, 8 or 16 */
   int cluster;                   /* whole-march cluster kernel (square 64..256 grids without
                                     scattering sums or checkpoints): 1 = use it, 2 = row/column
-                                    pass kernels (default: cluster at 64 and 128)               */
+                                    pass kernels (default: cluster at 64)                       */
   int col_fuse;                  /* weighted mode: 1 = one column pass per step (forward FFT,
                                     plane-wide sums across a thread-block cluster of the field's
                                     blocks, propagator, inverse FFT) where ny <= 512, nx <= 512
